@@ -1,0 +1,226 @@
+/*
+ * tsdf_c.h - C-ABI of the GB300 TSDF fusion engine (libtsdf_gb300.so).
+ *
+ * This is the drop-in boundary for the integration call of ros_tsdf
+ * (paths relative to that project):
+ *
+ *   tsdf::initGlobalVars(voxel_size, truncation_distance, max_weight,
+ *                        publish_distance_squared,
+ *                        garbage_collect_distance_squared)
+ *       tsdf_package/include/cuda/tsdf_handler.cuh:80-81
+ *       -> tsdf_params, given per map to tsdf_map_create()
+ *   tsdf::TSDFHandler::TSDFHandler() / TSDFContainer::TSDFContainer()
+ *       tsdf_handler.cu:954-958, tsdf_container.cu:11-19
+ *       -> tsdf_engine_create() + tsdf_map_create()
+ *   tsdf::TSDFHandler::processPointCloudAndUpdateVoxels(cloud, lidar_position,
+ *       publish_voxels_pos, publish_voxels_size, publish_voxels_data)
+ *       tsdf_handler.cuh:50-51, tsdf_handler.cu:974-1016
+ *       -> tsdf_integrate() (one scan) / tsdf_integrate_batch() (many maps)
+ *   tsdf::TSDFHandler::~TSDFHandler()  tsdf_handler.cu:960-964
+ *       -> tsdf_map_destroy() / tsdf_engine_destroy()
+ *   TSDFContainer::getCudaHashTable/getCudaBlockHeap tsdf_container.cuh:121-125
+ *       -> tsdf_dump_blocks() / tsdf_dump_free_list() / tsdf_dump_block_voxels()
+ *
+ * Differences from the reference surface, all deliberate:
+ *   - every call returns a tsdf_status instead of exit()/assert (the
+ *     reference's gpuErrchk exits the process, tsdf_handler.cu:14-22);
+ *   - parameters are per map, so one engine serves many independent maps
+ *     (the reference keeps them in __constant__ memory: one map per process);
+ *   - the publish count is output-only and the arrays are written only up to
+ *     min(count, pub_cap); *pub_count always holds the full count and
+ *     TSDF_WARN_PUBLISH_OVERFLOW flags truncation (the reference copies
+ *     PUBLISH_VOXELS_MAX_SIZE entries every call and keeps counting past it);
+ *   - points are float x,y,z at a caller-given stride: 12 bytes for packed
+ *     xyz, 16 bytes for pcl::PointXYZ.
+ *
+ * Threading: calls on one engine are serialized by the engine.  Each engine
+ * owns one CUDA device (tsdf_engine_cfg.device) and its own streams.
+ */
+#ifndef TSDF_C_H
+#define TSDF_C_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tsdf_status {
+  TSDF_OK = 0,
+  TSDF_ERR_INVALID_ARG = 1,       /* null pointer, bad size, unknown map id   */
+  TSDF_ERR_HEAP_FULL = 2,         /* admission refused / blocks dropped       */
+  TSDF_WARN_PUBLISH_OVERFLOW = 3, /* publish output truncated at pub_cap      */
+  TSDF_ERR_CUDA = 4,              /* a CUDA call failed; see tsdf_last_error  */
+  TSDF_ERR_CAPACITY = 5,          /* batch exceeds the engine's capacities    */
+  TSDF_ERR_SPIN_LIMIT = 6,        /* a bounded device-side wait gave up       */
+  TSDF_ERR_HASH_FULL = 7,         /* a map's hash table has no free entry     */
+  TSDF_ERR_BUSY = 8,              /* map already has a scan in flight         */
+  TSDF_ERR_NOT_READY = 9,         /* tsdf_poll: request still running         */
+  TSDF_ERR_BAD_POINTS = 10        /* warning: some points were skipped        */
+} tsdf_status;
+
+typedef struct tsdf_engine tsdf_engine;
+
+/* One voxel: Voxel{float sdf, weight} of tsdf_container.cuh:40-46. */
+typedef struct tsdf_voxel {
+  float sdf;
+  float weight;
+} tsdf_voxel;
+
+/* The five initGlobalVars parameters (tsdf_handler.cu:1289). */
+typedef struct tsdf_params {
+  float voxel_size;
+  float truncation_distance;
+  float max_weight;
+  float publish_distance_squared;
+  float garbage_collect_distance_squared;
+} tsdf_params;
+
+/* Engine capacities, fixed at creation.  Zero fields take defaults. */
+typedef struct tsdf_engine_cfg {
+  int device;               /* CUDA device ordinal                            */
+  int max_maps;             /* maps alive at once (default 64)                */
+  int64_t pool_blocks;      /* voxel blocks shared by all maps, 4 KiB each    */
+  int64_t max_batch_points; /* points per step over all maps (default 1<<20)  */
+  int64_t max_publish;      /* published voxels per step, staging (default 8M)*/
+  int bucket_size;          /* hash entries per bucket: 4, 8 or 16 (def. 8)   */
+  int ray_threads;          /* threads per CTA of the ray kernels (def. 256)  */
+  int ray_chunk;            /* points per work-queue item (default 256)       */
+  int max_routes;           /* per-point block routes of the voxel pass (16)  */
+  int lanes;                /* batches in flight at once (default 1, max 4)   */
+  int no_graphs;            /* 1: launch kernels directly; 0 (default): each
+                               step replays one captured CUDA graph           */
+} tsdf_engine_cfg;
+
+/* Per-scan counters; the field order matches the oracle's. */
+typedef struct tsdf_scan_stats {
+  int64_t n_points;            /* points given                               */
+  int64_t bad_points;          /* skipped: non-finite, zero ray, out of range*/
+  int64_t block_incidences;    /* cells visited by the block DDA             */
+  int64_t block_overflow;      /* block DDAs stopped by their cap            */
+  int64_t new_blocks;          /* blocks allocated                           */
+  int64_t heap_full_drops;     /* new blocks refused: heap full              */
+  int64_t voxel_updates;       /* voxel updates applied (U)                  */
+  int64_t voxel_overflow;      /* voxel DDAs stopped by their cap            */
+  int64_t route_overflow;      /* voxel updates beyond the route cap         */
+  int64_t missing_updates;     /* voxel updates whose block is absent        */
+  int64_t bad_local;           /* voxel updates with an out-of-block index   */
+  int64_t distinct_voxels;     /* distinct voxels updated (V)                */
+  int64_t blocks_touched;      /* distinct blocks updated (K)                */
+  int64_t published;           /* voxels published (full count)             */
+  int64_t published_blocks;    /* blocks that published at least one voxel   */
+  int64_t gc_blocks;           /* blocks garbage-collected                   */
+  int64_t block_count;         /* allocated blocks after the scan            */
+  int64_t alloc_blocks_before; /* allocated blocks before the scan (A)       */
+} tsdf_scan_stats;
+
+/* One scan of one map, for the batched and served entry points. */
+typedef struct tsdf_scan {
+  int map_id;
+  int stride_bytes;    /* 12 (packed xyz) or 16 (pcl::PointXYZ)              */
+  int64_t n_points;
+  const float* xyz;    /* host or device pointer; world frame                */
+  float origin[3];     /* sensor position in the same frame                  */
+} tsdf_scan;
+
+/* Where one scan's published voxels go.  Pointers may be host (pinned or
+ * pageable) or device memory; pinned and device buffers are written by the
+ * publish kernel directly. */
+typedef struct tsdf_scan_result {
+  float* pub_pos;          /* 3 floats per voxel (Vector3f)                  */
+  tsdf_voxel* pub_data;    /* sdf, weight per voxel                          */
+  int64_t pub_cap;         /* capacity of both arrays, in voxels             */
+  int64_t pub_count;       /* out: full count                                */
+  int status;              /* out: tsdf_status of this scan                  */
+  int reserved;
+  tsdf_scan_stats stats;   /* out                                            */
+} tsdf_scan_result;
+
+/* Occupancy of one map. */
+typedef struct tsdf_map_info {
+  int64_t heap_blocks;  /* capacity                                          */
+  int64_t block_count;  /* allocated                                         */
+  int64_t high_water;   /* highest slot ever used + 1                        */
+  int64_t hash_entries; /* hash table entries                                */
+  int64_t hash_used;    /* non-empty entries (live + deleted)                */
+  int64_t rehashes;     /* tombstone clean-ups so far                        */
+} tsdf_map_info;
+
+/* ---- engine ---------------------------------------------------------- */
+tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg, tsdf_engine** out);
+tsdf_status tsdf_engine_destroy(tsdf_engine* eng);
+/* Text of the last error on this engine (valid until the next call). */
+const char* tsdf_last_error(tsdf_engine* eng);
+/* Number of SMs of the engine's device, and the effective configuration. */
+tsdf_status tsdf_engine_get_cfg(tsdf_engine* eng, tsdf_engine_cfg* out, int* sm_count);
+
+/* ---- maps (replaces initGlobalVars + TSDFHandler()) ------------------- */
+/* Reserves heap_blocks blocks (plus a hash table of 2-4x that many entries)
+ * for a new map.  TSDF_ERR_HEAP_FULL when the pool cannot hold it: this is
+ * the admission control of the served mode. */
+tsdf_status tsdf_map_create(tsdf_engine* eng, const tsdf_params* params, int64_t heap_blocks, int* map_id);
+tsdf_status tsdf_map_destroy(tsdf_engine* eng, int map_id);
+tsdf_status tsdf_map_info_get(tsdf_engine* eng, int map_id, tsdf_map_info* out);
+
+/* ---- integration (replaces processPointCloudAndUpdateVoxels) ---------- */
+/* One scan of one map: allocate blocks, update voxels, publish the voxels of
+ * blocks within publish distance, garbage-collect blocks beyond the garbage
+ * distance.  Synchronous. */
+tsdf_status tsdf_integrate(tsdf_engine* eng, int map_id, const float* xyz, int64_t n_points, int stride_bytes,
+                           const float origin[3], float* pub_pos, tsdf_voxel* pub_data, int64_t pub_cap,
+                           int64_t* pub_count, tsdf_scan_stats* stats);
+/* One scan for each of n maps (distinct map ids) in one device step.
+ * Synchronous; per-scan status in results[i].status; returns the worst. */
+tsdf_status tsdf_integrate_batch(tsdf_engine* eng, int n, const tsdf_scan* scans, tsdf_scan_result* results);
+
+/* ---- served mode: continuous batching over many maps ------------------- */
+/* Queue one scan.  The engine's scheduler thread admits queued scans into the
+ * next device step as lanes free up; scans of different maps share a step,
+ * scans of one map run in submission order.  *ticket identifies it.  The
+ * caller keeps scan->xyz and *result alive until the request completes. */
+tsdf_status tsdf_submit(tsdf_engine* eng, const tsdf_scan* scan, tsdf_scan_result* result, uint64_t* ticket);
+/* TSDF_OK when done (result filled), TSDF_ERR_NOT_READY while running. */
+tsdf_status tsdf_poll(tsdf_engine* eng, uint64_t ticket);
+/* Wait up to timeout_ms (negative: no limit) for a ticket. */
+tsdf_status tsdf_wait(tsdf_engine* eng, uint64_t ticket, int64_t timeout_ms);
+/* Timestamps (ns, CLOCK_MONOTONIC) of a completed ticket: submitted,
+ * launched, completed.  Kept until tsdf_forget() or engine destroy. */
+tsdf_status tsdf_ticket_times(tsdf_engine* eng, uint64_t ticket, int64_t* t_submit, int64_t* t_launch,
+                              int64_t* t_done);
+tsdf_status tsdf_forget(tsdf_engine* eng, uint64_t ticket);
+
+/* ---- inspection for parity tests ------------------------------------- */
+/* Allocated blocks in ascending heap slot: integer block coordinates
+ * (3 ints each, floor(centre / block size)) and heap slot.  *count = total. */
+tsdf_status tsdf_dump_blocks(tsdf_engine* eng, int map_id, int32_t* kxyz, int32_t* slots, int64_t cap,
+                             int64_t* count);
+/* The map's free-block list (heap_blocks entries) and block count. */
+tsdf_status tsdf_dump_free_list(tsdf_engine* eng, int map_id, int32_t* out, int64_t cap, int64_t* block_count);
+/* The 512 voxels of one heap slot. */
+tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, tsdf_voxel* out512);
+
+/* ---- measurement helpers --------------------------------------------- */
+/* Record CUDA events around every pipeline stage of later steps. */
+tsdf_status tsdf_set_stage_timing(tsdf_engine* eng, int on);
+/* Stage names and accumulated milliseconds / launch counts since the last
+ * reset.  names may be NULL.  *n in: capacity, out: number of stages. */
+tsdf_status tsdf_stage_times(tsdf_engine* eng, const char** names, double* ms, int64_t* launches, int* n);
+tsdf_status tsdf_reset_stage_times(tsdf_engine* eng);
+/* Write a buffer larger than L2 on the engine's stream (between timed steps). */
+tsdf_status tsdf_flush_l2(tsdf_engine* eng);
+/* Kernel launches issued by this engine since creation. */
+int64_t tsdf_kernel_launches(tsdf_engine* eng);
+
+/* ---- memory helpers (pinned host / device buffers for callers) -------- */
+tsdf_status tsdf_host_alloc(void** p, int64_t bytes);
+tsdf_status tsdf_host_free(void* p);
+tsdf_status tsdf_device_alloc(tsdf_engine* eng, void** p, int64_t bytes);
+tsdf_status tsdf_device_free(tsdf_engine* eng, void* p);
+/* kind: 0 host->device, 1 device->host, 2 device->device; synchronous. */
+tsdf_status tsdf_copy(tsdf_engine* eng, void* dst, const void* src, int64_t bytes, int kind);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TSDF_C_H */

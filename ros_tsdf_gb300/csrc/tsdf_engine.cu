@@ -1,0 +1,1127 @@
+// Host side of the GB300 TSDF engine and its C-ABI (include/tsdf_c.h).
+//
+// One engine owns one device.  Global state (voxel block pool, per-slot keys,
+// free lists, hash tables, the map table) is shared by all maps; each map owns
+// a contiguous range of the block pool and of the hash pool, reserved at
+// tsdf_map_create (admission by free heap blocks).  A "lane" is a stream plus
+// the scratch of one in-flight step; the served mode keeps several lanes busy
+// at once with disjoint sets of maps.  Every step is the same sequence of
+// grid-fixed kernels reading its batch from device memory, so it is captured
+// once per lane as a CUDA graph and replayed for any batch.
+#include <cuda_runtime.h>
+#include <time.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/tsdf_c.h"
+#include "tsdf_internal.h"
+
+using namespace tsdfg;
+
+namespace {
+
+constexpr int kDefaultMaxMaps = 64;
+constexpr long long kDefaultPool = 1ll << 18;
+constexpr long long kDefaultBatchPoints = 1ll << 20;
+constexpr long long kDefaultPublish = 1ll << 23;
+constexpr int kMaxLanes = 4;
+constexpr long long kFlushBytes = 512ll << 20;
+
+const char* kStageNames[STAGE_COUNT] = {"init",        "ray_blocks", "alloc_order", "alloc", "ray_voxels",
+                                        "route_sort", "update",      "publish",     "gc"};
+
+int64_t now_ns() {
+  timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (int64_t)ts.tv_sec * 1000000000ll + ts.tv_nsec;
+}
+
+int bits_for(unsigned long long n) {  // bits to represent values 0..n-1
+  int b = 0;
+  while (b < 64 && (1ull << b) < n) ++b;
+  return b;
+}
+
+unsigned long long next_pow2(unsigned long long x) {
+  unsigned long long p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// First-fit allocator of [start, start+len) ranges of a pool.
+struct RangeAlloc {
+  std::map<long long, long long> free_;  // start -> len
+  void init(long long n) {
+    free_.clear();
+    if (n > 0) free_[0] = n;
+  }
+  long long alloc(long long n) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        long long s = it->first, l = it->second;
+        free_.erase(it);
+        if (l > n) free_[s + n] = l - n;
+        return s;
+      }
+    }
+    return -1;
+  }
+  void release(long long s, long long n) {
+    auto it = free_.emplace(s, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  long long largest() const {
+    long long b = 0;
+    for (auto& kv : free_) b = std::max(b, kv.second);
+    return b;
+  }
+};
+
+struct MapHost {
+  bool live = false;
+  tsdf_params params{};
+  MapDev dev{};
+  long long hash_entries = 0;
+  bool in_flight = false;
+  long long rehashes = 0;
+};
+
+struct Request {
+  uint64_t ticket;
+  tsdf_scan scan;
+  tsdf_scan_result* result;
+  int64_t t_submit = 0, t_launch = 0, t_done = 0;
+  bool done = false;
+};
+
+struct Lane {
+  cudaStream_t stream = nullptr;
+  Ctx ctx{};
+  // device scratch
+  BatchHdr* d_hdr = nullptr;
+  ItemDev* d_items = nullptr;
+  char* d_points = nullptr;
+  float* d_pub_pos = nullptr;
+  float2* d_pub_data = nullptr;
+  std::vector<void*> allocs;
+  // pinned host mirrors
+  char* h_desc = nullptr;       // BatchHdr + ItemDev[max_maps]
+  long long* h_stats = nullptr; // [max_maps][ST_COUNT]
+  LaneCounters* h_ctr = nullptr;
+  MapCounters* h_mctr = nullptr;
+  // graphs keyed by (rank_passes, rec_passes, timing)
+  std::map<int, cudaGraphExec_t> graphs;
+  std::map<int, long long> graph_launches;
+  cudaEvent_t ev_stage[STAGE_COUNT + 1] = {};
+  cudaEvent_t ev_done = nullptr;
+  // the batch currently in flight (served mode)
+  bool busy = false;
+  bool timed = false;
+  std::vector<std::shared_ptr<Request>> reqs;
+  struct Staged {
+    int item;
+    long long off;
+  };
+  std::vector<Staged> staged;
+  std::vector<int> maps;
+};
+
+}  // namespace
+
+struct tsdf_engine {
+  tsdf_engine_cfg cfg{};
+  int device = 0;
+  int sm_count = 0;
+  std::recursive_mutex mu;
+  std::string err;
+  // global device state
+  float2* voxels = nullptr;
+  unsigned long long* slot_key = nullptr;
+  int* nnz = nullptr;
+  int* free_list = nullptr;
+  HEntry* hash = nullptr;
+  MapDev* d_maps = nullptr;
+  MapCounters* d_mctr = nullptr;
+  long long hash_pool = 0;
+  void* flush_buf = nullptr;
+  int* d_tmp = nullptr;  // rehash scratch (2 ints)
+  RangeAlloc heap_ranges, hash_ranges;
+  std::vector<MapHost> maps;
+  Lane lanes[kMaxLanes];
+  int n_lanes = 1;
+  // measurement
+  bool stage_timing = false;
+  double stage_ms[STAGE_COUNT] = {};
+  long long stage_launches[STAGE_COUNT] = {};
+  std::atomic<long long> launches{0};
+  // served mode
+  std::thread sched;
+  bool sched_running = false;
+  bool sched_stop = false;
+  std::condition_variable_any cv;
+  std::deque<std::shared_ptr<Request>> queue;
+  std::unordered_map<uint64_t, std::shared_ptr<Request>> tickets;
+  uint64_t next_ticket = 1;
+};
+
+namespace {
+
+tsdf_status fail(tsdf_engine* e, tsdf_status st, const std::string& msg) {
+  e->err = msg;
+  return st;
+}
+
+#define CK(call)                                                                                     \
+  do {                                                                                               \
+    cudaError_t _e = (call);                                                                         \
+    if (_e != cudaSuccess)                                                                           \
+      return fail(eng, TSDF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));           \
+  } while (0)
+
+template <class T>
+tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>* track) {
+  void* q = nullptr;
+  size_t bytes = (size_t)std::max<long long>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess)
+    return fail(eng, TSDF_ERR_CUDA, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+  *p = (T*)q;
+  if (track) track->push_back(q);
+  return TSDF_OK;
+}
+
+#define TRY(x)                          \
+  do {                                  \
+    tsdf_status _s = (x);               \
+    if (_s != TSDF_OK) return _s;       \
+  } while (0)
+
+LaunchCfg launch_cfg(tsdf_engine* eng, int rank_passes, int rec_passes) {
+  LaunchCfg lc;
+  lc.sm_count = eng->sm_count;
+  lc.bucket_size = eng->cfg.bucket_size;
+  lc.ray_threads = eng->cfg.ray_threads;
+  lc.rank_passes = rank_passes;
+  lc.rec_passes = rec_passes;
+  return lc;
+}
+
+tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
+  const tsdf_engine_cfg& c = eng->cfg;
+  CK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+  for (int i = 0; i <= STAGE_COUNT; ++i) CK(cudaEventCreate(&L.ev_stage[i]));
+  CK(cudaEventCreateWithFlags(&L.ev_done, cudaEventDisableTiming));
+  const long long npts = c.max_batch_points;
+  const long long rank_cap = npts * c.max_routes;
+  const long long rec_cap = npts * c.max_routes;
+  const long long enum_cap = c.pool_blocks;
+  auto tiles = [](long long n, long long t) { return (int)((n + t - 1) / t); };
+  const int max_tiles_rank = tiles(rank_cap, 2048);
+  const int max_tiles_rec = tiles(rec_cap, 2048);
+  const int max_tiles_scan = tiles(std::max(rec_cap, enum_cap), 2048);
+  Ctx& x = L.ctx;
+  x.voxels = eng->voxels;
+  x.slot_key = eng->slot_key;
+  x.nnz = eng->nnz;
+  x.free_list = eng->free_list;
+  x.hash = eng->hash;
+  x.maps = eng->d_maps;
+  x.mctr = eng->d_mctr;
+  std::vector<void*>* tr = &L.allocs;
+  TRY(dalloc(eng, &L.d_hdr, 1, tr));
+  TRY(dalloc(eng, &L.d_items, c.max_maps, tr));
+  x.hdr = L.d_hdr;
+  x.items = L.d_items;
+  TRY(dalloc(eng, &x.item_stats, (long long)c.max_maps * ST_COUNT, tr));
+  TRY(dalloc(eng, &x.item_i, (long long)c.max_maps * II_COUNT, tr));
+  TRY(dalloc(eng, &x.ctr, 1, tr));
+  TRY(dalloc(eng, &x.newlist, rank_cap, tr));
+  for (int i = 0; i < 2; ++i) {
+    TRY(dalloc(eng, &x.rank_key[i], rank_cap, tr));
+    TRY(dalloc(eng, &x.rank_val[i], rank_cap, tr));
+    TRY(dalloc(eng, &x.rec_key[i], rec_cap, tr));
+    TRY(dalloc(eng, &x.rec_val[i], rec_cap, tr));
+  }
+  TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
+  TRY(dalloc(eng, &x.digit_tot, 256, tr));
+  TRY(dalloc(eng, &x.tile_sums, max_tiles_scan + 1, tr));
+  TRY(dalloc(eng, &x.seg_start, rec_cap, tr));
+  TRY(dalloc(eng, &x.enum_cnt, enum_cap, tr));
+  TRY(dalloc(eng, &x.enum_gc, enum_cap, tr));
+  TRY(dalloc(eng, &x.pub_prefix, enum_cap, tr));
+  TRY(dalloc(eng, &x.gc_prefix, enum_cap, tr));
+  x.seg_prefix = nullptr;
+  x.max_tiles_rank = max_tiles_rank;
+  x.max_tiles_rec = max_tiles_rec;
+  x.max_tiles_scan = max_tiles_scan;
+  x.ray_chunk = c.ray_chunk;
+  x.rank_cap = rank_cap;
+  x.rec_cap = rec_cap;
+  x.enum_cap = enum_cap;
+  TRY(dalloc(eng, &L.d_points, npts * 16, tr));
+  TRY(dalloc(eng, &L.d_pub_pos, c.max_publish * 3, tr));
+  TRY(dalloc(eng, &L.d_pub_data, c.max_publish, tr));
+  CK(cudaMallocHost(&L.h_desc, sizeof(BatchHdr) + sizeof(ItemDev) * c.max_maps));
+  CK(cudaMallocHost(&L.h_stats, sizeof(long long) * ST_COUNT * c.max_maps));
+  CK(cudaMallocHost(&L.h_ctr, sizeof(LaneCounters)));
+  CK(cudaMallocHost(&L.h_mctr, sizeof(MapCounters) * c.max_maps));
+  return TSDF_OK;
+}
+
+void lane_free(Lane& L) {
+  for (auto& kv : L.graphs) cudaGraphExecDestroy(kv.second);
+  L.graphs.clear();
+  for (void* p : L.allocs) cudaFree(p);
+  L.allocs.clear();
+  if (L.h_desc) cudaFreeHost(L.h_desc);
+  if (L.h_stats) cudaFreeHost(L.h_stats);
+  if (L.h_ctr) cudaFreeHost(L.h_ctr);
+  if (L.h_mctr) cudaFreeHost(L.h_mctr);
+  for (int i = 0; i <= STAGE_COUNT; ++i)
+    if (L.ev_stage[i]) cudaEventDestroy(L.ev_stage[i]);
+  if (L.ev_done) cudaEventDestroy(L.ev_done);
+  if (L.stream) cudaStreamDestroy(L.stream);
+  L = Lane();
+}
+
+// Enqueue the pipeline of one step on the lane's stream (used directly or
+// inside a graph capture).  Returns the number of kernel launches.
+long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool timed) {
+  LaunchCfg lc = launch_cfg(eng, rank_passes, rec_passes);
+  long long n = 0;
+  using Fn = void (*)(const Ctx&, const LaunchCfg&, cudaStream_t, long long*);
+  const Fn stages[STAGE_COUNT] = {stage_init,       stage_ray_blocks,  stage_alloc_order,
+                                  stage_alloc,      stage_ray_voxels,  stage_route_sort,
+                                  stage_update,     stage_publish,     stage_gc};
+  for (int i = 0; i < STAGE_COUNT; ++i) {
+    if (timed) cudaEventRecordWithFlags(L.ev_stage[i], L.stream, cudaEventRecordExternal);
+    stages[i](L.ctx, lc, L.stream, &n);
+  }
+  if (timed) cudaEventRecordWithFlags(L.ev_stage[STAGE_COUNT], L.stream, cudaEventRecordExternal);
+  return n;
+}
+
+tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes) {
+  const bool timed = eng->stage_timing;
+  L.timed = timed;
+  if (eng->cfg.no_graphs) {
+    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, timed);
+    CK(cudaGetLastError());
+    return TSDF_OK;
+  }
+  const int key = rank_passes * 100 + rec_passes * 10 + (timed ? 1 : 0);
+  auto it = L.graphs.find(key);
+  if (it == L.graphs.end()) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
+    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, timed);
+    cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
+    if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    cudaGraphExec_t ex = nullptr;
+    ce = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    it = L.graphs.emplace(key, ex).first;
+    L.graph_launches[key] = n;
+  }
+  CK(cudaGraphLaunch(it->second, L.stream));
+  eng->launches += L.graph_launches[key];
+  return TSDF_OK;
+}
+
+bool device_accessible(const void* p, const void** dev_ptr) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+    *dev_ptr = a.devicePointer ? a.devicePointer : p;
+    return true;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    *dev_ptr = a.devicePointer;
+    return true;
+  }
+  return false;
+}
+
+// Validate a batch and enqueue it on lane L (asynchronous).  On success the
+// lane is busy until finish_batch.
+tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans, tsdf_scan_result* res) {
+  const tsdf_engine_cfg& c = eng->cfg;
+  if (n <= 0 || n > c.max_maps) return fail(eng, TSDF_ERR_INVALID_ARG, "batch size out of range");
+  BatchHdr* hdr = reinterpret_cast<BatchHdr*>(L.h_desc);
+  ItemDev* items = reinterpret_cast<ItemDev*>(L.h_desc + sizeof(BatchHdr));
+  std::memset(hdr, 0, sizeof(BatchHdr));
+  long long total = 0, bytes = 0, pub_staged = 0;
+  long long lo = -1, hi = 0;
+  int rank_stride = 1, rec_stride = 1;
+  L.staged.clear();
+  L.maps.clear();
+  for (int i = 0; i < n; ++i) {
+    const tsdf_scan& s = scans[i];
+    if (s.map_id < 0 || s.map_id >= (int)eng->maps.size() || !eng->maps[s.map_id].live)
+      return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id " + std::to_string(s.map_id));
+    if (s.n_points < 0 || (s.n_points > 0 && !s.xyz)) return fail(eng, TSDF_ERR_INVALID_ARG, "bad point array");
+    if (s.stride_bytes < 12 || (s.stride_bytes & 3)) return fail(eng, TSDF_ERR_INVALID_ARG, "stride must be >= 12, multiple of 4");
+    if (!res[i].pub_pos || !res[i].pub_data) {
+      if (res[i].pub_cap > 0) return fail(eng, TSDF_ERR_INVALID_ARG, "null publish arrays");
+    }
+    for (int j = 0; j < i; ++j)
+      if (scans[j].map_id == s.map_id) return fail(eng, TSDF_ERR_INVALID_ARG, "map appears twice in one batch");
+    MapHost& m = eng->maps[s.map_id];
+    ItemDev& it = items[i];
+    std::memset(&it, 0, sizeof(it));
+    it.n = s.n_points;
+    it.point_base = total;
+    it.ox = s.origin[0], it.oy = s.origin[1], it.oz = s.origin[2];
+    it.stride = s.stride_bytes;
+    it.map = s.map_id;
+    total += s.n_points;
+    rank_stride = std::max(rank_stride, m.dev.amax);
+    rec_stride = std::max(rec_stride, m.dev.rmax);
+    lo = lo < 0 ? m.dev.heap_base : std::min(lo, m.dev.heap_base);
+    hi = std::max(hi, m.dev.heap_base + m.dev.heap_cap);
+  }
+  if (total > c.max_batch_points)
+    return fail(eng, TSDF_ERR_CAPACITY, "batch has " + std::to_string(total) + " points; capacity " +
+                                            std::to_string(c.max_batch_points));
+  // inputs
+  for (int i = 0; i < n; ++i) {
+    const tsdf_scan& s = scans[i];
+    ItemDev& it = items[i];
+    const void* dp = nullptr;
+    if (s.n_points == 0) {
+      it.pts = L.d_points;
+    } else if (device_accessible(s.xyz, &dp)) {
+      it.pts = (const char*)dp;
+    } else {
+      long long nb = s.n_points * (long long)s.stride_bytes;
+      if (bytes + nb > c.max_batch_points * 16) return fail(eng, TSDF_ERR_CAPACITY, "point staging full");
+      CK(cudaMemcpyAsync(L.d_points + bytes, s.xyz, nb, cudaMemcpyHostToDevice, L.stream));
+      it.pts = L.d_points + bytes;
+      bytes += (nb + 15) & ~15ll;
+    }
+    // outputs
+    const void* pp = nullptr;
+    const void* pd = nullptr;
+    it.out_cap = std::max<long long>(res[i].pub_cap, 0);
+    if (it.out_cap > 0 && device_accessible(res[i].pub_pos, &pp) && device_accessible(res[i].pub_data, &pd)) {
+      it.out_pos = (float*)pp;
+      it.out_data = (float2*)pd;
+    } else {
+      long long cap = it.out_cap;
+      if (pub_staged + cap > c.max_publish)
+        return fail(eng, TSDF_ERR_CAPACITY, "publish staging full (raise max_publish or pass pinned buffers)");
+      it.out_pos = L.d_pub_pos + 3 * pub_staged;
+      it.out_data = L.d_pub_data + pub_staged;
+      if (cap > 0) L.staged.push_back({i, pub_staged});
+      pub_staged += cap;
+    }
+  }
+  hdr->n_items = n;
+  hdr->rank_stride = rank_stride;
+  hdr->rec_stride = rec_stride;
+  hdr->total_points = total;
+  hdr->rec_total = total * rec_stride;
+  hdr->key_lo = lo;
+  hdr->rec_key_limit = kRecSentinel;
+  const unsigned long long rank_range = (unsigned long long)std::max<long long>(total, 1) * rank_stride;
+  if (rank_range >= 0xFFFFFFFFull) return fail(eng, TSDF_ERR_CAPACITY, "rank range exceeds 32 bits");
+  const int rank_passes = std::max(1, (bits_for(rank_range) + kRadixBits - 1) / kRadixBits);
+  const int rec_passes = std::max(1, (bits_for((unsigned long long)(hi - lo)) + kRadixBits - 1) / kRadixBits);
+  CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr), cudaMemcpyHostToDevice, L.stream));
+  CK(cudaMemcpyAsync(L.d_items, items, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
+  TRY(launch_pipeline(eng, L, rank_passes, rec_passes));
+  CK(cudaMemcpyAsync(L.h_stats, L.ctx.item_stats, sizeof(long long) * ST_COUNT * n, cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaMemcpyAsync(L.h_ctr, L.ctx.ctr, sizeof(LaneCounters), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaMemcpyAsync(L.h_mctr, eng->d_mctr, sizeof(MapCounters) * eng->maps.size(), cudaMemcpyDeviceToHost,
+                     L.stream));
+  CK(cudaEventRecord(L.ev_done, L.stream));
+  for (int i = 0; i < n; ++i) {
+    eng->maps[scans[i].map_id].in_flight = true;
+    L.maps.push_back(scans[i].map_id);
+  }
+  L.busy = true;
+  return TSDF_OK;
+}
+
+tsdf_status maybe_rehash(tsdf_engine* eng, int map_id, Lane& L);
+
+// Wait for lane L's batch and deliver its results.
+tsdf_status finish_batch(tsdf_engine* eng, Lane& L, int n, tsdf_scan_result* res) {
+  CK(cudaEventSynchronize(L.ev_done));
+  if (L.timed) {
+    for (int i = 0; i < STAGE_COUNT; ++i) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, L.ev_stage[i], L.ev_stage[i + 1]) == cudaSuccess) {
+        eng->stage_ms[i] += ms;
+        eng->stage_launches[i] += 1;
+      }
+    }
+    cudaGetLastError();
+  }
+  for (int m : L.maps) eng->maps[m].in_flight = false;
+  L.busy = false;
+  tsdf_status worst = TSDF_OK;
+  if (L.h_ctr->error) {
+    std::string what;
+    if (L.h_ctr->error & ERR_HASH_FULL) what += " hash table full;";
+    if (L.h_ctr->error & ERR_CAPACITY) what += " scratch capacity exceeded;";
+    if (L.h_ctr->error & ERR_SPIN) what += " bounded wait gave up;";
+    eng->err = "device step error:" + what;
+    worst = (L.h_ctr->error & ERR_HASH_FULL) ? TSDF_ERR_HASH_FULL : TSDF_ERR_CAPACITY;
+  }
+  std::vector<long long> counts(n);
+  for (int i = 0; i < n; ++i) {
+    const long long* st = L.h_stats + (long long)i * ST_COUNT;
+    std::memcpy(&res[i].stats, st, sizeof(tsdf_scan_stats));
+    res[i].pub_count = st[ST_PUB];
+    counts[i] = st[ST_PUB];
+    int s = TSDF_OK;
+    if (worst != TSDF_OK)
+      s = worst;
+    else if (st[ST_PUB] > res[i].pub_cap)
+      s = TSDF_WARN_PUBLISH_OVERFLOW;
+    else if (st[ST_HEAPFULL] > 0)
+      s = TSDF_ERR_HEAP_FULL;
+    else if (st[ST_BAD] > 0)
+      s = TSDF_ERR_BAD_POINTS;
+    res[i].status = s;
+  }
+  for (const auto& sg : L.staged) {
+    long long k = std::min<long long>(counts[sg.item], res[sg.item].pub_cap);
+    if (k <= 0) continue;
+    CK(cudaMemcpyAsync(res[sg.item].pub_pos, L.d_pub_pos + 3 * sg.off, sizeof(float) * 3 * k, cudaMemcpyDeviceToHost,
+                       L.stream));
+    CK(cudaMemcpyAsync(res[sg.item].pub_data, L.d_pub_data + sg.off, sizeof(float2) * k, cudaMemcpyDeviceToHost,
+                       L.stream));
+  }
+  if (!L.staged.empty()) CK(cudaStreamSynchronize(L.stream));
+  for (int m : L.maps) TRY(maybe_rehash(eng, m, L));
+  if (worst != TSDF_OK) return worst;
+  int w = TSDF_OK;
+  for (int i = 0; i < n; ++i) {
+    int s = res[i].status;
+    if (s == TSDF_ERR_HEAP_FULL || (w != TSDF_ERR_HEAP_FULL && s != TSDF_OK)) w = s;
+  }
+  return (tsdf_status)w;
+}
+
+// Rebuild a map's hash table when tombstones crowd it (more than half of the
+// entries non-empty).  Only between steps, with the map idle.
+tsdf_status maybe_rehash(tsdf_engine* eng, int map_id, Lane& L) {
+  MapHost& m = eng->maps[map_id];
+  const MapCounters& mc = L.h_mctr[map_id];
+  if ((long long)mc.hash_used * 2 <= m.hash_entries) return TSDF_OK;
+  const int G = eng->cfg.bucket_size;
+  CK(cudaMemsetAsync(eng->d_tmp + 1, 0, sizeof(int), L.stream));
+  launch_map_rehash(L.ctx, map_id, G, m.dev.heap_base, mc.hw, m.dev.hash_base, m.hash_entries, m.dev.hash_mask,
+                    eng->d_tmp, eng->d_tmp + 1, L.stream);
+  CK(cudaMemcpyAsync(&eng->d_mctr[map_id].hash_used, eng->d_tmp, sizeof(int), cudaMemcpyDeviceToDevice, L.stream));
+  int host[2] = {0, 0};
+  CK(cudaMemcpyAsync(host, eng->d_tmp, sizeof(int) * 2, cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  m.rehashes++;
+  if (host[1]) return fail(eng, TSDF_ERR_HASH_FULL, "rehash: table full");
+  return TSDF_OK;
+}
+
+tsdf_status run_batch_sync(tsdf_engine* eng, int n, const tsdf_scan* scans, tsdf_scan_result* res) {
+  Lane& L = eng->lanes[0];
+  for (int i = 0; i < n; ++i) {
+    if (scans[i].map_id >= 0 && scans[i].map_id < (int)eng->maps.size() && eng->maps[scans[i].map_id].in_flight)
+      return fail(eng, TSDF_ERR_BUSY, "map has a scan in flight");
+  }
+  tsdf_status s = start_batch(eng, L, n, scans, res);
+  if (s != TSDF_OK) {
+    if (L.busy) finish_batch(eng, L, n, res);
+    return s;
+  }
+  return finish_batch(eng, L, n, res);
+}
+
+// ---------------------------------------------------------------------------
+// served mode: a scheduler thread forms batches from queued scans (one per
+// map, FIFO per map), launches each on a free lane, and completes lanes as
+// their steps finish.  Requests that arrive while lanes are busy join the
+// next step on the next free lane (continuous batching).
+void complete_lane(tsdf_engine* eng, Lane& L) {
+  std::vector<tsdf_scan_result> tmp(L.reqs.size());
+  for (size_t i = 0; i < L.reqs.size(); ++i) tmp[i] = *L.reqs[i]->result;
+  finish_batch(eng, L, (int)L.reqs.size(), tmp.data());
+  int64_t t = now_ns();
+  for (size_t i = 0; i < L.reqs.size(); ++i) {
+    *L.reqs[i]->result = tmp[i];
+    L.reqs[i]->t_done = t;
+    L.reqs[i]->done = true;
+  }
+  L.reqs.clear();
+}
+
+void scheduler_loop(tsdf_engine* eng) {
+  cudaSetDevice(eng->device);
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  while (true) {
+    bool progressed = false;
+    // complete finished lanes
+    for (int li = 0; li < eng->n_lanes; ++li) {
+      Lane& L = eng->lanes[li];
+      if (L.busy && !L.reqs.empty() && cudaEventQuery(L.ev_done) == cudaSuccess) {
+        complete_lane(eng, L);
+        progressed = true;
+      }
+    }
+    if (progressed) eng->cv.notify_all();
+    // launch on free lanes
+    for (int li = 0; li < eng->n_lanes && !eng->queue.empty(); ++li) {
+      Lane& L = eng->lanes[li];
+      if (L.busy) continue;
+      std::vector<std::shared_ptr<Request>> pick;
+      std::vector<int> used;
+      long long pts = 0;
+      for (auto it = eng->queue.begin(); it != eng->queue.end();) {
+        auto& r = *it;
+        int m = r->scan.map_id;
+        bool seen = std::find(used.begin(), used.end(), m) != used.end();
+        bool busy = m >= 0 && m < (int)eng->maps.size() && eng->maps[m].in_flight;
+        if (seen || busy) {
+          used.push_back(m);  // keep per-map FIFO order
+          ++it;
+          continue;
+        }
+        if ((int)pick.size() >= eng->cfg.max_maps || pts + r->scan.n_points > eng->cfg.max_batch_points) break;
+        pts += r->scan.n_points;
+        used.push_back(m);
+        pick.push_back(r);
+        it = eng->queue.erase(it);
+      }
+      if (pick.empty()) break;
+      std::vector<tsdf_scan> sc(pick.size());
+      std::vector<tsdf_scan_result> rs(pick.size());
+      for (size_t i = 0; i < pick.size(); ++i) {
+        sc[i] = pick[i]->scan;
+        rs[i] = *pick[i]->result;
+      }
+      int64_t t = now_ns();
+      tsdf_status st = start_batch(eng, L, (int)pick.size(), sc.data(), rs.data());
+      if (st != TSDF_OK) {
+        if (L.busy) {
+          finish_batch(eng, L, (int)pick.size(), rs.data());
+        }
+        for (auto& r : pick) {
+          r->result->status = st;
+          r->t_launch = t;
+          r->t_done = now_ns();
+          r->done = true;
+        }
+        eng->cv.notify_all();
+        continue;
+      }
+      for (auto& r : pick) r->t_launch = t;
+      L.reqs = pick;
+      progressed = true;
+    }
+    if (eng->sched_stop) {
+      bool any = false;
+      for (int li = 0; li < eng->n_lanes; ++li) any |= eng->lanes[li].busy && !eng->lanes[li].reqs.empty();
+      if (!any && eng->queue.empty()) break;
+    }
+    if (!progressed) {
+      bool any_busy = false;
+      for (int li = 0; li < eng->n_lanes; ++li) any_busy |= eng->lanes[li].busy;
+      if (any_busy)
+        eng->cv.wait_for(lk, std::chrono::microseconds(20));
+      else
+        eng->cv.wait_for(lk, std::chrono::milliseconds(2));
+    }
+  }
+}
+
+void ensure_scheduler(tsdf_engine* eng) {
+  if (eng->sched_running) return;
+  eng->sched_stop = false;
+  eng->sched_running = true;
+  eng->sched = std::thread(scheduler_loop, eng);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+extern "C" {
+
+tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out) {
+  if (!out) return TSDF_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::unique_ptr<tsdf_engine> e(new tsdf_engine());
+  tsdf_engine* eng = e.get();
+  tsdf_engine_cfg c{};
+  if (cfg_in) c = *cfg_in;
+  if (c.max_maps <= 0) c.max_maps = kDefaultMaxMaps;
+  if (c.max_maps > 1024) return TSDF_ERR_INVALID_ARG;
+  if (c.pool_blocks <= 0) c.pool_blocks = kDefaultPool;
+  if (c.max_batch_points <= 0) c.max_batch_points = kDefaultBatchPoints;
+  if (c.max_publish <= 0) c.max_publish = kDefaultPublish;
+  if (c.bucket_size <= 0) c.bucket_size = 8;
+  if (c.bucket_size != 4 && c.bucket_size != 8 && c.bucket_size != 16) return TSDF_ERR_INVALID_ARG;
+  if (c.ray_threads <= 0) c.ray_threads = 256;
+  if (c.ray_threads != 64 && c.ray_threads != 128 && c.ray_threads != 256) return TSDF_ERR_INVALID_ARG;
+  if (c.ray_chunk <= 0) c.ray_chunk = 256;
+  c.ray_chunk = ((c.ray_chunk + 31) / 32) * 32;
+  if (c.max_routes <= 0) c.max_routes = 16;
+  if (c.lanes <= 0) c.lanes = 1;
+  if (c.lanes > kMaxLanes) c.lanes = kMaxLanes;
+  if (c.pool_blocks >= (1ll << 31) || c.max_batch_points * (long long)c.max_routes >= (1ll << 31))
+    return TSDF_ERR_INVALID_ARG;
+  eng->cfg = c;
+  eng->device = c.device;
+  eng->n_lanes = c.lanes;
+  if (cudaSetDevice(c.device) != cudaSuccess) return TSDF_ERR_CUDA;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess) return TSDF_ERR_CUDA;
+  eng->sm_count = sms;
+  // global state
+  eng->hash_pool = c.pool_blocks * 4 + 4096;
+  if (dalloc(eng, &eng->voxels, c.pool_blocks * kVoxelsPerBlock, nullptr) != TSDF_OK ||
+      dalloc(eng, &eng->slot_key, c.pool_blocks, nullptr) != TSDF_OK ||
+      dalloc(eng, &eng->nnz, c.pool_blocks, nullptr) != TSDF_OK ||
+      dalloc(eng, &eng->free_list, c.pool_blocks, nullptr) != TSDF_OK ||
+      dalloc(eng, &eng->hash, eng->hash_pool, nullptr) != TSDF_OK ||
+      dalloc(eng, &eng->d_maps, c.max_maps, nullptr) != TSDF_OK ||
+      dalloc(eng, &eng->d_mctr, c.max_maps, nullptr) != TSDF_OK || dalloc(eng, &eng->d_tmp, 2, nullptr) != TSDF_OK) {
+    tsdf_engine_destroy(e.release());
+    return TSDF_ERR_CUDA;
+  }
+  cudaMemset(eng->slot_key, 0xFF, sizeof(unsigned long long) * c.pool_blocks);
+  cudaMemset(eng->nnz, 0, sizeof(int) * c.pool_blocks);
+  cudaMemset(eng->hash, 0xFF, sizeof(HEntry) * eng->hash_pool);
+  cudaMemset(eng->d_maps, 0, sizeof(MapDev) * c.max_maps);
+  cudaMemset(eng->d_mctr, 0, sizeof(MapCounters) * c.max_maps);
+  eng->heap_ranges.init(c.pool_blocks);
+  eng->hash_ranges.init(eng->hash_pool);
+  eng->maps.resize(c.max_maps);
+  for (int i = 0; i < eng->n_lanes; ++i) {
+    if (lane_init(eng, eng->lanes[i]) != TSDF_OK) {
+      std::string msg = eng->err;
+      tsdf_engine_destroy(e.release());
+      return TSDF_ERR_CUDA;
+    }
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    tsdf_engine_destroy(e.release());
+    return TSDF_ERR_CUDA;
+  }
+  *out = e.release();
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_engine_destroy(tsdf_engine* eng) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  {
+    std::unique_lock<std::recursive_mutex> lk(eng->mu);
+    if (eng->sched_running) {
+      eng->sched_stop = true;
+      eng->cv.notify_all();
+    }
+  }
+  if (eng->sched.joinable()) eng->sched.join();
+  cudaSetDevice(eng->device);
+  cudaDeviceSynchronize();
+  for (int i = 0; i < kMaxLanes; ++i) lane_free(eng->lanes[i]);
+  cudaFree(eng->voxels);
+  cudaFree(eng->slot_key);
+  cudaFree(eng->nnz);
+  cudaFree(eng->free_list);
+  cudaFree(eng->hash);
+  cudaFree(eng->d_maps);
+  cudaFree(eng->d_mctr);
+  cudaFree(eng->d_tmp);
+  if (eng->flush_buf) cudaFree(eng->flush_buf);
+  delete eng;
+  return TSDF_OK;
+}
+
+const char* tsdf_last_error(tsdf_engine* eng) { return eng ? eng->err.c_str() : "null engine"; }
+
+tsdf_status tsdf_engine_get_cfg(tsdf_engine* eng, tsdf_engine_cfg* out, int* sm_count) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  if (out) *out = eng->cfg;
+  if (sm_count) *sm_count = eng->sm_count;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_map_create(tsdf_engine* eng, const tsdf_params* p, int64_t heap_blocks, int* map_id) {
+  if (!eng || !p || !map_id) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  if (!(p->voxel_size > 0.0f) || !(p->truncation_distance > 0.0f) || !(p->max_weight > 0.0f) ||
+      !std::isfinite(p->voxel_size) || !std::isfinite(p->truncation_distance))
+    return fail(eng, TSDF_ERR_INVALID_ARG, "voxel_size, truncation_distance and max_weight must be positive");
+  if (heap_blocks <= 0 || heap_blocks >= (1ll << 31)) return fail(eng, TSDF_ERR_INVALID_ARG, "heap_blocks out of range");
+  int id = -1;
+  for (int i = 0; i < (int)eng->maps.size(); ++i)
+    if (!eng->maps[i].live) {
+      id = i;
+      break;
+    }
+  if (id < 0) return fail(eng, TSDF_ERR_CAPACITY, "max_maps reached");
+  MapDev d{};
+  // initGlobalVars, tsdf_handler.cu:1289-1317 (float arithmetic)
+  d.vs = p->voxel_size;
+  d.T = p->truncation_distance;
+  d.maxw = p->max_weight;
+  d.pub_d2 = p->publish_distance_squared;
+  d.gc_d2 = p->garbage_collect_distance_squared;
+  d.half_vs = d.vs / 2.0f;
+  d.bs = d.vs * (float)kVoxelsPerSide;
+  d.half_bs = d.bs / 2.0f;
+  d.scale_v = 1.0f / d.vs;
+  d.scale_b = 1.0f / d.bs;
+  const float t2 = d.T * 2.0f;
+  d.vmax = (int)(std::ceil(t2 / d.vs) * 4.0f);
+  d.amax = (int)(std::ceil(t2 / d.bs) * 4.0f);
+  d.rmax = d.amax + 4;
+  d.margin = d.amax + d.vmax / kVoxelsPerSide + 2;
+  if (d.rmax > eng->cfg.max_routes)
+    return fail(eng, TSDF_ERR_INVALID_ARG,
+                "truncation_distance / voxel_size too large for max_routes (needs " + std::to_string(d.rmax) + ")");
+  if (d.margin >= kKeyBias / 2) return fail(eng, TSDF_ERR_INVALID_ARG, "truncation_distance too large");
+  const long long heap_base = eng->heap_ranges.alloc(heap_blocks);
+  if (heap_base < 0)
+    return fail(eng, TSDF_ERR_HEAP_FULL, "block pool cannot hold " + std::to_string(heap_blocks) +
+                                             " blocks (largest free range " +
+                                             std::to_string(eng->heap_ranges.largest()) + ")");
+  const int G = eng->cfg.bucket_size;
+  const unsigned long long buckets = next_pow2((unsigned long long)((2 * heap_blocks + G - 1) / G));
+  const long long entries = (long long)buckets * G;
+  const long long hash_base = eng->hash_ranges.alloc(entries);
+  if (hash_base < 0) {
+    eng->heap_ranges.release(heap_base, heap_blocks);
+    return fail(eng, TSDF_ERR_HEAP_FULL, "hash pool exhausted");
+  }
+  d.heap_cap = (int)heap_blocks;
+  d.live = 1;
+  d.heap_base = heap_base;
+  d.hash_base = hash_base;
+  d.hash_mask = (unsigned)(buckets - 1);
+  Lane& L = eng->lanes[0];
+  launch_map_init(eng->voxels, eng->slot_key, eng->nnz, eng->free_list, eng->hash, heap_base, heap_blocks, hash_base,
+                  entries, L.stream);
+  CK(cudaMemcpyAsync(eng->d_maps + id, &d, sizeof(d), cudaMemcpyHostToDevice, L.stream));
+  MapCounters z{};
+  CK(cudaMemcpyAsync(eng->d_mctr + id, &z, sizeof(z), cudaMemcpyHostToDevice, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  MapHost& m = eng->maps[id];
+  m = MapHost();
+  m.live = true;
+  m.params = *p;
+  m.dev = d;
+  m.hash_entries = entries;
+  *map_id = id;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_map_destroy(tsdf_engine* eng, int map_id) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  MapHost& m = eng->maps[map_id];
+  if (m.in_flight) return fail(eng, TSDF_ERR_BUSY, "map has a scan in flight");
+  for (auto& r : eng->queue)
+    if (r->scan.map_id == map_id) return fail(eng, TSDF_ERR_BUSY, "map has queued scans");
+  CK(cudaSetDevice(eng->device));
+  MapDev d{};
+  CK(cudaMemcpy(eng->d_maps + map_id, &d, sizeof(d), cudaMemcpyHostToDevice));
+  eng->heap_ranges.release(m.dev.heap_base, m.dev.heap_cap);
+  eng->hash_ranges.release(m.dev.hash_base, m.hash_entries);
+  m = MapHost();
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_map_info_get(tsdf_engine* eng, int map_id, tsdf_map_info* out) {
+  if (!eng || !out) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  CK(cudaSetDevice(eng->device));
+  MapCounters mc;
+  CK(cudaMemcpy(&mc, eng->d_mctr + map_id, sizeof(mc), cudaMemcpyDeviceToHost));
+  const MapHost& m = eng->maps[map_id];
+  out->heap_blocks = m.dev.heap_cap;
+  out->block_count = mc.block_count;
+  out->high_water = mc.hw;
+  out->hash_entries = m.hash_entries;
+  out->hash_used = mc.hash_used;
+  out->rehashes = m.rehashes;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_integrate_batch(tsdf_engine* eng, int n, const tsdf_scan* scans, tsdf_scan_result* results) {
+  if (!eng || !scans || !results || n <= 0) return TSDF_ERR_INVALID_ARG;
+  {
+    std::unique_lock<std::recursive_mutex> lk(eng->mu);
+    if (!eng->sched_running) {
+      if (cudaSetDevice(eng->device) != cudaSuccess) return TSDF_ERR_CUDA;
+      return run_batch_sync(eng, n, scans, results);
+    }
+  }
+  // the scheduler owns the lanes: route through it
+  std::vector<uint64_t> t(n);
+  for (int i = 0; i < n; ++i) {
+    tsdf_status s = tsdf_submit(eng, &scans[i], &results[i], &t[i]);
+    if (s != TSDF_OK) return s;
+  }
+  int w = TSDF_OK;
+  for (int i = 0; i < n; ++i) {
+    tsdf_wait(eng, t[i], -1);
+    tsdf_forget(eng, t[i]);
+    if (results[i].status != TSDF_OK && w == TSDF_OK) w = results[i].status;
+  }
+  return (tsdf_status)w;
+}
+
+tsdf_status tsdf_integrate(tsdf_engine* eng, int map_id, const float* xyz, int64_t n_points, int stride_bytes,
+                           const float origin[3], float* pub_pos, tsdf_voxel* pub_data, int64_t pub_cap,
+                           int64_t* pub_count, tsdf_scan_stats* stats) {
+  if (!eng || !origin) return TSDF_ERR_INVALID_ARG;
+  tsdf_scan s{};
+  s.map_id = map_id;
+  s.stride_bytes = stride_bytes;
+  s.n_points = n_points;
+  s.xyz = xyz;
+  s.origin[0] = origin[0], s.origin[1] = origin[1], s.origin[2] = origin[2];
+  tsdf_scan_result r{};
+  r.pub_pos = pub_pos;
+  r.pub_data = pub_data;
+  r.pub_cap = pub_cap;
+  tsdf_status st = tsdf_integrate_batch(eng, 1, &s, &r);
+  if (pub_count) *pub_count = r.pub_count;
+  if (stats) *stats = r.stats;
+  return st;
+}
+
+tsdf_status tsdf_submit(tsdf_engine* eng, const tsdf_scan* scan, tsdf_scan_result* result, uint64_t* ticket) {
+  if (!eng || !scan || !result || !ticket) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (scan->map_id < 0 || scan->map_id >= (int)eng->maps.size() || !eng->maps[scan->map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  if (scan->n_points > eng->cfg.max_batch_points) return fail(eng, TSDF_ERR_CAPACITY, "scan larger than a step");
+  auto r = std::make_shared<Request>();
+  r->ticket = eng->next_ticket++;
+  r->scan = *scan;
+  r->result = result;
+  r->t_submit = now_ns();
+  eng->queue.push_back(r);
+  eng->tickets[r->ticket] = r;
+  *ticket = r->ticket;
+  ensure_scheduler(eng);
+  eng->cv.notify_all();
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_poll(tsdf_engine* eng, uint64_t ticket) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  auto it = eng->tickets.find(ticket);
+  if (it == eng->tickets.end()) return TSDF_ERR_INVALID_ARG;
+  return it->second->done ? TSDF_OK : TSDF_ERR_NOT_READY;
+}
+
+tsdf_status tsdf_wait(tsdf_engine* eng, uint64_t ticket, int64_t timeout_ms) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  auto it = eng->tickets.find(ticket);
+  if (it == eng->tickets.end()) return TSDF_ERR_INVALID_ARG;
+  std::shared_ptr<Request> r = it->second;
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
+  while (!r->done) {
+    if (timeout_ms >= 0 && std::chrono::steady_clock::now() >= deadline) return TSDF_ERR_NOT_READY;
+    eng->cv.wait_for(lk, std::chrono::milliseconds(1));
+  }
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_ticket_times(tsdf_engine* eng, uint64_t ticket, int64_t* t_submit, int64_t* t_launch,
+                              int64_t* t_done) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  auto it = eng->tickets.find(ticket);
+  if (it == eng->tickets.end()) return TSDF_ERR_INVALID_ARG;
+  if (t_submit) *t_submit = it->second->t_submit;
+  if (t_launch) *t_launch = it->second->t_launch;
+  if (t_done) *t_done = it->second->t_done;
+  return it->second->done ? TSDF_OK : TSDF_ERR_NOT_READY;
+}
+
+tsdf_status tsdf_forget(tsdf_engine* eng, uint64_t ticket) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  auto it = eng->tickets.find(ticket);
+  if (it == eng->tickets.end()) return TSDF_ERR_INVALID_ARG;
+  if (!it->second->done) return TSDF_ERR_NOT_READY;
+  eng->tickets.erase(it);
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_dump_blocks(tsdf_engine* eng, int map_id, int32_t* kxyz, int32_t* slots, int64_t cap,
+                             int64_t* count) {
+  if (!eng || !count) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  CK(cudaSetDevice(eng->device));
+  const MapHost& m = eng->maps[map_id];
+  MapCounters mc;
+  CK(cudaMemcpy(&mc, eng->d_mctr + map_id, sizeof(mc), cudaMemcpyDeviceToHost));
+  std::vector<unsigned long long> keys((size_t)mc.hw);
+  if (mc.hw > 0)
+    CK(cudaMemcpy(keys.data(), eng->slot_key + m.dev.heap_base, sizeof(unsigned long long) * mc.hw,
+                  cudaMemcpyDeviceToHost));
+  int64_t c = 0;
+  for (int s = 0; s < mc.hw; ++s) {
+    if (keys[s] == kEmptyKey) continue;
+    if (c < cap) {
+      if (kxyz) {
+        kxyz[3 * c] = (int)((keys[s] >> 42) & 0x1FFFFF) - kKeyBias;
+        kxyz[3 * c + 1] = (int)((keys[s] >> 21) & 0x1FFFFF) - kKeyBias;
+        kxyz[3 * c + 2] = (int)(keys[s] & 0x1FFFFF) - kKeyBias;
+      }
+      if (slots) slots[c] = s;
+    }
+    ++c;
+  }
+  *count = c;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_dump_free_list(tsdf_engine* eng, int map_id, int32_t* out, int64_t cap, int64_t* block_count) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  CK(cudaSetDevice(eng->device));
+  const MapHost& m = eng->maps[map_id];
+  long long n = std::min<long long>(cap, m.dev.heap_cap);
+  if (out && n > 0)
+    CK(cudaMemcpy(out, eng->free_list + m.dev.heap_base, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (block_count) {
+    MapCounters mc;
+    CK(cudaMemcpy(&mc, eng->d_mctr + map_id, sizeof(mc), cudaMemcpyDeviceToHost));
+    *block_count = mc.block_count;
+  }
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, tsdf_voxel* out512) {
+  if (!eng || !out512) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  const MapHost& m = eng->maps[map_id];
+  if (slot < 0 || slot >= m.dev.heap_cap) return fail(eng, TSDF_ERR_INVALID_ARG, "slot out of range");
+  CK(cudaSetDevice(eng->device));
+  CK(cudaMemcpy(out512, eng->voxels + (m.dev.heap_base + slot) * kVoxelsPerBlock, sizeof(float2) * kVoxelsPerBlock,
+                cudaMemcpyDeviceToHost));
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_set_stage_timing(tsdf_engine* eng, int on) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  eng->stage_timing = on != 0;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_stage_times(tsdf_engine* eng, const char** names, double* ms, int64_t* launches, int* n) {
+  if (!eng || !n) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  int k = std::min(*n, (int)STAGE_COUNT);
+  for (int i = 0; i < k; ++i) {
+    if (names) names[i] = kStageNames[i];
+    if (ms) ms[i] = eng->stage_ms[i];
+    if (launches) launches[i] = eng->stage_launches[i];
+  }
+  *n = STAGE_COUNT;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_reset_stage_times(tsdf_engine* eng) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  for (int i = 0; i < STAGE_COUNT; ++i) eng->stage_ms[i] = 0, eng->stage_launches[i] = 0;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_flush_l2(tsdf_engine* eng) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  if (!eng->flush_buf) CK(cudaMalloc(&eng->flush_buf, kFlushBytes));
+  launch_flush(eng->flush_buf, kFlushBytes, 0, eng->lanes[0].stream);
+  CK(cudaStreamSynchronize(eng->lanes[0].stream));
+  return TSDF_OK;
+}
+
+int64_t tsdf_kernel_launches(tsdf_engine* eng) { return eng ? (int64_t)eng->launches.load() : 0; }
+
+tsdf_status tsdf_host_alloc(void** p, int64_t bytes) {
+  if (!p || bytes < 0) return TSDF_ERR_INVALID_ARG;
+  return cudaMallocHost(p, (size_t)std::max<int64_t>(bytes, 1)) == cudaSuccess ? TSDF_OK : TSDF_ERR_CUDA;
+}
+
+tsdf_status tsdf_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? TSDF_OK : TSDF_ERR_CUDA; }
+
+tsdf_status tsdf_device_alloc(tsdf_engine* eng, void** p, int64_t bytes) {
+  if (!eng || !p || bytes < 0) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  CK(cudaMalloc(p, (size_t)std::max<int64_t>(bytes, 1)));
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_device_free(tsdf_engine* eng, void* p) {
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  CK(cudaFree(p));
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_copy(tsdf_engine* eng, void* dst, const void* src, int64_t bytes, int kind) {
+  if (!eng || bytes < 0) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  CK(cudaMemcpy(dst, src, (size_t)bytes, k));
+  return TSDF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,190 @@
+// Structures shared by the host engine (tsdf_engine.cu) and the device
+// pipeline (tsdf_kernels.cu).  Nothing here is part of the public C-ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tsdfg {
+
+constexpr int kVoxelsPerSide = 8;      // tsdf_container.cuh:19
+constexpr int kVoxelsPerBlock = 512;   // tsdf_container.cuh:21
+constexpr int kKeyBias = 1 << 20;      // 21-bit signed block coordinates
+constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr unsigned long long kTombKey = ~0ull - 1ull;
+constexpr int kSlotPending = -2;
+constexpr unsigned kRankNone = 0xFFFFFFFFu;
+constexpr unsigned kRecSentinel = 0xFFFFFFFFu;
+constexpr int kRadixBits = 8;
+constexpr int kMaxRadixPasses = 4;
+constexpr int kUpdEntries = 32;        // voxel entries of one point inside one block (<= 22)
+
+// One hash entry: packed block key, logical heap slot, first-touch rank.
+// Invariants: slot >= 0 only while the key is live; rank == kRankNone except
+// while the entry is pending allocation inside one step.
+struct __align__(16) HEntry {
+  unsigned long long key;
+  int slot;
+  unsigned rank;
+};
+
+// Per-map constants (device table).  Derived values follow initGlobalVars,
+// tsdf_handler.cu:1289-1317, computed in float on the host.
+struct MapDev {
+  float vs, T, maxw, pub_d2, gc_d2;
+  float half_vs, bs, half_bs, scale_v, scale_b;
+  int vmax, amax, rmax, margin;
+  int heap_cap, live;
+  long long heap_base;   // first physical slot of the map's heap range
+  long long hash_base;   // first hash entry of the map's table
+  unsigned hash_mask;    // number of buckets - 1 (power of two)
+  int pad;
+};
+
+// Per-map mutable counters (device).
+struct MapCounters {
+  int block_count;  // allocated blocks (BlockHeap::block_count)
+  int hw;           // high-water slot + 1
+  int hash_used;    // non-empty hash entries (live + tombstones)
+  int pad;
+};
+
+// One scan in the current step (device copy written by the host each step).
+struct ItemDev {
+  const char* pts;
+  long long n;
+  long long point_base;   // first global point index of this item
+  float ox, oy, oz;
+  int stride;
+  int map;
+  int pad;
+  float* out_pos;         // published positions (device-accessible) or null
+  float2* out_data;       // published voxels (device-accessible)
+  long long out_cap;
+};
+
+// Per-item stats slots (match tsdf_scan_stats field order).
+enum {
+  ST_N = 0, ST_BAD, ST_BINC, ST_BOVF, ST_NEW, ST_HEAPFULL, ST_UPD, ST_VOVF, ST_ROVF, ST_MISS, ST_BADLOCAL,
+  ST_DVOX, ST_BTOUCH, ST_PUB, ST_PUBBLK, ST_GC, ST_BC, ST_ABEFORE, ST_COUNT
+};
+
+// Per-item scratch integers.
+enum {
+  II_NEW = 0,      // new keys claimed by this item
+  II_NEW_BASE,     // exclusive prefix of II_NEW
+  II_SLOT_BASE,    // first enumeration index of the item's slots
+  II_SLOT_N,       // number of enumerated slots (the map's high water)
+  II_PUB_BASE,     // publish prefix at the item's first slot
+  II_GC_BASE,      // gc prefix at the item's first slot
+  II_GC_N,         // blocks collected
+  II_COUNT
+};
+
+// Step header (device copy written by the host each step).
+struct BatchHdr {
+  int n_items;
+  int rank_stride;     // max block-DDA cap over items (rank = g * stride + j)
+  int rec_stride;      // routes per point in the record buffer
+  int pad0;
+  long long total_points;
+  long long rec_total;        // total_points * rec_stride
+  long long key_lo;           // record key = physical slot - key_lo
+  unsigned rec_key_limit;     // record keys >= this are empty routes
+  int pad1;
+};
+
+// Device-side counters of one step (zeroed by the first kernel).
+struct LaneCounters {
+  unsigned long long q_blocks;   // work queue heads
+  unsigned long long q_voxels;
+  unsigned long long q_update;
+  unsigned long long q_pubwrite;
+  long long n_new;        // new keys appended
+  long long n_rank_live;  // after the rank sort (== n_new)
+  long long n_rec_live;   // live routing records after the first sort pass
+  long long n_seg;        // segments (distinct blocks updated)
+  long long n_enum;       // enumerated slots for publish / gc
+  long long scan_total;   // scratch for scans
+  int error;              // bit flags, see ERR_*
+  int pad;
+};
+
+enum { ERR_HASH_FULL = 1, ERR_SPIN = 2, ERR_CAPACITY = 4 };
+
+// Everything a kernel can reach.  Passed by value; identical for every launch
+// of one lane, so a step can be captured once as a CUDA graph.
+struct Ctx {
+  // global (engine) state
+  float2* voxels;                // pool_blocks * 512
+  unsigned long long* slot_key;  // pool_blocks, kEmptyKey when free
+  int* nnz;                      // non-zero-weight voxels per block
+  int* free_list;                // pool_blocks (map range: logical slots)
+  HEntry* hash;                  // all maps' tables
+  const MapDev* maps;
+  MapCounters* mctr;
+  // lane state
+  const BatchHdr* hdr;
+  const ItemDev* items;
+  long long* item_stats;         // [max_maps][ST_COUNT]
+  int* item_i;                   // [max_maps][II_COUNT]
+  LaneCounters* ctr;
+  unsigned* newlist;             // entry indices of new keys
+  unsigned* rank_key[2];
+  unsigned* rank_val[2];
+  unsigned* rec_key[2];
+  unsigned* rec_val[2];
+  int* hist;                     // [256][max_tiles]
+  int* digit_tot;                // [256]
+  int* tile_sums;                // scan tiles
+  int* seg_start;
+  int* enum_cnt;                 // publish counts per enumerated slot
+  int* enum_gc;                  // gc flags per enumerated slot
+  int* pub_prefix;
+  int* gc_prefix;
+  int* seg_prefix;
+  int max_tiles_rank;
+  int max_tiles_rec;
+  int max_tiles_scan;
+  int ray_chunk;
+  long long rank_cap;            // capacity of the rank / newlist arrays
+  long long rec_cap;             // capacity of the record arrays
+  long long enum_cap;            // capacity of the enumeration arrays
+};
+
+// Stage ids for timing.
+enum {
+  STAGE_INIT = 0, STAGE_RAY_BLOCKS, STAGE_ALLOC_ORDER, STAGE_ALLOC, STAGE_RAY_VOXELS, STAGE_ROUTE_SORT,
+  STAGE_UPDATE, STAGE_PUBLISH, STAGE_GC, STAGE_COUNT
+};
+
+// Launch entry points implemented in tsdf_kernels.cu.  Each enqueues one
+// pipeline stage on `s`; every launch is counted in *launches.
+struct LaunchCfg {
+  int sm_count;
+  int bucket_size;   // 4, 8 or 16
+  int ray_threads;
+  int rank_passes;
+  int rec_passes;
+};
+
+void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+
+// Map maintenance (outside steps).
+void launch_map_init(float2* voxels, unsigned long long* slot_key, int* nnz, int* free_list, HEntry* hash,
+                     long long heap_base, long long heap_cap, long long hash_base, long long hash_entries,
+                     cudaStream_t s);
+void launch_map_rehash(const Ctx& c, int map, int bucket_size, long long heap_base, long long heap_hw,
+                       long long hash_base, long long hash_entries, unsigned hash_mask, int* d_used, int* d_err,
+                       cudaStream_t s);
+void launch_flush(void* buf, long long bytes, int value, cudaStream_t s);
+
+}  // namespace tsdfg

@@ -1,0 +1,1366 @@
+// Device pipeline of the GB300 TSDF engine: one integration step over a batch
+// of scans, one scan per map, all maps in the same launches.
+//
+// Stages (each a handful of grid-fixed kernels, so a step captures as one
+// CUDA graph and replays for any batch composition):
+//   ray_blocks   persistent work queue over (scan, point chunk): truncation
+//                segment + block DDA per point; warp-cooperative lookup /
+//                lock-free CAS insertion of every block into the map's hash
+//                table; unallocated blocks enter as "pending" with the
+//                smallest first-touch rank seen.
+//                (tsdf_handler.cu:112-272, :282-500)
+//   alloc_order  pending entries sorted by first-touch rank (LSD radix sort)
+//   alloc        heap slot = free_list[block_count + rank within the map]
+//                (device free-list stack), block zeroed, entry resolved
+//   ray_voxels   voxel DDA per point; its voxels grouped into runs of one
+//                block; one routing record (block slot, point) per run
+//   route_sort   stable radix sort of the records by block slot; segment
+//                heads -> one work item per block touched
+//   update       one CTA per block: 4 KiB of voxels staged in shared memory
+//                with 16-byte loads/stores; each point's voxels in the block
+//                recomputed and applied per voxel in ascending point order
+//                (tsdf_handler.cu:604-665)
+//   publish      in-radius blocks counted, prefix-summed, compacted to the
+//                output (tsdf_handler.cu:767-825)
+//   gc           out-of-radius blocks compacted, pushed to the free list in
+//                ascending slot order, hash entries tombstoned
+//                (tsdf_handler.cu:836-952)
+//
+// Float arithmetic uses explicit round-to-nearest intrinsics (no FMA
+// contraction) so every value matches the sequential CPU restatement bit for
+// bit.  Every loop that waits on another thread's progress is bounded.
+#include <cstdio>
+
+#include "tsdf_internal.h"
+
+namespace tsdfg {
+
+namespace {
+
+constexpr int kMaxItems = 1024;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// ----------------------------------------------------------------------------
+// float helpers: IEEE round-to-nearest, never contracted
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float sq3(float a, float b, float c) {
+  return fadd(fadd(fmul(a, a), fmul(b, b)), fmul(c, c));
+}
+
+// getVolumeCenterFromPoint (tsdf_handler.cu:65-85): floor(x*scale)/scale + half
+__device__ __forceinline__ float cell_center(float x, float scale, float half, float* fk) {
+  float f = floorf(fmul(x, scale));
+  *fk = f;
+  return fadd(fdiv(f, scale), half);
+}
+
+__device__ __forceinline__ unsigned long long pack_key(int kx, int ky, int kz) {
+  return ((unsigned long long)(unsigned)(kx + kKeyBias) << 42) |
+         ((unsigned long long)(unsigned)(ky + kKeyBias) << 21) | (unsigned long long)(unsigned)(kz + kKeyBias);
+}
+__device__ __forceinline__ void unpack_key(unsigned long long k, int* kx, int* ky, int* kz) {
+  *kx = (int)((k >> 42) & 0x1FFFFF) - kKeyBias;
+  *ky = (int)((k >> 21) & 0x1FFFFF) - kKeyBias;
+  *kz = (int)(k & 0x1FFFFF) - kKeyBias;
+}
+
+// MurmurHash3 64-bit finalizer (Appleby, public domain).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+struct Seg {
+  float ax, ay, az, bx, by, bz;
+};
+
+// getTruncationLineEndPoints (tsdf_handler.cu:112-133) plus the input checks
+// the reference lacks (non-finite point, zero-length ray, block coordinate out
+// of the 21-bit key range).
+__device__ __forceinline__ bool make_segment(float px, float py, float pz, float sx, float sy, float sz,
+                                             const MapDev& m, Seg* s) {
+  if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) return false;
+  if (!isfinite(sx) || !isfinite(sy) || !isfinite(sz)) return false;
+  float vx = fsub(px, sx), vy = fsub(py, sy), vz = fsub(pz, sz);
+  float mag = __fsqrt_rn(sq3(vx, vy, vz));
+  if (!(mag > 0.0f) || !isfinite(mag)) return false;
+  float nx = fdiv(vx, mag), ny = fdiv(vy, mag), nz = fdiv(vz, mag);
+  float tx = fmul(m.T, nx), ty = fmul(m.T, ny), tz = fmul(m.T, nz);
+  float ax = fsub(px, tx), ay = fsub(py, ty), az = fsub(pz, tz);
+  float bx = fadd(px, tx), by = fadd(py, ty), bz = fadd(pz, tz);
+  float da = sq3(fsub(ax, sx), fsub(ay, sy), fsub(az, sz));
+  float db = sq3(fsub(bx, sx), fsub(by, sy), fsub(bz, sz));
+  if (db < da) {
+    float t;
+    t = ax, ax = bx, bx = t;
+    t = ay, ay = by, by = t;
+    t = az, az = bz, bz = t;
+  }
+  const float lim = (float)(kKeyBias - m.margin);
+  float c[6] = {ax, ay, az, bx, by, bz};
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    float f = floorf(fmul(c[i], m.scale_b));
+    if (!(f > -lim && f < lim)) return false;
+  }
+  s->ax = ax, s->ay = ay, s->az = az, s->bx = bx, s->by = by, s->bz = bz;
+  return true;
+}
+
+// traverseVolume (tsdf_handler.cu:146-245) as a resumable walker: next()
+// yields the cells in the reference's order, stops where the reference
+// returns, and stops after `cap` cells (setting ovf) where the reference would
+// overrun its buffer.
+struct Dda {
+  float cx, cy, cz;
+  float tmx, tmy, tmz, tdx, tdy, tdz, stx, sty, stz;
+  float ccx, ccy, ccz, fx, fy, fz;
+  float ecx, ecy, ecz;
+  float vs, scale, half, eps, vpe, vme;
+  int n, cap;
+  bool done, ovf;
+
+  __device__ __forceinline__ void init(const Seg& s, float vs_, float scale_, float half_, int cap_) {
+    vs = vs_;
+    scale = scale_;
+    half = half_;
+    eps = fdiv(vs, 4.0f);
+    vpe = fadd(vs, eps);
+    vme = fsub(vs, eps);
+    float vx = fsub(s.bx, s.ax), vy = fsub(s.by, s.ay), vz = fsub(s.bz, s.az);
+    stx = vx > 0.0f ? vs : fmul(-1.0f, vs);
+    sty = vy > 0.0f ? vs : fmul(-1.0f, vs);
+    stz = vz > 0.0f ? vs : fmul(-1.0f, vs);
+    float d;
+    float scx = cell_center(s.ax, scale, half, &d);
+    float scy = cell_center(s.ay, scale, half, &d);
+    float scz = cell_center(s.az, scale, half, &d);
+    tmx = fabsf(vx < 0.0f ? fdiv(fsub(fsub(scx, half), s.ax), vx) : fdiv(fsub(fadd(scx, half), s.ax), vx));
+    tmy = fabsf(vy < 0.0f ? fdiv(fsub(fsub(scy, half), s.ay), vy) : fdiv(fsub(fadd(scy, half), s.ay), vy));
+    tmz = fabsf(vz < 0.0f ? fdiv(fsub(fsub(scz, half), s.az), vz) : fdiv(fsub(fadd(scz, half), s.az), vz));
+    tdx = fabsf(fdiv(vs, vx));
+    tdy = fabsf(fdiv(vs, vy));
+    tdz = fabsf(fdiv(vs, vz));
+    cx = s.ax, cy = s.ay, cz = s.az;
+    ccx = cell_center(cx, scale, half, &fx);
+    ccy = cell_center(cy, scale, half, &fy);
+    ccz = cell_center(cz, scale, half, &fz);
+    ecx = cell_center(s.bx, scale, half, &d);
+    ecy = cell_center(s.by, scale, half, &d);
+    ecz = cell_center(s.bz, scale, half, &d);
+    n = 0;
+    cap = cap_;
+    done = false;
+    ovf = false;
+  }
+
+  __device__ __forceinline__ bool next(float* ox, float* oy, float* oz, int* kx, int* ky, int* kz) {
+    if (done) return false;
+    bool at_end = fabsf(fsub(ccx, ecx)) < eps && fabsf(fsub(ccy, ecy)) < eps && fabsf(fsub(ccz, ecz)) < eps;
+    if (n == cap) {
+      ovf = true;
+      done = true;
+      return false;
+    }
+    *ox = ccx, *oy = ccy, *oz = ccz;
+    *kx = (int)fx, *ky = (int)fy, *kz = (int)fz;
+    ++n;
+    if (at_end) {
+      done = true;
+      return true;
+    }
+    if (tmx < tmy) {
+      if (tmx < tmz) {
+        cx = fadd(cx, stx);
+        tmx = fadd(tmx, tdx);
+      } else if (tmx > tmz) {
+        cz = fadd(cz, stz);
+        tmz = fadd(tmz, tdz);
+      } else {
+        cx = fadd(cx, stx);
+        cz = fadd(cz, stz);
+        tmx = fadd(tmx, tdx);
+        tmz = fadd(tmz, tdz);
+      }
+    } else if (tmx > tmy) {
+      if (tmy < tmz) {
+        cy = fadd(cy, sty);
+        tmy = fadd(tmy, tdy);
+      } else if (tmy > tmz) {
+        cz = fadd(cz, stz);
+        tmz = fadd(tmz, tdz);
+      } else {
+        cy = fadd(cy, sty);
+        cz = fadd(cz, stz);
+        tmy = fadd(tmy, tdy);
+        tmz = fadd(tmz, tdz);
+      }
+    } else {
+      if (tmz < tmx) {
+        cz = fadd(cz, stz);
+        tmz = fadd(tmz, tdz);
+      } else if (tmz > tmx) {
+        cx = fadd(cx, stx);
+        cy = fadd(cy, sty);
+        tmx = fadd(tmx, tdx);
+        tmy = fadd(tmy, tdy);
+      } else {
+        cx = fadd(cx, stx);
+        cy = fadd(cy, sty);
+        cz = fadd(cz, stz);
+        tmx = fadd(tmx, tdx);
+        tmy = fadd(tmy, tdy);
+        tmz = fadd(tmz, tdz);
+      }
+    }
+    float px = ccx, py = ccy, pz = ccz;
+    ccx = cell_center(cx, scale, half, &fx);
+    ccy = cell_center(cy, scale, half, &fy);
+    ccz = cell_center(cz, scale, half, &fz);
+    float d0 = fabsf(fsub(px, ccx)), d1 = fabsf(fsub(py, ccy)), d2 = fabsf(fsub(pz, ccz));
+    if ((d0 < vme && d1 < vme && d2 < vme) || (d0 > vpe || d1 > vpe || d2 > vpe)) done = true;
+    return true;
+  }
+};
+
+// getDistanceUpdate (tsdf_handler.cu:562-573)
+__device__ __forceinline__ float distance_update(float x, float y, float z, float px, float py, float pz, float sx,
+                                                 float sy, float sz) {
+  float ax = fsub(px, sx), ay = fsub(py, sy), az = fsub(pz, sz);
+  float bx = fsub(px, x), by = fsub(py, y), bz = fsub(pz, z);
+  float mag = __fsqrt_rn(sq3(bx, by, bz));
+  float dot = fadd(fadd(fmul(ax, bx), fmul(ay, by)), fmul(az, bz));
+  if (dot < 0.0f) mag = fmul(mag, -1.0f);
+  return mag;
+}
+
+__device__ __forceinline__ int find_item(const long long* pb, int n, long long g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (pb[mid] <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void stat_add(long long* st, int item, int k, long long v) {
+  if (v) atomicAdd(reinterpret_cast<unsigned long long*>(&st[item * ST_COUNT + k]), (unsigned long long)v);
+}
+
+// Warp-aggregated stat add; all 32 lanes must call it.
+__device__ __forceinline__ void stat_add_warp(long long* st, int item, int k, unsigned v) {
+  unsigned peers = __match_any_sync(kFull, item);
+  unsigned sum = __reduce_add_sync(peers, v);
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && sum)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&st[item * ST_COUNT + k]), (unsigned long long)sum);
+}
+
+__device__ __forceinline__ void set_error(LaneCounters* c, int bit) { atomicOr(&c->error, bit); }
+
+__device__ __forceinline__ ulonglong2 load_entry_cg(const HEntry* e) {
+  return __ldcg(reinterpret_cast<const ulonglong2*>(e));
+}
+__device__ __forceinline__ ulonglong2 load_entry_ro(const HEntry* e) {
+  return __ldg(reinterpret_cast<const ulonglong2*>(e));
+}
+
+// ----------------------------------------------------------------------------
+// Hash table: per map, (mask+1) buckets of G entries; bucket = mix64(key) &
+// mask, linear probing over buckets.  A group of G lanes probes one bucket per
+// step (one 16-byte entry per lane, G*16 contiguous bytes), votes with ballot.
+
+enum { INS_FOUND = 0, INS_NEW = 1, INS_FULL = 2 };
+
+// Lookup; returns the logical slot or -1.  Group-uniform arguments.
+template <int G>
+__device__ __forceinline__ int group_lookup(const HEntry* tab, unsigned mask, unsigned long long key, int gl, int gbase,
+                                            unsigned gmask) {
+  const unsigned long long h = mix64(key);
+  for (unsigned p = 0; p <= mask; ++p) {
+    unsigned b = (unsigned)(h + p) & mask;
+    ulonglong2 raw = load_entry_ro(tab + (size_t)b * G + gl);
+    unsigned hit = __ballot_sync(gmask, raw.x == key) & gmask;
+    if (hit) return __shfl_sync(gmask, (int)(unsigned)(raw.y & 0xFFFFFFFFull), __ffs(hit) - 1);
+    unsigned emp = __ballot_sync(gmask, raw.x == kEmptyKey) & gmask;
+    if (emp) return -1;
+  }
+  return -1;
+}
+
+// Find-or-claim for the block pass.  A found pending entry gets atomicMin of
+// the rank; a claimed entry (first EMPTY or TOMB slot from the home bucket,
+// CAS on the key) becomes pending with this rank.  All inserters of one key
+// walk the same sequence and treat "entry == key" as found, so a key is never
+// claimed twice; no entry is freed during the pass.
+template <int G>
+__device__ __forceinline__ int group_insert(HEntry* tab, unsigned mask, unsigned long long key, unsigned rank, int gl,
+                                            int gbase, unsigned gmask, unsigned* entry_out, bool* from_empty) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long h = mix64(key);
+  for (unsigned p = 0; p <= mask; ++p) {
+    unsigned b = (unsigned)(h + p) & mask;
+    HEntry* e = tab + (size_t)b * G + gl;
+    ulonglong2 raw = load_entry_cg(e);
+    unsigned hit = __ballot_sync(gmask, raw.x == key) & gmask;
+    if (hit) {
+      if (lane == __ffs(hit) - 1 && (int)(unsigned)(raw.y & 0xFFFFFFFFull) < 0) atomicMin(&e->rank, rank);
+      return INS_FOUND;
+    }
+    if (__ballot_sync(gmask, raw.x == kEmptyKey) & gmask) break;
+  }
+  unsigned q = 0;
+  unsigned guard = 0;
+  const unsigned guard_max = (mask + 1u) * (unsigned)G * 4u + 64u;
+  while (q <= mask) {
+    if (++guard > guard_max) return INS_FULL;
+    unsigned b = (unsigned)(h + q) & mask;
+    HEntry* e = tab + (size_t)b * G + gl;
+    ulonglong2 raw = load_entry_cg(e);
+    unsigned hit = __ballot_sync(gmask, raw.x == key) & gmask;
+    if (hit) {
+      if (lane == __ffs(hit) - 1 && (int)(unsigned)(raw.y & 0xFFFFFFFFull) < 0) atomicMin(&e->rank, rank);
+      return INS_FOUND;
+    }
+    unsigned cand = __ballot_sync(gmask, raw.x == kEmptyKey || raw.x == kTombKey) & gmask;
+    if (!cand) {
+      ++q;
+      continue;
+    }
+    int src = __ffs(cand) - 1;
+    unsigned long long old = 0;
+    if (lane == src) {
+      old = atomicCAS(&e->key, raw.x, key);
+      if (old == raw.x) {
+        atomicMin(&e->rank, rank);
+        atomicExch(&e->slot, kSlotPending);
+      }
+    }
+    old = __shfl_sync(gmask, old, src);
+    unsigned long long seen = __shfl_sync(gmask, raw.x, src);
+    if (old == seen) {
+      *entry_out = b * (unsigned)G + (unsigned)(src - gbase);
+      *from_empty = seen == kEmptyKey;
+      return INS_NEW;
+    }
+    if (old == key) {
+      if (lane == src) atomicMin(&e->rank, rank);
+      return INS_FOUND;
+    }
+  }
+  return INS_FULL;
+}
+
+// Single-thread find of the entry holding key (for deletion); -1 if absent.
+__device__ long long thread_find_entry(const HEntry* tab, unsigned mask, int G, unsigned long long key) {
+  const unsigned long long h = mix64(key);
+  for (unsigned p = 0; p <= mask; ++p) {
+    unsigned b = (unsigned)(h + p) & mask;
+    for (int i = 0; i < G; ++i) {
+      unsigned long long k = tab[(size_t)b * G + i].key;
+      if (k == key) return (long long)b * G + i;
+      if (k == kEmptyKey) return -1;
+    }
+  }
+  return -1;
+}
+
+// ----------------------------------------------------------------------------
+// step init
+__global__ void k_step_init(Ctx c) {
+  const BatchHdr h = *c.hdr;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    LaneCounters z = {};
+    *c.ctr = z;
+  }
+  for (int i = t; i < h.n_items * ST_COUNT; i += gridDim.x * blockDim.x) {
+    const int item = i / ST_COUNT, k = i % ST_COUNT;
+    long long v = 0;
+    if (k == ST_N) v = c.items[item].n;
+    if (k == ST_ABEFORE) v = c.mctr[c.items[item].map].block_count;
+    c.item_stats[i] = v;
+  }
+  for (int i = t; i < h.n_items * II_COUNT; i += gridDim.x * blockDim.x) c.item_i[i] = 0;
+}
+
+// ----------------------------------------------------------------------------
+// ray pass 1: block DDA + find-or-claim (getVoxelBlocksCuda + allocation lookup)
+template <int G>
+__global__ void __launch_bounds__(256) k_ray_blocks(Ctx c) {
+  __shared__ long long s_pb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int gl = lane % G;
+  const int gbase = lane - gl;
+  const unsigned gmask = (G == 32) ? kFull : (((1u << G) - 1u) << gbase);
+  const long long total = h.total_points;
+  const long long chunk = c.ray_chunk;
+  while (true) {
+    unsigned long long q = 0;
+    if (lane == 0) q = atomicAdd(&c.ctr->q_blocks, 1ull);
+    long long start = (long long)__shfl_sync(kFull, q, 0) * chunk;
+    if (start >= total) break;
+    long long end = min(start + chunk, total);
+    for (long long base = start; base < end; base += 32) {
+      long long g = base + lane;
+      bool active = g < end;
+      int item = active ? find_item(s_pb, h.n_items, g) : 0;
+      const ItemDev& it = c.items[item];
+      const int mi = it.map;
+      const MapDev& m = c.maps[mi];
+      Seg seg;
+      bool valid = false;
+      if (active) {
+        const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
+        valid = make_segment(p[0], p[1], p[2], it.ox, it.oy, it.oz, m, &seg);
+      }
+      Dda dda;
+      if (valid) dda.init(seg, m.bs, m.scale_b, m.half_bs, m.amax);
+      HEntry* tab = c.hash + m.hash_base;
+      const unsigned mask = m.hash_mask;
+      unsigned inc = 0;
+      for (int j = 0;; ++j) {
+        float x, y, z;
+        int kx, ky, kz;
+        bool has = valid && dda.next(&x, &y, &z, &kx, &ky, &kz);
+        unsigned hm = __ballot_sync(kFull, has);
+        if (!hm) break;
+        unsigned long long key = has ? pack_key(kx, ky, kz) : 0ull;
+        unsigned rank = has ? (unsigned)(g * (long long)h.rank_stride + j) : 0u;
+        inc += has ? 1u : 0u;
+        for (int i = 0; i < G; ++i) {
+          const int src = gbase + i;
+          if (!((hm >> src) & 1u)) continue;
+          unsigned long long k2 = __shfl_sync(gmask, key, src);
+          unsigned r2 = __shfl_sync(gmask, rank, src);
+          HEntry* t2 = reinterpret_cast<HEntry*>(__shfl_sync(gmask, reinterpret_cast<unsigned long long>(tab), src));
+          unsigned m2 = __shfl_sync(gmask, mask, src);
+          int map2 = __shfl_sync(gmask, mi, src);
+          int item2 = __shfl_sync(gmask, item, src);
+          unsigned entry = 0;
+          bool from_empty = false;
+          int res = group_insert<G>(t2, m2, k2, r2, gl, gbase, gmask, &entry, &from_empty);
+          if (gl == 0) {
+            if (res == INS_NEW) {
+              unsigned long long slot = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_new), 1ull);
+              long long gidx = (long long)(t2 - c.hash) + entry;
+              if ((long long)slot < c.rank_cap)
+                c.newlist[slot] = (unsigned)gidx;
+              else
+                set_error(c.ctr, ERR_CAPACITY);
+              atomicAdd(&c.item_i[item2 * II_COUNT + II_NEW], 1);
+              if (from_empty) atomicAdd(&c.mctr[map2].hash_used, 1);
+            } else if (res == INS_FULL) {
+              set_error(c.ctr, ERR_HASH_FULL);
+            }
+          }
+        }
+      }
+      stat_add_warp(c.item_stats, item, ST_BINC, inc);
+      stat_add_warp(c.item_stats, item, ST_BAD, (active && !valid) ? 1u : 0u);
+      stat_add_warp(c.item_stats, item, ST_BOVF, (valid && dda.ovf) ? 1u : 0u);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// generic exclusive scan (3 kernels, grid-fixed, n read on the device)
+constexpr int SC_T = 256;
+constexpr int SC_IPT = 8;
+constexpr int SC_TILE = SC_T * SC_IPT;
+
+__device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(kFull, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = w;
+  }
+  __syncthreads();
+  int warp_off = warp ? s_warp[warp - 1] : 0;
+  *total = s_warp[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+template <class F>
+__global__ void __launch_bounds__(SC_T) k_scan_reduce(F f, const long long* n_ptr, int* tile_sums) {
+  __shared__ int s_warp[32];
+  const long long n = *n_ptr;
+  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int sum = 0;
+    for (int r = 0; r < SC_IPT; ++r) {
+      long long i = tile * SC_TILE + r * SC_T + threadIdx.x;
+      if (i < n) sum += f(i);
+    }
+    int tot;
+    block_excl_scan(sum, s_warp, &tot);
+    if (threadIdx.x == 0) tile_sums[tile] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(int* tile_sums, const long long* n_ptr, long long* total_out) {
+  __shared__ int s_warp[32];
+  const long long n = *n_ptr;
+  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
+  long long carry = 0;
+  for (long long b = 0; b < ntiles; b += blockDim.x) {
+    long long i = b + threadIdx.x;
+    int v = i < ntiles ? tile_sums[i] : 0;
+    int tot;
+    int ex = block_excl_scan(v, s_warp, &tot);
+    if (i < ntiles) tile_sums[i] = (int)(carry + ex);
+    carry += tot;
+  }
+  if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+template <class F, class O>
+__global__ void __launch_bounds__(SC_T) k_scan_apply(F f, O o, const long long* n_ptr, const int* tile_offs) {
+  __shared__ int s_warp[32];
+  const long long n = *n_ptr;
+  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int carry = tile_offs[tile];
+    for (int r = 0; r < SC_IPT; ++r) {
+      long long i = tile * SC_TILE + r * SC_T + threadIdx.x;
+      int v = i < n ? f(i) : 0;
+      int tot;
+      int ex = block_excl_scan(v, s_warp, &tot);
+      if (i < n) o(i, carry + ex, v);
+      carry += tot;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// LSD radix sort of (u32 key, u32 value), 8-bit digits, stable.
+constexpr int RS_T = 256;
+constexpr int RS_IPT = 8;
+constexpr int RS_TILE = RS_T * RS_IPT;
+
+__global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* keys, const long long* n_ptr, long long cap,
+                                                  int shift, unsigned key_limit, int* hist, int max_tiles) {
+  __shared__ int s_h[256];
+  const long long n = min(*n_ptr, cap);
+  const long long ntiles = (n + RS_TILE - 1) / RS_TILE;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    s_h[threadIdx.x] = 0;
+    __syncthreads();
+    for (int r = 0; r < RS_IPT; ++r) {
+      long long i = tile * RS_TILE + r * RS_T + threadIdx.x;
+      if (i < n) {
+        unsigned k = keys[i];
+        if (k < key_limit) atomicAdd(&s_h[(k >> shift) & 255u], 1);
+      }
+    }
+    __syncthreads();
+    hist[threadIdx.x * max_tiles + tile] = s_h[threadIdx.x];
+    __syncthreads();
+  }
+}
+
+// One CTA per digit: exclusive scan of the digit's row over tiles.
+__global__ void __launch_bounds__(1024) k_rs_scan_digits(int* hist, const long long* n_ptr, long long cap,
+                                                         int max_tiles, int* digit_tot) {
+  __shared__ int s_warp[32];
+  const long long n = min(*n_ptr, cap);
+  const long long ntiles = (n + RS_TILE - 1) / RS_TILE;
+  int* row = hist + (long long)blockIdx.x * max_tiles;
+  long long carry = 0;
+  for (long long b = 0; b < ntiles; b += blockDim.x) {
+    long long i = b + threadIdx.x;
+    int v = i < ntiles ? row[i] : 0;
+    int tot;
+    int ex = block_excl_scan(v, s_warp, &tot);
+    if (i < ntiles) row[i] = (int)(carry + ex);
+    carry += tot;
+  }
+  if (threadIdx.x == 0) digit_tot[blockIdx.x] = (int)carry;
+}
+
+__global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* kin, const unsigned* vin, unsigned* kout,
+                                                     unsigned* vout, const long long* n_ptr, long long cap,
+                                                     int shift, unsigned key_limit, const int* hist,
+                                                     int max_tiles, const int* digit_tot, long long* n_out) {
+  __shared__ int s_base[256];
+  __shared__ int s_run[256];
+  __shared__ int s_wc[RS_T / 32][256];
+  __shared__ int s_warp[32];
+  const long long n = min(*n_ptr, cap);
+  const long long ntiles = (n + RS_TILE - 1) / RS_TILE;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  {
+    int tot;
+    int v = digit_tot[t];
+    int ex = block_excl_scan(v, s_warp, &tot);
+    s_base[t] = ex;
+    if (blockIdx.x == 0 && t == 0 && n_out) *n_out = tot;
+  }
+  __syncthreads();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    s_run[t] = hist[t * max_tiles + tile];
+    __syncthreads();
+    for (int r = 0; r < RS_IPT; ++r) {
+      long long i = tile * RS_TILE + r * RS_T + t;
+      unsigned k = 0, v = 0;
+      bool valid = false;
+      if (i < n) {
+        k = kin[i];
+        valid = k < key_limit;
+        if (valid) v = vin[i];
+      }
+      int d = valid ? (int)((k >> shift) & 255u) : 256;
+#pragma unroll
+      for (int w = 0; w < RS_T / 32; ++w) s_wc[w][t] = 0;
+      __syncthreads();
+      unsigned peers = __match_any_sync(kFull, d);
+      int lt = __popc(peers & lt_mask);
+      if (valid && lt == 0) s_wc[warp][d] = __popc(peers);
+      __syncthreads();
+      {
+        int acc = s_run[t];
+#pragma unroll
+        for (int w = 0; w < RS_T / 32; ++w) {
+          int cnt = s_wc[w][t];
+          s_wc[w][t] = acc;
+          acc += cnt;
+        }
+        s_run[t] = acc;
+      }
+      __syncthreads();
+      if (valid) {
+        long long pos = (long long)s_base[d] + s_wc[warp][d] + lt;
+        kout[pos] = k;
+        vout[pos] = v;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+void radix_sort(const Ctx& c, unsigned* const* keys, unsigned* const* vals, const long long* n_first,
+                unsigned key_limit, long long* n_live, long long cap, int passes, int max_tiles, int sm_count,
+                cudaStream_t s, long long* launches) {
+  const int grid = sm_count * 4;
+  for (int p = 0; p < passes; ++p) {
+    const unsigned* kin = keys[p & 1];
+    const unsigned* vin = vals[p & 1];
+    unsigned* kout = keys[(p + 1) & 1];
+    unsigned* vout = vals[(p + 1) & 1];
+    const long long* np = p == 0 ? n_first : n_live;
+    const unsigned lim = p == 0 ? key_limit : 0xFFFFFFFFu;
+    k_rs_hist<<<grid, RS_T, 0, s>>>(kin, np, cap, p * kRadixBits, lim, c.hist, max_tiles);
+    k_rs_scan_digits<<<256, 1024, 0, s>>>(c.hist, np, cap, max_tiles, c.digit_tot);
+    k_rs_scatter<<<grid, RS_T, 0, s>>>(kin, vin, kout, vout, np, cap, p * kRadixBits, lim, c.hist, max_tiles,
+                                       c.digit_tot, p == 0 ? n_live : nullptr);
+    *launches += 3;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// allocation
+__global__ void k_gather_ranks(Ctx c) {
+  const long long n = min(c.ctr->n_new, c.rank_cap);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned e = c.newlist[i];
+    c.rank_key[0][i] = c.hash[e].rank;
+    c.rank_val[0][i] = e;
+  }
+}
+
+__global__ void k_alloc_prefix(Ctx c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = c.hdr->n_items;
+  int acc = 0;
+  for (int i = 0; i < n; ++i) {
+    c.item_i[i * II_COUNT + II_NEW_BASE] = acc;
+    acc += c.item_i[i * II_COUNT + II_NEW];
+  }
+}
+
+// One warp per new block, in first-touch order: pop the free list, resolve
+// the pending entry, zero the 4 KiB block (the reference's new VoxelBlock()).
+__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel) {
+  __shared__ long long s_pb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const long long n = min(c.ctr->n_new, c.rank_cap);
+  const int lane = threadIdx.x & 31;
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const unsigned* rk = c.rank_key[rank_sel];
+  const unsigned* rv = c.rank_val[rank_sel];
+  for (long long i = wid; i < n; i += nw) {
+    unsigned rank = rk[i];
+    unsigned e = rv[i];
+    long long g = (long long)(rank / (unsigned)h.rank_stride);
+    int item = find_item(s_pb, h.n_items, g);
+    int mi = c.items[item].map;
+    const MapDev& m = c.maps[mi];
+    long long rb = i - c.item_i[item * II_COUNT + II_NEW_BASE];
+    long long bc = c.mctr[mi].block_count;
+    HEntry* en = c.hash + e;
+    if (bc + rb < m.heap_cap) {
+      int slot = c.free_list[m.heap_base + bc + rb];
+      long long phys = m.heap_base + slot;
+      if (lane == 0) {
+        en->slot = slot;
+        en->rank = kRankNone;
+        c.slot_key[phys] = en->key;
+        c.nnz[phys] = 0;
+        atomicMax(&c.mctr[mi].hw, slot + 1);
+        stat_add(c.item_stats, item, ST_NEW, 1);
+      }
+      float4* dst = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < kVoxelsPerBlock / 2 / 32; ++k) dst[k * 32 + lane] = z;
+    } else if (lane == 0) {
+      en->key = kTombKey;
+      en->slot = -1;
+      en->rank = kRankNone;
+      stat_add(c.item_stats, item, ST_HEAPFULL, 1);
+    }
+  }
+}
+
+// block_count += allocated; slot enumeration bases for publish / gc.
+__global__ void k_alloc_finalize(Ctx c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = c.hdr->n_items;
+  long long acc = 0;
+  for (int i = 0; i < n; ++i) {
+    int mi = c.items[i].map;
+    const MapDev& m = c.maps[mi];
+    int bc = c.mctr[mi].block_count;
+    int nn = c.item_i[i * II_COUNT + II_NEW];
+    int room = m.heap_cap - bc;
+    c.mctr[mi].block_count = bc + (nn < room ? nn : room);
+    int hw = c.mctr[mi].hw;
+    c.item_i[i * II_COUNT + II_SLOT_BASE] = (int)acc;
+    c.item_i[i * II_COUNT + II_SLOT_N] = hw;
+    acc += hw;
+  }
+  c.ctr->n_enum = acc;
+}
+
+// ----------------------------------------------------------------------------
+// ray pass 2: voxel DDA, runs of one block, one routing record per run
+template <int G>
+__global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
+  __shared__ long long s_pb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int gl = lane % G;
+  const int gbase = lane - gl;
+  const unsigned gmask = (G == 32) ? kFull : (((1u << G) - 1u) << gbase);
+  const long long total = h.total_points;
+  const long long chunk = c.ray_chunk;
+  const int R = h.rec_stride;
+  unsigned* rk = c.rec_key[0];
+  unsigned* rv = c.rec_val[0];
+  while (true) {
+    unsigned long long q = 0;
+    if (lane == 0) q = atomicAdd(&c.ctr->q_voxels, 1ull);
+    long long start = (long long)__shfl_sync(kFull, q, 0) * chunk;
+    if (start >= total) break;
+    long long end = min(start + chunk, total);
+    for (long long base = start; base < end; base += 32) {
+      long long g = base + lane;
+      bool active = g < end;
+      int item = active ? find_item(s_pb, h.n_items, g) : 0;
+      const ItemDev& it = c.items[item];
+      const int mi = it.map;
+      const MapDev& m = c.maps[mi];
+      Seg seg;
+      bool valid = false;
+      if (active) {
+        const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
+        valid = make_segment(p[0], p[1], p[2], it.ox, it.oy, it.oz, m, &seg);
+      }
+      Dda dda;
+      if (valid) dda.init(seg, m.vs, m.scale_v, m.half_vs, m.vmax);
+      const HEntry* tab = c.hash + m.hash_base;
+      const unsigned mask = m.hash_mask;
+      const long long kbase = m.heap_base - c.hdr->key_lo;
+      unsigned long long cur = kEmptyKey;
+      int run = -1, run_slot = -1;
+      unsigned route_ovf = 0, missing = 0;
+      const long long rbase = g * (long long)R;
+      while (true) {
+        float x, y, z;
+        int kx, ky, kz;
+        bool has = valid && dda.next(&x, &y, &z, &kx, &ky, &kz);
+        if (!__ballot_sync(kFull, has)) break;
+        unsigned long long bkey = 0;
+        if (has) {
+          int bx = (int)floorf(fmul(x, m.scale_b));
+          int by = (int)floorf(fmul(y, m.scale_b));
+          int bz = (int)floorf(fmul(z, m.scale_b));
+          bkey = pack_key(bx, by, bz);
+        }
+        bool newrun = has && bkey != cur;
+        if (newrun) {
+          ++run;
+          cur = bkey;
+          run_slot = -1;
+        }
+        bool need = newrun && run < m.rmax;
+        unsigned nm = __ballot_sync(kFull, need);
+        for (int i = 0; i < G; ++i) {
+          const int src = gbase + i;
+          if (!((nm >> src) & 1u)) continue;
+          unsigned long long k2 = __shfl_sync(gmask, bkey, src);
+          const HEntry* t2 =
+              reinterpret_cast<const HEntry*>(__shfl_sync(gmask, reinterpret_cast<unsigned long long>(tab), src));
+          unsigned m2 = __shfl_sync(gmask, mask, src);
+          int res = group_lookup<G>(t2, m2, k2, gl, gbase, gmask);
+          if (lane == src) run_slot = res;
+        }
+        if (need) {
+          rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
+          rv[rbase + run] = (unsigned)g;
+        }
+        if (has) {
+          if (run >= m.rmax)
+            ++route_ovf;
+          else if (run_slot < 0)
+            ++missing;
+        }
+      }
+      if (active) {
+        int first = valid ? min(run + 1, m.rmax) : 0;
+        for (int j = first; j < R; ++j) rk[rbase + j] = kRecSentinel;
+      }
+      stat_add_warp(c.item_stats, item, ST_VOVF, (valid && dda.ovf) ? 1u : 0u);
+      stat_add_warp(c.item_stats, item, ST_ROVF, route_ovf);
+      stat_add_warp(c.item_stats, item, ST_MISS, missing);
+    }
+  }
+}
+
+// segment heads of the sorted records
+struct SegHeadIn {
+  const unsigned* k;
+  __device__ int operator()(long long i) const { return (i == 0 || k[i] != k[i - 1]) ? 1 : 0; }
+};
+struct SegHeadOut {
+  int* seg_start;
+  __device__ void operator()(long long i, int prefix, int v) const {
+    if (v) seg_start[prefix] = (int)i;
+  }
+};
+
+// ----------------------------------------------------------------------------
+// update: one CTA per block touched
+constexpr int UPD_T = 128;
+
+__device__ __forceinline__ int find_item_global(const ItemDev* items, int n, long long g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (items[mid].point_base <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
+  __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
+  __shared__ float s_d[UPD_T * kUpdEntries];
+  __shared__ unsigned short s_l[UPD_T * kUpdEntries];
+  __shared__ unsigned short s_bin[UPD_T * kUpdEntries];
+  __shared__ int s_cnt[kVoxelsPerBlock];
+  __shared__ int s_off[kVoxelsPerBlock];
+  __shared__ int s_cur[kVoxelsPerBlock];
+  __shared__ unsigned s_touch[kVoxelsPerBlock / 32];
+  __shared__ int s_warp[32];
+  __shared__ long long s_seg;
+  const BatchHdr h = *c.hdr;
+  const int t = threadIdx.x;
+  const long long nseg = c.ctr->n_seg;
+  const long long nrec = c.ctr->n_rec_live;
+  const unsigned* rk = c.rec_key[rec_sel];
+  const unsigned* rv = c.rec_val[rec_sel];
+  while (true) {
+    if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
+    __syncthreads();
+    const long long sj = s_seg;
+    __syncthreads();
+    if (sj >= nseg) break;
+    const long long b0 = c.seg_start[sj];
+    const long long b1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
+    const long long phys = h.key_lo + rk[b0];
+    const int item = find_item_global(c.items, h.n_items, (long long)rv[b0]);
+    const ItemDev& it = c.items[item];
+    const MapDev& m = c.maps[it.map];
+    int tkx, tky, tkz;
+    unpack_key(c.slot_key[phys], &tkx, &tky, &tkz);
+    // block centre and bottom-left corner (tsdf_handler.cu:612-624)
+    const float bcx = fadd(fdiv((float)tkx, m.scale_b), m.half_bs);
+    const float bcy = fadd(fdiv((float)tky, m.scale_b), m.half_bs);
+    const float bcz = fadd(fdiv((float)tkz, m.scale_b), m.half_bs);
+    const float blx = fsub(bcx, m.half_bs), bly = fsub(bcy, m.half_bs), blz = fsub(bcz, m.half_bs);
+    float4* gv = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
+    float4* sv4 = reinterpret_cast<float4*>(s_vox);
+    sv4[t] = gv[t];
+    sv4[t + UPD_T] = gv[t + UPD_T];
+    if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
+    unsigned n_upd = 0, n_bad = 0;
+    for (long long cb = b0; cb < b1; cb += UPD_T) {
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_cnt[l] = 0;
+      int ne = 0;
+      if (cb + t < b1) {
+        const long long g = rv[cb + t];
+        const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
+        const float px = p[0], py = p[1], pz = p[2];
+        Seg seg;
+        if (make_segment(px, py, pz, it.ox, it.oy, it.oz, m, &seg)) {
+          Dda dda;
+          dda.init(seg, m.vs, m.scale_v, m.half_vs, m.vmax);
+          bool seen = false;
+          float x, y, z;
+          int kx, ky, kz;
+          while (dda.next(&x, &y, &z, &kx, &ky, &kz)) {
+            float fbx = floorf(fmul(x, m.scale_b));
+            float fby = floorf(fmul(y, m.scale_b));
+            float fbz = floorf(fmul(z, m.scale_b));
+            bool in = (int)fbx == tkx && (int)fby == tky && (int)fbz == tkz;
+            if (!in) {
+              if (seen) break;
+              continue;
+            }
+            seen = true;
+            // getLocalVoxelIndex (tsdf_handler.cu:507-512)
+            float dx = fdiv(fsub(x, blx), m.vs), dy = fdiv(fsub(y, bly), m.vs), dz = fdiv(fsub(z, blz), m.vs);
+            float ix = floorf(dx), iy = floorf(dy), iz = floorf(dz);
+            if (!(ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f) || ne >= kUpdEntries) {
+              ++n_bad;
+              continue;
+            }
+            int local = (int)ix + (int)iy * 8 + (int)iz * 64;
+            s_d[t * kUpdEntries + ne] = distance_update(x, y, z, px, py, pz, it.ox, it.oy, it.oz);
+            s_l[t * kUpdEntries + ne] = (unsigned short)local;
+            ++ne;
+          }
+        }
+      }
+      n_upd += ne;
+      __syncthreads();
+      for (int k = 0; k < ne; ++k) atomicAdd(&s_cnt[s_l[t * kUpdEntries + k]], 1);
+      __syncthreads();
+      {
+        // exclusive scan of 512 counters, 4 per thread
+        int a0 = s_cnt[4 * t], a1 = s_cnt[4 * t + 1], a2 = s_cnt[4 * t + 2], a3 = s_cnt[4 * t + 3];
+        int tot;
+        int ex = block_excl_scan(a0 + a1 + a2 + a3, s_warp, &tot);
+        s_off[4 * t] = ex;
+        s_off[4 * t + 1] = ex + a0;
+        s_off[4 * t + 2] = ex + a0 + a1;
+        s_off[4 * t + 3] = ex + a0 + a1 + a2;
+        s_cur[4 * t] = ex;
+        s_cur[4 * t + 1] = ex + a0;
+        s_cur[4 * t + 2] = ex + a0 + a1;
+        s_cur[4 * t + 3] = ex + a0 + a1 + a2;
+      }
+      __syncthreads();
+      for (int k = 0; k < ne; ++k) {
+        int l = s_l[t * kUpdEntries + k];
+        int pos = atomicAdd(&s_cur[l], 1);
+        s_bin[pos] = (unsigned short)(t * kUpdEntries + k);
+      }
+      __syncthreads();
+      // owners: voxel l by thread l % UPD_T, entries in ascending point order
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+        const int cnt = s_cnt[l];
+        if (!cnt) continue;
+        unsigned short* bin = s_bin + s_off[l];
+        for (int a = 1; a < cnt; ++a) {
+          unsigned short v = bin[a];
+          int b = a - 1;
+          while (b >= 0 && bin[b] > v) {
+            bin[b + 1] = bin[b];
+            --b;
+          }
+          bin[b + 1] = v;
+        }
+        float sdf = s_vox[l].x, w = s_vox[l].y;
+        for (int a = 0; a < cnt; ++a) {
+          const float d = s_d[bin[a]];
+          // getWeightUpdate + update rule (tsdf_handler.cu:579-581, :648-654)
+          const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
+          const float wd = fmul(wt, d);
+          const float nw = fadd(w, wt);
+          sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
+          w = fminf(nw, m.maxw);
+        }
+        s_vox[l] = make_float2(sdf, w);
+        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+      }
+      __syncthreads();
+    }
+    gv[t] = sv4[t];
+    gv[t + UPD_T] = sv4[t + UPD_T];
+    int nz = 0;
+    for (int l = t; l < kVoxelsPerBlock; l += UPD_T) nz += s_vox[l].y != 0.0f;
+    int tot;
+    block_excl_scan(nz, s_warp, &tot);
+    int touched = t < kVoxelsPerBlock / 32 ? __popc(s_touch[t]) : 0;
+    int ttot;
+    block_excl_scan(touched, s_warp, &ttot);
+    int upd_tot;
+    block_excl_scan((int)n_upd, s_warp, &upd_tot);
+    int bad_tot;
+    block_excl_scan((int)n_bad, s_warp, &bad_tot);
+    if (t == 0) {
+      c.nnz[phys] = tot;
+      stat_add(c.item_stats, item, ST_UPD, upd_tot);
+      stat_add(c.item_stats, item, ST_BADLOCAL, bad_tot);
+      stat_add(c.item_stats, item, ST_DVOX, ttot);
+      stat_add(c.item_stats, item, ST_BTOUCH, 1);
+    }
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------------------
+// publish + gc flags over every slot below each map's high water
+__device__ __forceinline__ int find_item_i(const int* base, int n, long long e) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
+  __shared__ int s_sb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
+  __syncthreads();
+  const long long n = c.ctr->n_enum;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    int item = find_item_i(s_sb, h.n_items, e);
+    const ItemDev& it = c.items[item];
+    const MapDev& m = c.maps[it.map];
+    long long phys = m.heap_base + (e - s_sb[item]);
+    unsigned long long key = c.slot_key[phys];
+    int cnt = 0, gc = 0;
+    if (key != kEmptyKey) {
+      int kx, ky, kz;
+      unpack_key(key, &kx, &ky, &kz);
+      float cx = fadd(fdiv((float)kx, m.scale_b), m.half_bs);
+      float cy = fadd(fdiv((float)ky, m.scale_b), m.half_bs);
+      float cz = fadd(fdiv((float)kz, m.scale_b), m.half_bs);
+      // withinDistanceSquared (tsdf_handler.cu:749-757): diff = lidar - block
+      float d2 = sq3(fsub(it.ox, cx), fsub(it.oy, cy), fsub(it.oz, cz));
+      if (d2 <= m.pub_d2) cnt = c.nnz[phys];
+      gc = (d2 <= m.gc_d2) ? 0 : 1;
+      if (cnt > 0) stat_add(c.item_stats, item, ST_PUBBLK, 1);
+    }
+    c.enum_cnt[e] = cnt;
+    c.enum_gc[e] = gc;
+  }
+}
+
+struct ArrIn {
+  const int* a;
+  __device__ int operator()(long long i) const { return a[i]; }
+};
+struct PrefixOut {
+  int* p;
+  __device__ void operator()(long long i, int prefix, int) const { p[i] = prefix; }
+};
+
+// per-item bases of a scanned enumeration array
+__global__ void k_item_bases(Ctx c, const int* prefix, const long long* total, int base_field, int count_field,
+                             int stat_field) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = c.hdr->n_items;
+  const long long ne = c.ctr->n_enum;
+  const long long tot = *total;
+  for (int i = 0; i < n; ++i) {
+    long long sb = c.item_i[i * II_COUNT + II_SLOT_BASE];
+    long long se = sb + c.item_i[i * II_COUNT + II_SLOT_N];
+    long long b = sb < ne ? prefix[sb] : tot;
+    long long e = se < ne ? prefix[se] : tot;
+    c.item_i[i * II_COUNT + base_field] = (int)b;
+    if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
+    if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
+  }
+}
+
+// publish write: one warp per publishing block; voxels in ascending local
+// index (getVoxelCoordinatesFromLocalVoxelIndex, tsdf_handler.cu:520-534)
+__global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
+  __shared__ int s_sb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long n = c.ctr->n_enum;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
+    long long e0 = base + lane;
+    int cnt = e0 < n ? c.enum_cnt[e0] : 0;
+    unsigned work = __ballot_sync(kFull, cnt > 0);
+    while (work) {
+      int src = __ffs(work) - 1;
+      work &= work - 1;
+      long long e = base + src;
+      int item = find_item_i(s_sb, h.n_items, e);
+      const ItemDev& it = c.items[item];
+      const MapDev& m = c.maps[it.map];
+      long long phys = m.heap_base + (e - s_sb[item]);
+      int kx, ky, kz;
+      unpack_key(c.slot_key[phys], &kx, &ky, &kz);
+      const float blx = fsub(fadd(fdiv((float)kx, m.scale_b), m.half_bs), m.half_bs);
+      const float bly = fsub(fadd(fdiv((float)ky, m.scale_b), m.half_bs), m.half_bs);
+      const float blz = fsub(fadd(fdiv((float)kz, m.scale_b), m.half_bs), m.half_bs);
+      long long out = (long long)c.pub_prefix[e] - c.item_i[item * II_COUNT + II_PUB_BASE];
+      const float2* vox = c.voxels + phys * kVoxelsPerBlock;
+      for (int r = 0; r < kVoxelsPerBlock / 32; ++r) {
+        const int l = r * 32 + lane;
+        float2 v = vox[l];
+        bool nzv = v.y != 0.0f;
+        unsigned bm = __ballot_sync(kFull, nzv);
+        if (nzv) {
+          long long o = out + __popc(bm & lt_mask);
+          if (o < it.out_cap) {
+            float x = (float)(l & 7), y = (float)((l >> 3) & 7), z = (float)(l >> 6);
+            it.out_pos[3 * o + 0] = fadd(fadd(fmul(x, m.vs), m.half_vs), blx);
+            it.out_pos[3 * o + 1] = fadd(fadd(fmul(y, m.vs), m.half_vs), bly);
+            it.out_pos[3 * o + 2] = fadd(fadd(fmul(z, m.vs), m.half_vs), blz);
+            it.out_data[o] = v;
+          }
+        }
+        out += __popc(bm);
+      }
+    }
+  }
+}
+
+// gc apply: free_list push in ascending slot order, entry tombstoned
+__global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
+  __shared__ int s_sb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
+  __syncthreads();
+  const long long n = c.ctr->n_enum;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    if (!c.enum_gc[e]) continue;
+    int item = find_item_i(s_sb, h.n_items, e);
+    const int mi = c.items[item].map;
+    const MapDev& m = c.maps[mi];
+    const int slot = (int)(e - s_sb[item]);
+    const long long phys = m.heap_base + slot;
+    const int r = c.gc_prefix[e] - c.item_i[item * II_COUNT + II_GC_BASE];
+    const int bc = c.mctr[mi].block_count;
+    c.free_list[m.heap_base + bc - 1 - r] = slot;
+    unsigned long long key = c.slot_key[phys];
+    c.slot_key[phys] = kEmptyKey;
+    c.nnz[phys] = 0;
+    HEntry* tab = c.hash + m.hash_base;
+    long long ei = thread_find_entry(tab, m.hash_mask, bucket_size, key);
+    if (ei >= 0) {
+      tab[ei].slot = -1;
+      tab[ei].rank = kRankNone;
+      tab[ei].key = kTombKey;
+    } else {
+      set_error(c.ctr, ERR_HASH_FULL);
+    }
+  }
+}
+
+__global__ void k_gc_finalize(Ctx c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = c.hdr->n_items;
+  for (int i = 0; i < n; ++i) {
+    int mi = c.items[i].map;
+    int g = c.item_i[i * II_COUNT + II_GC_N];
+    c.mctr[mi].block_count -= g;
+    c.item_stats[i * ST_COUNT + ST_GC] = g;
+    c.item_stats[i * ST_COUNT + ST_BC] = c.mctr[mi].block_count;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// map maintenance
+__global__ void k_map_init(int* free_list, unsigned long long* slot_key, int* nnz, long long heap_base,
+                           long long cap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cap; i += (long long)gridDim.x * blockDim.x) {
+    free_list[heap_base + i] = (int)i;
+    slot_key[heap_base + i] = kEmptyKey;
+    nnz[heap_base + i] = 0;
+  }
+}
+
+__global__ void k_map_rehash(Ctx c, int G, long long heap_base, long long hw, long long hash_base, unsigned mask,
+                             int* used, int* err) {
+  HEntry* tab = c.hash + hash_base;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < hw; s += (long long)gridDim.x * blockDim.x) {
+    unsigned long long key = c.slot_key[heap_base + s];
+    if (key == kEmptyKey) continue;
+    const unsigned long long h = mix64(key);
+    bool done = false;
+    for (unsigned p = 0; p <= mask && !done; ++p) {
+      unsigned b = (unsigned)(h + p) & mask;
+      for (int i = 0; i < G && !done; ++i) {
+        HEntry* e = tab + (size_t)b * G + i;
+        if (atomicCAS(&e->key, kEmptyKey, key) == kEmptyKey) {
+          e->slot = (int)s;
+          e->rank = kRankNone;
+          atomicAdd(used, 1);
+          done = true;
+        }
+      }
+    }
+    if (!done) atomicOr(err, ERR_HASH_FULL);
+  }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------
+// stage launchers
+void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  k_step_init<<<8, 256, 0, s>>>(c);
+  *launches += 1;
+}
+
+void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  const int grid = lc.sm_count * (2048 / lc.ray_threads);
+  switch (lc.bucket_size) {
+    case 4: k_ray_blocks<4><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 16: k_ray_blocks<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    default: k_ray_blocks<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
+  }
+  *launches += 1;
+}
+
+void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c);
+  *launches += 1;
+  radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
+             lc.rank_passes, c.max_tiles_rank, lc.sm_count, s, launches);
+  k_alloc_prefix<<<1, 32, 0, s>>>(c);
+  *launches += 1;
+}
+
+void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1);
+  k_alloc_finalize<<<1, 32, 0, s>>>(c);
+  *launches += 2;
+}
+
+void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  const int grid = lc.sm_count * (2048 / lc.ray_threads);
+  switch (lc.bucket_size) {
+    case 4: k_ray_voxels<4><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 16: k_ray_voxels<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    default: k_ray_voxels<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
+  }
+  *launches += 1;
+}
+
+void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  radix_sort(c, c.rec_key, c.rec_val, &c.hdr->rec_total, kRecSentinel, &c.ctr->n_rec_live, c.rec_cap,
+             lc.rec_passes, c.max_tiles_rec, lc.sm_count, s, launches);
+  const int sel = lc.rec_passes & 1;
+  SegHeadIn fin{c.rec_key[sel]};
+  SegHeadOut fout{c.seg_start};
+  const int grid = lc.sm_count * 2;
+  k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums);
+  k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_rec_live, &c.ctr->n_seg);
+  k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
+  *launches += 3;
+}
+
+void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, lc.rec_passes & 1);
+  *launches += 1;
+}
+
+void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  const int grid = lc.sm_count * 2;
+  k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c);
+  ArrIn cin{c.enum_cnt};
+  PrefixOut pout{c.pub_prefix};
+  k_scan_reduce<<<grid, SC_T, 0, s>>>(cin, &c.ctr->n_enum, c.tile_sums);
+  k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_enum, &c.ctr->scan_total);
+  k_scan_apply<<<grid, SC_T, 0, s>>>(cin, pout, &c.ctr->n_enum, c.tile_sums);
+  k_item_bases<<<1, 32, 0, s>>>(c, c.pub_prefix, &c.ctr->scan_total, II_PUB_BASE, -1, ST_PUB);
+  k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c);
+  *launches += 6;
+}
+
+void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  const int grid = lc.sm_count * 2;
+  ArrIn gin{c.enum_gc};
+  PrefixOut gout{c.gc_prefix};
+  k_scan_reduce<<<grid, SC_T, 0, s>>>(gin, &c.ctr->n_enum, c.tile_sums);
+  k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_enum, &c.ctr->scan_total);
+  k_scan_apply<<<grid, SC_T, 0, s>>>(gin, gout, &c.ctr->n_enum, c.tile_sums);
+  k_item_bases<<<1, 32, 0, s>>>(c, c.gc_prefix, &c.ctr->scan_total, II_GC_BASE, II_GC_N, -1);
+  k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
+  k_gc_finalize<<<1, 32, 0, s>>>(c);
+  *launches += 6;
+}
+
+void launch_map_init(float2* voxels, unsigned long long* slot_key, int* nnz, int* free_list, HEntry* hash,
+                     long long heap_base, long long heap_cap, long long hash_base, long long hash_entries,
+                     cudaStream_t s) {
+  (void)voxels;
+  k_map_init<<<256, 256, 0, s>>>(free_list, slot_key, nnz, heap_base, heap_cap);
+  cudaMemsetAsync(hash + hash_base, 0xFF, (size_t)hash_entries * sizeof(HEntry), s);
+}
+
+void launch_map_rehash(const Ctx& c, int map, int bucket_size, long long heap_base, long long heap_hw,
+                       long long hash_base, long long hash_entries, unsigned hash_mask, int* d_used, int* d_err,
+                       cudaStream_t s) {
+  (void)map;
+  cudaMemsetAsync(c.hash + hash_base, 0xFF, (size_t)hash_entries * sizeof(HEntry), s);
+  cudaMemsetAsync(d_used, 0, sizeof(int), s);
+  k_map_rehash<<<256, 256, 0, s>>>(c, bucket_size, heap_base, heap_hw, hash_base, hash_mask, d_used, d_err);
+}
+
+void launch_flush(void* buf, long long bytes, int value, cudaStream_t s) { cudaMemsetAsync(buf, value, bytes, s); }
+
+}  // namespace tsdfg

@@ -1,0 +1,305 @@
+"""Python front end of the GB300 TSDF engine (thin ctypes layer over libtsdf_gb300.so).
+
+The compute path is the CUDA engine only: every call goes through the C-ABI,
+and importing this module fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+
+class TsdfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{L.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+# statuses that describe a completed scan (results valid) rather than a failure
+SOFT = (L.OK, L.WARN_PUBLISH_OVERFLOW, L.ERR_HEAP_FULL, L.ERR_BAD_POINTS)
+
+
+@dataclass
+class TsdfParams:
+    """The five initGlobalVars parameters (tsdf_handler.cu:1289)."""
+    voxel_size: float
+    truncation_distance: float
+    max_weight: float
+    publish_distance_squared: float
+    garbage_collect_distance_squared: float
+
+    def c(self) -> L.Params:
+        return L.Params(self.voxel_size, self.truncation_distance, self.max_weight,
+                        self.publish_distance_squared, self.garbage_collect_distance_squared)
+
+
+@dataclass
+class ScanResult:
+    pos: np.ndarray          # (count, 3) float32 (truncated at pub_cap)
+    data: np.ndarray         # (count, 2) float32: sdf, weight
+    count: int               # full publish count
+    status: int
+    stats: dict = field(default_factory=dict)
+
+
+def _as_points(xyz) -> tuple[np.ndarray, int]:
+    a = np.ascontiguousarray(xyz, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] not in (3, 4):
+        raise ValueError("points must be (N, 3) or (N, 4) float32")
+    return a, a.shape[1] * 4
+
+
+class Engine:
+    def __init__(self, device: int = 0, max_maps: int = 64, pool_blocks: int = 1 << 18,
+                 max_batch_points: int = 1 << 20, max_publish: int = 1 << 23, bucket_size: int = 8,
+                 ray_threads: int = 256, ray_chunk: int = 256, max_routes: int = 16, lanes: int = 1,
+                 graphs: bool = True):
+        self.lib = L.load()
+        cfg = L.EngineCfg(device, max_maps, pool_blocks, max_batch_points, max_publish, bucket_size,
+                          ray_threads, ray_chunk, max_routes, lanes, 0 if graphs else 1)
+        h = C.c_void_p()
+        st = self.lib.tsdf_engine_create(C.byref(cfg), C.byref(h))
+        if st != L.OK:
+            raise TsdfError(st, "tsdf_engine_create failed (device, capacities or CUDA)")
+        self.h = h
+        self.cfg = cfg
+        sm = C.c_int()
+        self.lib.tsdf_engine_get_cfg(self.h, C.byref(self.cfg), C.byref(sm))
+        self.sm_count = sm.value
+        self._keep = {}
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tsdf_engine_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int, what: str, soft: bool = False):
+        if st == L.OK or (soft and st in SOFT):
+            return st
+        raise TsdfError(st, f"{what}: {self.lib.tsdf_last_error(self.h).decode(errors='replace')}")
+
+    # -- maps -------------------------------------------------------------
+    def create_map(self, params: TsdfParams, heap_blocks: int) -> int:
+        mid = C.c_int()
+        self._check(self.lib.tsdf_map_create(self.h, C.byref(params.c()), int(heap_blocks), C.byref(mid)),
+                    "tsdf_map_create")
+        return mid.value
+
+    def destroy_map(self, map_id: int):
+        self._check(self.lib.tsdf_map_destroy(self.h, int(map_id)), "tsdf_map_destroy")
+
+    def map_info(self, map_id: int) -> dict:
+        mi = L.MapInfo()
+        self._check(self.lib.tsdf_map_info_get(self.h, int(map_id), C.byref(mi)), "tsdf_map_info_get")
+        return {f: int(getattr(mi, f)) for f, _ in L.MapInfo._fields_}
+
+    # -- integration --------------------------------------------------------
+    def integrate(self, map_id: int, xyz, origin, pub_cap: int = 400000) -> ScanResult:
+        return self.integrate_batch([(map_id, xyz, origin)], pub_cap=pub_cap)[0]
+
+    def integrate_batch(self, scans, pub_cap=400000, outputs=None) -> list[ScanResult]:
+        """scans: list of (map_id, points (N,3|4) float32, origin (3,)).
+        outputs: optional list of (pos (cap,3) float32, data (cap,2) float32) arrays to write into."""
+        n = len(scans)
+        sc = (L.Scan * n)()
+        rs = (L.ScanResult * n)()
+        keep = []
+        outs = []
+        for i, (mid, xyz, org) in enumerate(scans):
+            a, stride = _as_points(xyz)
+            keep.append(a)
+            sc[i].map_id = int(mid)
+            sc[i].stride_bytes = stride
+            sc[i].n_points = a.shape[0]
+            sc[i].xyz = a.ctypes.data if a.shape[0] else None
+            sc[i].origin[:] = [float(v) for v in org]
+            if outputs is not None:
+                pos, data = outputs[i]
+                cap = pos.shape[0]
+            else:
+                cap = int(pub_cap[i] if isinstance(pub_cap, (list, tuple)) else pub_cap)
+                pos = np.empty((cap, 3), np.float32)
+                data = np.empty((cap, 2), np.float32)
+            outs.append((pos, data))
+            rs[i].pub_pos = pos.ctypes.data
+            rs[i].pub_data = data.ctypes.data
+            rs[i].pub_cap = cap
+        st = self.lib.tsdf_integrate_batch(self.h, n, sc, rs)
+        self._check(st, "tsdf_integrate_batch", soft=True)
+        res = []
+        for i in range(n):
+            k = min(rs[i].pub_count, rs[i].pub_cap)
+            res.append(ScanResult(outs[i][0][:k], outs[i][1][:k], int(rs[i].pub_count), int(rs[i].status),
+                                  rs[i].stats.to_dict()))
+        return res
+
+    # -- served mode --------------------------------------------------------
+    def submit(self, map_id: int, xyz, origin, pub_cap: int = 400000):
+        """Queue a scan; returns a handle for wait().  Buffers are kept alive by the handle."""
+        a, stride = _as_points(xyz)
+        sc = L.Scan()
+        sc.map_id = int(map_id)
+        sc.stride_bytes = stride
+        sc.n_points = a.shape[0]
+        sc.xyz = a.ctypes.data if a.shape[0] else None
+        sc.origin[:] = [float(v) for v in origin]
+        pos = np.empty((pub_cap, 3), np.float32)
+        data = np.empty((pub_cap, 2), np.float32)
+        rs = L.ScanResult()
+        rs.pub_pos = pos.ctypes.data
+        rs.pub_data = data.ctypes.data
+        rs.pub_cap = pub_cap
+        t = C.c_uint64()
+        self._check(self.lib.tsdf_submit(self.h, C.byref(sc), C.byref(rs), C.byref(t)), "tsdf_submit")
+        handle = (t.value, a, sc, rs, pos, data)
+        self._keep[t.value] = handle
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        st = self.lib.tsdf_poll(self.h, ticket)
+        if st == L.ERR_NOT_READY:
+            return False
+        self._check(st, "tsdf_poll")
+        return True
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> ScanResult:
+        st = self.lib.tsdf_wait(self.h, ticket, timeout_ms)
+        self._check(st, "tsdf_wait")
+        _, _, _, rs, pos, data = self._keep[ticket]
+        times = [C.c_int64(), C.c_int64(), C.c_int64()]
+        self.lib.tsdf_ticket_times(self.h, ticket, *[C.byref(x) for x in times])
+        self.lib.tsdf_forget(self.h, ticket)
+        del self._keep[ticket]
+        k = min(rs.pub_count, rs.pub_cap)
+        r = ScanResult(pos[:k], data[:k], int(rs.pub_count), int(rs.status), rs.stats.to_dict())
+        r.stats["t_submit_ns"], r.stats["t_launch_ns"], r.stats["t_done_ns"] = (x.value for x in times)
+        return r
+
+    # -- inspection -----------------------------------------------------------
+    def dump_blocks(self, map_id: int):
+        """(kxyz (n,3) int32, slots (n,) int32) in ascending slot."""
+        cnt = C.c_int64()
+        self._check(self.lib.tsdf_dump_blocks(self.h, map_id, None, None, 0, C.byref(cnt)), "tsdf_dump_blocks")
+        n = cnt.value
+        k = np.empty((max(n, 1), 3), np.int32)
+        s = np.empty(max(n, 1), np.int32)
+        self._check(self.lib.tsdf_dump_blocks(self.h, map_id, k.ctypes.data, s.ctypes.data, n, C.byref(cnt)),
+                    "tsdf_dump_blocks")
+        return k[:n], s[:n]
+
+    def dump_free_list(self, map_id: int):
+        info = self.map_info(map_id)
+        out = np.empty(info["heap_blocks"], np.int32)
+        bc = C.c_int64()
+        self._check(self.lib.tsdf_dump_free_list(self.h, map_id, out.ctypes.data, out.shape[0], C.byref(bc)),
+                    "tsdf_dump_free_list")
+        return out, bc.value
+
+    def dump_block_voxels(self, map_id: int, slot: int) -> np.ndarray:
+        out = np.empty((512, 2), np.float32)
+        self._check(self.lib.tsdf_dump_block_voxels(self.h, map_id, int(slot), out.ctypes.data),
+                    "tsdf_dump_block_voxels")
+        return out
+
+    # -- measurement ----------------------------------------------------------
+    def set_stage_timing(self, on: bool):
+        self._check(self.lib.tsdf_set_stage_timing(self.h, 1 if on else 0), "tsdf_set_stage_timing")
+
+    def stage_times(self) -> dict:
+        n = C.c_int(16)
+        names = (C.c_char_p * 16)()
+        ms = (C.c_double * 16)()
+        cnt = (C.c_int64 * 16)()
+        self._check(self.lib.tsdf_stage_times(self.h, names, ms, cnt, C.byref(n)), "tsdf_stage_times")
+        return {names[i].decode(): (ms[i], int(cnt[i])) for i in range(n.value)}
+
+    def reset_stage_times(self):
+        self.lib.tsdf_reset_stage_times(self.h)
+
+    def flush_l2(self):
+        self._check(self.lib.tsdf_flush_l2(self.h), "tsdf_flush_l2")
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.tsdf_kernel_launches(self.h))
+
+    # -- buffers --------------------------------------------------------------
+    def device_array(self, host: np.ndarray) -> "DeviceBuffer":
+        return DeviceBuffer(self, host)
+
+    def pinned_empty(self, shape, dtype=np.float32) -> np.ndarray:
+        return pinned_empty(self.lib, shape, dtype)
+
+
+class DeviceBuffer:
+    """A device copy of a host array, freed with the engine."""
+
+    def __init__(self, eng: Engine, host: np.ndarray):
+        self.eng = eng
+        host = np.ascontiguousarray(host)
+        self.shape = host.shape
+        self.dtype = host.dtype
+        self.nbytes = host.nbytes
+        p = C.c_void_p()
+        eng._check(eng.lib.tsdf_device_alloc(eng.h, C.byref(p), self.nbytes), "tsdf_device_alloc")
+        self.ptr = p.value
+        if self.nbytes:
+            eng._check(eng.lib.tsdf_copy(eng.h, C.c_void_p(self.ptr), host.ctypes.data, self.nbytes, 0), "tsdf_copy")
+
+    def to_host(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        if self.nbytes:
+            self.eng._check(self.eng.lib.tsdf_copy(self.eng.h, out.ctypes.data, C.c_void_p(self.ptr), self.nbytes, 1),
+                            "tsdf_copy")
+        return out
+
+    def free(self):
+        if self.ptr and self.eng.h:
+            self.eng.lib.tsdf_device_free(self.eng.h, C.c_void_p(self.ptr))
+        self.ptr = None
+
+
+class _PinnedOwner:
+    def __init__(self, lib, ptr):
+        self.lib, self.ptr = lib, ptr
+
+    def __del__(self):
+        try:
+            self.lib.tsdf_host_free(C.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+def pinned_empty(lib, shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory (freed when garbage-collected)."""
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    p = C.c_void_p()
+    st = lib.tsdf_host_alloc(C.byref(p), max(nbytes, 1))
+    if st != L.OK:
+        raise TsdfError(st, "tsdf_host_alloc")
+    buf = (C.c_char * max(nbytes, 1)).from_address(p.value)
+    arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+    arr_owner = _PinnedOwner(lib, p.value)
+    arr.flags.writeable = True
+    _pinned_owners[id(arr)] = arr_owner
+    return arr
+
+
+_pinned_owners: dict = {}
