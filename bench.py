@@ -1,0 +1,440 @@
+"""Benchmark of the TSDF integration step on GB300.
+
+Workload (default "multimap32"): 32 independent maps with the plain_small
+parameters (voxel 0.5 m, truncation 4 m, max weight 1000, publish d2 2500,
+gc d2 250000), each with its own seeded scene, circular trajectory and lidar of
+{16,32,64} channels x {64,256,1024} azimuths; every step integrates one scan
+into every map (one batched device step, replayed from a CUDA graph).
+Synthetic scans stand in for the reference's private AirSim recordings.
+
+value   points integrated / s, inputs resident in HBM, device time from CUDA
+        events recorded on the engine's stream around the step's kernels; L2
+        is flushed (512 MiB write) between timed steps.
+e2e     same workload through tsdf_integrate_batch with pinned host input and
+        output buffers: host->device copy of the points and the publish
+        output landing in host memory are inside the (wall-clock) timed step.
+plain   the same scans integrated one scan per call (tsdf_integrate), the
+        reference's calling pattern.
+
+--impl reference times the reference's algorithm on the host cores (the CPU
+oracle, a restatement of ros_tsdf's integration call; the CUDA original
+cannot be built: it needs CUDA dynamic parallelism with device-side
+cudaDeviceSynchronize, removed in CUDA 12+, plus Eigen/PCL/ROS2).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "points integrated/s (batched multi-map step)"
+UNIT = "points/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="multimap32", choices=["multimap32", "plain_small", "large_stream"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--heap-blocks", type=int, default=1 << 16, help="per-map heap capacity (blocks)")
+    ap.add_argument("--pub-cap", type=int, default=1 << 20)
+    ap.add_argument("--json-out", default=None)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_init(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+def make_workload(name: str, rank: int, heap_blocks: int = 1 << 16):
+    from ros_tsdf_gb300 import workloads as W
+
+    if name == "multimap32":
+        specs = W.multimap32(32, base_seed=1000 + 100 * rank, heap_blocks=heap_blocks)
+    elif name == "plain_small":
+        specs = [W.plain_small(seed=rank, heap_blocks=heap_blocks)]
+    else:
+        specs = [W.large_stream(seed=2000 + rank, heap_blocks=max(heap_blocks, 1 << 21))]
+    return specs
+
+
+def gen_scans(specs, n_steps: int):
+    from ros_tsdf_gb300 import workloads as W
+
+    out = []
+    for sp in specs:
+        src = W.ScanSource(sp)
+        out.append([src.scan(k) for k in range(n_steps)])
+    return out
+
+
+def mean_stats(all_stats):
+    keys = all_stats[0][0].keys()
+    return {k: float(np.mean([sum(s[k] for s in step) for step in all_stats])) for k in keys}
+
+
+def run_ours(args, rank, world, local, pg):
+    from ros_tsdf_gb300 import Engine
+
+    specs = make_workload(args.workload, rank, args.heap_blocks)
+    n_steps = args.warmup + args.steps
+    scans = gen_scans(specs, n_steps)
+    pts_per_step = [sum(scans[m][k][0].shape[0] for m in range(len(specs))) for k in range(n_steps)]
+    timed_pts = float(sum(pts_per_step[args.warmup:]))
+    pool = sum(s.heap_blocks for s in specs) + 1024
+    max_pts = max(pts_per_step) + 1024
+    cap = args.pub_cap
+
+    def new_engine(**kw):
+        return Engine(device=local, max_maps=max(64, len(specs)), pool_blocks=pool, max_batch_points=max_pts,
+                      max_publish=cap * len(specs), **kw)
+
+    # ---- value: device-resident inputs and outputs, CUDA-event device time
+    eng = new_engine()
+    mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+    dev_in = [[eng.device_array(scans[m][k][0]) for k in range(n_steps)] for m in range(len(specs))]
+    dev_pos = [eng.device_array(np.zeros((cap, 3), np.float32)) for _ in specs]
+    dev_dat = [eng.device_array(np.zeros((cap, 2), np.float32)) for _ in specs]
+    import ctypes as C
+    from ros_tsdf_gb300 import _lib as L
+
+    def batch_call(e, k, inputs, outs_pos, outs_dat, caps):
+        n = len(specs)
+        sc = (L.Scan * n)()
+        rs = (L.ScanResult * n)()
+        for m in range(n):
+            sc[m].map_id = mids_of[e][m]
+            sc[m].stride_bytes = 12
+            sc[m].n_points = scans[m][k][0].shape[0]
+            sc[m].xyz = inputs(m, k)
+            sc[m].origin[:] = [float(v) for v in scans[m][k][1]]
+            rs[m].pub_pos = outs_pos(m)
+            rs[m].pub_data = outs_dat(m)
+            rs[m].pub_cap = caps
+        st = e.lib.tsdf_integrate_batch(e.h, n, sc, rs)
+        if st not in (0, 2, 3, 10):
+            raise RuntimeError(f"tsdf_integrate_batch: {st} {e.lib.tsdf_last_error(e.h)}")
+        return [rs[m].stats.to_dict() for m in range(n)], [rs[m].status for m in range(n)]
+
+    mids_of = {eng: mids}
+    stats_steps = []
+    dev_ms = []
+    eng.set_stage_timing(True)
+    stage_acc = {}
+    launches0 = 0
+    barrier(pg)
+    with ClockSampler(local) as clk:
+        for k in range(n_steps):
+            if k == args.warmup:
+                eng.reset_stage_times()
+                launches0 = eng.kernel_launches()
+            eng.flush_l2()
+            before = eng.stage_times()
+            st, stat = batch_call(eng, k, lambda m, kk: dev_in[m][kk].ptr, lambda m: dev_pos[m].ptr,
+                                  lambda m: dev_dat[m].ptr, cap)
+            after = eng.stage_times()
+            step_ms = sum(after[s][0] - before[s][0] for s in after)
+            if k >= args.warmup:
+                dev_ms.append(step_ms)
+                stats_steps.append(st)
+    gpu_launches = eng.kernel_launches() - launches0
+    stage_acc = eng.stage_times()
+    clocks = clk.summary()
+    t_dev = sum(dev_ms) / 1000.0
+    t_dev = max_over_ranks(pg, t_dev)
+    total_pts = sum_over_ranks(pg, timed_pts)
+    value = total_pts / t_dev
+    ms_per_step = t_dev * 1000.0 / args.steps
+    mstats = mean_stats(stats_steps)
+    for lst in dev_in:
+        for b in lst:
+            b.free()
+    eng.close()
+
+    # ---- e2e: pinned host buffers through the C-ABI, wall clock
+    if args.no_e2e:
+        return dict(value=value, ms_per_step=ms_per_step, e2e=None, plain=None, stats=mstats, stages=stage_acc,
+                    clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
+                    dev_ms=dev_ms)
+    eng2 = new_engine()
+    mids_of[eng2] = [eng2.create_map(s.params, s.heap_blocks) for s in specs]
+    pin_in = []
+    for m in range(len(specs)):
+        row = []
+        for k in range(n_steps):
+            a = eng2.pinned_empty(scans[m][k][0].shape, np.float32)
+            a[:] = scans[m][k][0]
+            row.append(a)
+        pin_in.append(row)
+    pin_pos = [eng2.pinned_empty((cap, 3), np.float32) for _ in specs]
+    pin_dat = [eng2.pinned_empty((cap, 2), np.float32) for _ in specs]
+    e2e_t = 0.0
+    h2d = d2h = 0
+    barrier(pg)
+    for k in range(n_steps):
+        eng2.flush_l2()
+        t0 = time.perf_counter()
+        st, _ = batch_call(eng2, k, lambda m, kk: pin_in[m][kk].ctypes.data, lambda m: pin_pos[m].ctypes.data,
+                           lambda m: pin_dat[m].ctypes.data, cap)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            e2e_t += dt
+            h2d += sum(scans[m][k][0].nbytes for m in range(len(specs)))
+            d2h += sum(min(s["published"], cap) * 20 + 18 * 8 for s in st)
+    eng2.close()
+    e2e_t = max_over_ranks(pg, e2e_t)
+    e2e = {"value": total_pts / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+           "d2h_bytes_per_step": int(d2h / args.steps), "ms_per_step": e2e_t * 1000.0 / args.steps,
+           "path": "tsdf_integrate_batch, pinned host in/out (publish kernel writes host memory over C2C)"}
+
+    # ---- plain: one scan per call, host pageable arrays (reference calling pattern)
+    plain = None
+    if not args.no_plain:
+        eng3 = new_engine()
+        pm = [eng3.create_map(s.params, s.heap_blocks) for s in specs]
+        outp = np.empty((cap, 3), np.float32)
+        outd = np.empty((cap, 2), np.float32)
+        tp = 0.0
+        for k in range(n_steps):
+            t0 = time.perf_counter()
+            for m in range(len(specs)):
+                eng3.integrate_batch([(pm[m], scans[m][k][0], scans[m][k][1])], outputs=[(outp, outd)])
+            dt = time.perf_counter() - t0
+            if k >= args.warmup:
+                tp += dt
+        eng3.close()
+        tp = max_over_ranks(pg, tp)
+        plain = {"value": total_pts / tp, "unit": UNIT, "ms_per_step": tp * 1000.0 / args.steps,
+                 "path": "tsdf_integrate one scan per call, pageable host in/out"}
+
+    return dict(value=value, ms_per_step=ms_per_step, e2e=e2e, plain=plain, stats=mstats, stages=stage_acc,
+                clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
+                dev_ms=dev_ms)
+
+
+def algorithmic_bytes(s: dict) -> dict:
+    """Per-step algorithmic bytes ('Roofline')."""
+    whole = (12 * s["n_points"] + 16 * s["distinct_voxels"] + 16 * s["blocks_touched"] + 20 * s["new_blocks"]
+             + 16 * s["alloc_blocks_before"] + 4096 * s["published_blocks"] + 20 * s["published"]
+             + 16 * s["alloc_blocks_before"] + 20 * s["gc_blocks"])
+    update = 8192 * s["blocks_touched"]
+    publish = 4096 * s["published_blocks"] + 20 * s["published"] + 24 * s["alloc_blocks_before"]
+    return {"step": whole, "update": update, "publish": publish}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline_run(specs, scans, n_steps, warmup, threads):
+    """The oracle (reference algorithm as host code) on the same scans."""
+    import oracle as O
+
+    maps = [O.OracleMap(s.params, s.heap_blocks) for s in specs]
+    t = 0.0
+    pts = 0
+    for k in range(n_steps):
+        xs = [scans[m][k][0] for m in range(len(specs))]
+        orgs = [scans[m][k][1] for m in range(len(specs))]
+        t0 = time.perf_counter()
+        O.integrate_many(maps, xs, orgs, pub_cap=0, threads=threads)
+        dt = time.perf_counter() - t0
+        if k >= warmup:
+            t += dt
+            pts += sum(x.shape[0] for x in xs)
+    return pts / t, t
+
+
+def traffic_from_profiles(kernel: str):
+    """Per-unit DRAM bytes of `kernel` from a committed ncu summary, if present."""
+    p = ROOT / "profiles" / f"{kernel}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_unit:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_init(args.gpus)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        specs = make_workload(args.workload, 0, args.heap_blocks)
+        n_steps = args.warmup + args.steps
+        scans = gen_scans(specs, n_steps)
+        threads = os.cpu_count() or 1
+        v, t = cpu_baseline_run(specs, scans, n_steps, args.warmup, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000.0 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
+                "config": {"workload": args.workload, "maps": len(specs), "per_step": "one scan per map"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": min(threads, len(specs)), "kind": "port",
+                                 "sample": f"all {args.steps} timed steps of the workload ({args.warmup} warm-up), "
+                                           "one host thread per map"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference CUDA path unbuildable here (CDP1 device-side cudaDeviceSynchronize is "
+                        "rejected by CUDA 13; Eigen/PCL/ROS2 absent); timed its algorithm as host code"}
+        print(json.dumps(line))
+        return
+    r = run_ours(args, rank, world, local, pg)
+    peak, peak_kind = load_peaks()
+    ab = algorithmic_bytes(r["stats"])
+    stages = r["stages"]
+    n = args.steps
+    stage_ms = {k: v[0] / max(v[1], 1) for k, v in stages.items()}
+    dom = max(stage_ms, key=stage_ms.get)
+    if dom == "update":
+        dom_bytes, kernel = ab["update"], "k_update"
+    elif dom == "publish":
+        dom_bytes, kernel = ab["publish"], "k_pub_write"
+    else:
+        dom_bytes, kernel = ab["step"] * stage_ms[dom] / max(sum(stage_ms.values()), 1e-9), dom
+    achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
+    step_gbs = ab["step"] / (r["ms_per_step"] / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": n, "warmup": args.warmup,
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
+        "config": {"workload": args.workload, "maps": len(r["specs"]),
+                   "points_per_step": r["timed_pts"] / n, "voxel_size": 0.5, "truncation_distance": 4.0,
+                   "l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step"},
+        "e2e": r["e2e"], "plain": r["plain"],
+        "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic_from_profiles(kernel),
+                     "step_achieved_gbs": step_gbs, "step_frac": step_gbs / peak},
+        "stage_ms_per_step": stage_ms,
+        "per_step": {k: r["stats"][k] for k in ("n_points", "voxel_updates", "distinct_voxels", "blocks_touched",
+                                                "new_blocks", "published", "published_blocks", "gc_blocks")},
+        "voxel_updates_per_s": r["stats"]["voxel_updates"] / (r["ms_per_step"] / 1000.0),
+        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"],
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = min(os.cpu_count() or 1, len(r["specs"]))
+        v, t = cpu_baseline_run(r["specs"], r["scans"], min(args.warmup + 3, args.warmup + args.steps),
+                                args.warmup, threads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"first {args.warmup} steps untimed then 3 timed steps of the same "
+                                          "workload, one host thread per map"}
+    if rank == 0:
+        print(json.dumps(line))
+        if args.json_out:
+            Path(args.json_out).write_text(json.dumps(line, indent=1))
+
+
+if __name__ == "__main__":
+    main()

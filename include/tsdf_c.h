@@ -85,7 +85,7 @@ typedef struct tsdf_engine_cfg {
   int64_t max_publish;      /* published voxels per step, staging (default 8M)*/
   int bucket_size;          /* hash entries per bucket: 4, 8 or 16 (def. 8)   */
   int ray_threads;          /* threads per CTA of the ray kernels (def. 256)  */
-  int ray_chunk;            /* points per work-queue item (default 256)       */
+  int ray_chunk;            /* points per work-queue item (default 32)        */
   int max_routes;           /* per-point block routes of the voxel pass (16)  */
   int lanes;                /* batches in flight at once (default 1, max 4)   */
   int no_graphs;            /* 1: launch kernels directly; 0 (default): each

@@ -1,0 +1,154 @@
+// tsdf_handler.hpp - C++ drop-in for ros_tsdf's TSDFHandler surface, header-only
+// over the C-ABI in tsdf_c.h (link libtsdf_gb300.so).
+//
+// Mirrors tsdf_package/include/cuda/tsdf_handler.cuh:41-81 of ros_tsdf:
+//   tsdf::initGlobalVars(voxel_size, truncation_distance, max_weight,
+//                        publish_distance_squared,
+//                        garbage_collect_distance_squared);      // :80-81
+//   tsdf::TSDFHandler handler;                                    // :44
+//   handler.processPointCloudAndUpdateVoxels(cloud, &lidar_position,
+//       publish_voxels_pos, &publish_voxels_size, publish_voxels_data); // :50-51
+// with PCL/Eigen replaced by layout-compatible PODs: PointXYZ is 16 bytes
+// (pcl::PointXYZ), Vector3f 12 bytes (Eigen::Matrix<float,3,1>), Voxel is
+// {sdf, weight} (tsdf_container.cuh:40-46).
+//
+// Semantics kept from the reference: initGlobalVars must come first; the
+// output arrays are caller-owned with PUBLISH_VOXELS_MAX_SIZE entries;
+// *publish_voxels_size is in/out (writing starts at its input value,
+// tsdf_handler.cu:1200-1214).  Changed: errors throw std::runtime_error
+// instead of exit() (tsdf_handler.cu:14-22).
+#ifndef TSDF_HANDLER_HPP
+#define TSDF_HANDLER_HPP
+
+#include <cstdint>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tsdf_c.h"
+
+namespace tsdf {
+
+constexpr int PUBLISH_VOXELS_MAX_SIZE = 400000;  // tsdf_handler.cuh:15-16
+constexpr int NUM_HEAP_BLOCKS = 524288;          // tsdf_container.cuh:31
+
+struct PointXYZ {  // pcl::PointXYZ layout
+  float x, y, z, pad;
+};
+
+struct Vector3f {  // Eigen::Matrix<float, 3, 1> storage
+  float data[3];
+  float& operator()(int i) { return data[i]; }
+  float operator()(int i) const { return data[i]; }
+  float x() const { return data[0]; }
+  float y() const { return data[1]; }
+  float z() const { return data[2]; }
+};
+
+using Voxel = tsdf_voxel;
+
+static_assert(sizeof(PointXYZ) == 16, "PointXYZ must match pcl::PointXYZ");
+static_assert(sizeof(Vector3f) == 12, "Vector3f must match Eigen::Vector3f");
+static_assert(sizeof(Voxel) == 8, "Voxel must be {sdf, weight}");
+
+namespace detail {
+struct Globals {
+  tsdf_params params{};
+  bool set = false;
+  tsdf_engine* engine = nullptr;
+  std::mutex mu;
+};
+inline Globals& globals() {
+  static Globals g;
+  return g;
+}
+inline void check(tsdf_engine* e, tsdf_status s, const char* what) {
+  if (s == TSDF_OK || s == TSDF_WARN_PUBLISH_OVERFLOW || s == TSDF_ERR_HEAP_FULL || s == TSDF_ERR_BAD_POINTS) return;
+  throw std::runtime_error(std::string(what) + ": " + (e ? tsdf_last_error(e) : "engine creation failed"));
+}
+inline tsdf_engine* shared_engine() {
+  Globals& g = globals();
+  std::lock_guard<std::mutex> lk(g.mu);
+  if (!g.engine) {
+    tsdf_engine_cfg cfg{};
+    cfg.pool_blocks = 4ll * NUM_HEAP_BLOCKS;
+    cfg.max_maps = 16;
+    cfg.max_publish = 4ll * PUBLISH_VOXELS_MAX_SIZE;
+    check(nullptr, tsdf_engine_create(&cfg, &g.engine), "tsdf_engine_create");
+  }
+  return g.engine;
+}
+}  // namespace detail
+
+// Sets the parameters of the next TSDFHandler (tsdf_handler.cu:1289-1317).
+inline void initGlobalVars(float voxel_size, float truncation_distance, float max_weight,
+                           float publish_distance_squared, float garbage_collect_distance_squared) {
+  detail::Globals& g = detail::globals();
+  g.params = tsdf_params{voxel_size, truncation_distance, max_weight, publish_distance_squared,
+                         garbage_collect_distance_squared};
+  g.set = true;
+}
+
+// Hash table + block heap of one map (tsdf_container.cuh:112-133).
+class TSDFContainer {
+ public:
+  TSDFContainer(tsdf_engine* eng, int64_t heap_blocks) : eng_(eng) {
+    detail::Globals& g = detail::globals();
+    if (!g.set) throw std::runtime_error("initGlobalVars must be called before TSDFHandler()");
+    detail::check(eng_, tsdf_map_create(eng_, &g.params, heap_blocks, &map_), "tsdf_map_create");
+  }
+  ~TSDFContainer() {
+    if (map_ >= 0) tsdf_map_destroy(eng_, map_);
+  }
+  TSDFContainer(const TSDFContainer&) = delete;
+  TSDFContainer& operator=(const TSDFContainer&) = delete;
+  int mapId() const { return map_; }
+  tsdf_engine* engine() const { return eng_; }
+
+ private:
+  tsdf_engine* eng_;
+  int map_ = -1;
+};
+
+class TSDFHandler {
+ public:
+  TSDFHandler() : container_(detail::shared_engine(), NUM_HEAP_BLOCKS) {}
+  explicit TSDFHandler(tsdf_engine* eng, int64_t heap_blocks = NUM_HEAP_BLOCKS) : container_(eng, heap_blocks) {}
+
+  // tsdf_handler.cu:974-1016: integrate, publish, garbage-collect.
+  void processPointCloudAndUpdateVoxels(const std::vector<PointXYZ>& cloud, Vector3f* lidar_position_h,
+                                        Vector3f* publish_voxels_pos_h, int* publish_voxels_size_h,
+                                        Voxel* publish_voxels_data_h) {
+    processPointCloudAndUpdateVoxels(cloud.data(), (int64_t)cloud.size(), lidar_position_h, publish_voxels_pos_h,
+                                     publish_voxels_size_h, publish_voxels_data_h);
+  }
+
+  void processPointCloudAndUpdateVoxels(const PointXYZ* points, int64_t n, Vector3f* lidar_position_h,
+                                        Vector3f* publish_voxels_pos_h, int* publish_voxels_size_h,
+                                        Voxel* publish_voxels_data_h, int64_t capacity = PUBLISH_VOXELS_MAX_SIZE) {
+    const int start = *publish_voxels_size_h;
+    if (start < 0 || start > capacity) throw std::runtime_error("publish_voxels_size out of range");
+    int64_t count = 0;
+    tsdf_status st = tsdf_integrate(container_.engine(), container_.mapId(), reinterpret_cast<const float*>(points),
+                                    n, (int)sizeof(PointXYZ), lidar_position_h->data,
+                                    reinterpret_cast<float*>(publish_voxels_pos_h + start),
+                                    publish_voxels_data_h + start, capacity - start, &count, &last_stats_);
+    detail::check(container_.engine(), st, "processPointCloudAndUpdateVoxels");
+    last_status_ = st;
+    *publish_voxels_size_h = start + (int)count;
+  }
+
+  tsdf_status lastStatus() const { return last_status_; }
+  const tsdf_scan_stats& lastStats() const { return last_stats_; }
+  const TSDFContainer& container() const { return container_; }
+
+ private:
+  TSDFContainer container_;
+  tsdf_status last_status_ = TSDF_OK;
+  tsdf_scan_stats last_stats_{};
+};
+
+}  // namespace tsdf
+
+#endif  // TSDF_HANDLER_HPP

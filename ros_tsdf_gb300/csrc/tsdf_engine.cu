@@ -240,6 +240,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   const long long rank_cap = npts * c.max_routes;
   const long long rec_cap = npts * c.max_routes;
   const long long enum_cap = c.pool_blocks;
+  const long long entry_cap = npts * 8ll * (c.max_routes - 4);
   auto tiles = [](long long n, long long t) { return (int)((n + t - 1) / t); };
   const int max_tiles_rank = tiles(rank_cap, 2048);
   const int max_tiles_rec = tiles(rec_cap, 2048);
@@ -267,6 +268,10 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
     TRY(dalloc(eng, &x.rec_key[i], rec_cap, tr));
     TRY(dalloc(eng, &x.rec_val[i], rec_cap, tr));
   }
+  TRY(dalloc(eng, &x.entries, entry_cap, tr));
+  TRY(dalloc(eng, &x.bin_d, entry_cap, tr));
+  TRY(dalloc(eng, &x.heavy, rec_cap, tr));
+  x.entry_cap = entry_cap;
   TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
   TRY(dalloc(eng, &x.digit_tot, 256, tr));
   TRY(dalloc(eng, &x.tile_sums, max_tiles_scan + 1, tr));
@@ -275,7 +280,6 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.enum_gc, enum_cap, tr));
   TRY(dalloc(eng, &x.pub_prefix, enum_cap, tr));
   TRY(dalloc(eng, &x.gc_prefix, enum_cap, tr));
-  x.seg_prefix = nullptr;
   x.max_tiles_rank = max_tiles_rank;
   x.max_tiles_rec = max_tiles_rec;
   x.max_tiles_scan = max_tiles_scan;
@@ -381,7 +385,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   std::memset(hdr, 0, sizeof(BatchHdr));
   long long total = 0, bytes = 0, pub_staged = 0;
   long long lo = -1, hi = 0;
-  int rank_stride = 1, rec_stride = 1;
+  int rank_stride = 1, rec_stride = 1, vox_stride = 1;
   L.staged.clear();
   L.maps.clear();
   for (int i = 0; i < n; ++i) {
@@ -406,6 +410,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     total += s.n_points;
     rank_stride = std::max(rank_stride, m.dev.amax);
     rec_stride = std::max(rec_stride, m.dev.rmax);
+    vox_stride = std::max(vox_stride, m.dev.vmax);
     lo = lo < 0 ? m.dev.heap_base : std::min(lo, m.dev.heap_base);
     hi = std::max(hi, m.dev.heap_base + m.dev.heap_cap);
   }
@@ -448,6 +453,9 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   hdr->n_items = n;
   hdr->rank_stride = rank_stride;
   hdr->rec_stride = rec_stride;
+  hdr->vox_stride = vox_stride;
+  if (total * (long long)vox_stride > L.ctx.entry_cap || total * (long long)vox_stride >= (1ll << 27))
+    return fail(eng, TSDF_ERR_CAPACITY, "voxel-update entries exceed capacity");
   hdr->total_points = total;
   hdr->rec_total = total * rec_stride;
   hdr->key_lo = lo;
@@ -693,12 +701,14 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   if (c.bucket_size != 4 && c.bucket_size != 8 && c.bucket_size != 16) return TSDF_ERR_INVALID_ARG;
   if (c.ray_threads <= 0) c.ray_threads = 256;
   if (c.ray_threads != 64 && c.ray_threads != 128 && c.ray_threads != 256) return TSDF_ERR_INVALID_ARG;
-  if (c.ray_chunk <= 0) c.ray_chunk = 256;
+  if (c.ray_chunk <= 0) c.ray_chunk = 32;
   c.ray_chunk = ((c.ray_chunk + 31) / 32) * 32;
   if (c.max_routes <= 0) c.max_routes = 16;
   if (c.lanes <= 0) c.lanes = 1;
   if (c.lanes > kMaxLanes) c.lanes = kMaxLanes;
-  if (c.pool_blocks >= (1ll << 31) || c.max_batch_points * (long long)c.max_routes >= (1ll << 31))
+  if (c.max_routes < 8 || c.max_routes > 64) return TSDF_ERR_INVALID_ARG;
+  if (c.pool_blocks >= (1ll << 31) || c.max_batch_points * (long long)c.max_routes >= (1ll << 31) ||
+      c.max_batch_points * 8ll * (c.max_routes - 4) >= (1ll << 27))
     return TSDF_ERR_INVALID_ARG;
   eng->cfg = c;
   eng->device = c.device;

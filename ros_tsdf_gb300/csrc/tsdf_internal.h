@@ -17,7 +17,8 @@ constexpr unsigned kRankNone = 0xFFFFFFFFu;
 constexpr unsigned kRecSentinel = 0xFFFFFFFFu;
 constexpr int kRadixBits = 8;
 constexpr int kMaxRadixPasses = 4;
-constexpr int kUpdEntries = 32;        // voxel entries of one point inside one block (<= 22)
+constexpr int kUpdEntries = 24;        // voxel updates of one point inside one block (<= 3*7+1 = 22)
+constexpr unsigned kBadLocal = 0xFFFFu;  // entry whose local voxel index fell outside its block
 
 // One hash entry: packed block key, logical heap slot, first-touch rank.
 // Invariants: slot >= 0 only while the key is live; rank == kRankNone except
@@ -86,7 +87,7 @@ struct BatchHdr {
   int n_items;
   int rank_stride;     // max block-DDA cap over items (rank = g * stride + j)
   int rec_stride;      // routes per point in the record buffer
-  int pad0;
+  int vox_stride;      // max voxel-DDA cap over items (entry = g * stride + j)
   long long total_points;
   long long rec_total;        // total_points * rec_stride
   long long key_lo;           // record key = physical slot - key_lo
@@ -106,6 +107,8 @@ struct LaneCounters {
   long long n_seg;        // segments (distinct blocks updated)
   long long n_enum;       // enumerated slots for publish / gc
   long long scan_total;   // scratch for scans
+  long long n_heavy;      // segments with more records than one update chunk
+  unsigned long long bin_cursor;  // bump allocator of the heavy-segment bins
   int error;              // bit flags, see ERR_*
   int pad;
 };
@@ -134,6 +137,7 @@ struct Ctx {
   unsigned* rank_val[2];
   unsigned* rec_key[2];
   unsigned* rec_val[2];
+  uint2* entries;                // per voxel update: (float bits of d, local index)
   int* hist;                     // [256][max_tiles]
   int* digit_tot;                // [256]
   int* tile_sums;                // scan tiles
@@ -142,7 +146,8 @@ struct Ctx {
   int* enum_gc;                  // gc flags per enumerated slot
   int* pub_prefix;
   int* gc_prefix;
-  int* seg_prefix;
+  int* heavy;                    // segment ids of heavy segments
+  float* bin_d;                  // heavy-segment bins (entry_cap floats)
   int max_tiles_rank;
   int max_tiles_rec;
   int max_tiles_scan;
@@ -150,6 +155,7 @@ struct Ctx {
   long long rank_cap;            // capacity of the rank / newlist arrays
   long long rec_cap;             // capacity of the record arrays
   long long enum_cap;            // capacity of the enumeration arrays
+  long long entry_cap;           // capacity of the entries array
 };
 
 // Stage ids for timing.

@@ -773,7 +773,11 @@ __global__ void k_alloc_finalize(Ctx c) {
 }
 
 // ----------------------------------------------------------------------------
-// ray pass 2: voxel DDA, runs of one block, one routing record per run
+// ray pass 2: voxel DDA (getVoxelsAndUpdateCuda, tsdf_handler.cu:675-710).
+// Each voxel of a found block yields one update entry (distance d and local
+// voxel index, getDistanceUpdate / getLocalVoxelIndex) stored at
+// entries[g * vox_stride + j]; each run of voxels in one block yields one
+// routing record (block slot, entry range) at rec[g * rec_stride + run].
 template <int G>
 __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
   __shared__ long long s_pb[kMaxItems];
@@ -787,8 +791,10 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
   const long long total = h.total_points;
   const long long chunk = c.ray_chunk;
   const int R = h.rec_stride;
+  const int VS = h.vox_stride;
   unsigned* rk = c.rec_key[0];
   unsigned* rv = c.rec_val[0];
+  uint2* ent = c.entries;
   while (true) {
     unsigned long long q = 0;
     if (lane == 0) q = atomicAdd(&c.ctr->q_voxels, 1ull);
@@ -804,39 +810,54 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
       const MapDev& m = c.maps[mi];
       Seg seg;
       bool valid = false;
+      float px = 0.f, py = 0.f, pz = 0.f;
       if (active) {
         const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
-        valid = make_segment(p[0], p[1], p[2], it.ox, it.oy, it.oz, m, &seg);
+        px = p[0], py = p[1], pz = p[2];
+        valid = make_segment(px, py, pz, it.ox, it.oy, it.oz, m, &seg);
       }
       Dda dda;
       if (valid) dda.init(seg, m.vs, m.scale_v, m.half_vs, m.vmax);
       const HEntry* tab = c.hash + m.hash_base;
       const unsigned mask = m.hash_mask;
-      const long long kbase = m.heap_base - c.hdr->key_lo;
-      unsigned long long cur = kEmptyKey;
-      int run = -1, run_slot = -1;
-      unsigned route_ovf = 0, missing = 0;
+      const long long kbase = m.heap_base - h.key_lo;
       const long long rbase = g * (long long)R;
+      const long long ebase = g * (long long)VS;
+      unsigned long long cur = kEmptyKey;
+      int run = -1, run_slot = -1, run_start = 0, run_cnt = 0, j = 0;
+      float blx = 0.f, bly = 0.f, blz = 0.f;
+      unsigned route_ovf = 0, missing = 0, bad = 0;
       while (true) {
         float x, y, z;
         int kx, ky, kz;
         bool has = valid && dda.next(&x, &y, &z, &kx, &ky, &kz);
         if (!__ballot_sync(kFull, has)) break;
         unsigned long long bkey = 0;
+        float fbx = 0.f, fby = 0.f, fbz = 0.f;
         if (has) {
-          int bx = (int)floorf(fmul(x, m.scale_b));
-          int by = (int)floorf(fmul(y, m.scale_b));
-          int bz = (int)floorf(fmul(z, m.scale_b));
-          bkey = pack_key(bx, by, bz);
+          fbx = floorf(fmul(x, m.scale_b));
+          fby = floorf(fmul(y, m.scale_b));
+          fbz = floorf(fmul(z, m.scale_b));
+          bkey = pack_key((int)fbx, (int)fby, (int)fbz);
         }
-        bool newrun = has && bkey != cur;
+        const bool newrun = has && bkey != cur;
         if (newrun) {
+          if (run >= 0 && run < m.rmax) {
+            rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
+            rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
+          }
           ++run;
           cur = bkey;
           run_slot = -1;
+          run_start = j;
+          run_cnt = 0;
+          // block centre and bottom-left corner (tsdf_handler.cu:612-624)
+          blx = fsub(fadd(fdiv(fbx, m.scale_b), m.half_bs), m.half_bs);
+          bly = fsub(fadd(fdiv(fby, m.scale_b), m.half_bs), m.half_bs);
+          blz = fsub(fadd(fdiv(fbz, m.scale_b), m.half_bs), m.half_bs);
         }
-        bool need = newrun && run < m.rmax;
-        unsigned nm = __ballot_sync(kFull, need);
+        const bool need = newrun && run < m.rmax;
+        const unsigned nm = __ballot_sync(kFull, need);
         for (int i = 0; i < G; ++i) {
           const int src = gbase + i;
           if (!((nm >> src) & 1u)) continue;
@@ -847,24 +868,42 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
           int res = group_lookup<G>(t2, m2, k2, gl, gbase, gmask);
           if (lane == src) run_slot = res;
         }
-        if (need) {
-          rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
-          rv[rbase + run] = (unsigned)g;
-        }
         if (has) {
-          if (run >= m.rmax)
+          if (run >= m.rmax) {
             ++route_ovf;
-          else if (run_slot < 0)
+          } else if (run_slot < 0) {
             ++missing;
+          } else if (run_cnt >= 31) {
+            ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
+          } else {
+            // getLocalVoxelIndex (tsdf_handler.cu:507-512)
+            float ix = floorf(fdiv(fsub(x, blx), m.vs));
+            float iy = floorf(fdiv(fsub(y, bly), m.vs));
+            float iz = floorf(fdiv(fsub(z, blz), m.vs));
+            unsigned local = kBadLocal;
+            if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
+              local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
+            else
+              ++bad;
+            const float d = distance_update(x, y, z, px, py, pz, it.ox, it.oy, it.oz);
+            ent[ebase + j] = make_uint2(__float_as_uint(d), local);
+            ++run_cnt;
+          }
+          ++j;
         }
       }
       if (active) {
+        if (run >= 0 && run < m.rmax) {
+          rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
+          rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
+        }
         int first = valid ? min(run + 1, m.rmax) : 0;
-        for (int j = first; j < R; ++j) rk[rbase + j] = kRecSentinel;
+        for (int r = first; r < R; ++r) rk[rbase + r] = kRecSentinel;
       }
       stat_add_warp(c.item_stats, item, ST_VOVF, (valid && dda.ovf) ? 1u : 0u);
       stat_add_warp(c.item_stats, item, ST_ROVF, route_ovf);
       stat_add_warp(c.item_stats, item, ST_MISS, missing);
+      stat_add_warp(c.item_stats, item, ST_BADLOCAL, bad);
     }
   }
 }
@@ -881,9 +920,38 @@ struct SegHeadOut {
   }
 };
 
-// ----------------------------------------------------------------------------
-// update: one CTA per block touched
+// segments with more records than one update chunk go to the heavy list
 constexpr int UPD_T = 128;
+
+__global__ void k_seg_classify(Ctx c) {
+  const long long nseg = c.ctr->n_seg;
+  const long long nrec = c.ctr->n_rec_live;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nseg;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+    if (b1 - c.seg_start[j] > UPD_T) {
+      unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_heavy), 1ull);
+      c.heavy[k] = (int)j;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// update: one CTA per block touched (updateVoxelsCuda, tsdf_handler.cu:
+// 604-665).  The block's 512 voxels are staged in shared memory with 16-byte
+// loads/stores.  Its routing records (ascending point index) are taken 128 at
+// a time; every voxel gets a 128-bit mask of the records that update it, an
+// entry's rank in its voxel's bin is a popcount of the mask below it, so each
+// bin lists its updates in ascending point order and its owner thread applies
+// them sequentially: the reference's update rule, in a fixed order.
+//
+// Segments longer than one chunk (a block that many points update, e.g. the
+// blocks around a sensor standing inside an object) are taken first and
+// handled in three passes: per-voxel counts over all records, ordered
+// placement of every update into per-voxel bins in global scratch (mask
+// popcount + running per-voxel cursor), then one sequential chain per voxel
+// with its loads issued ahead.  The chain of the most-updated voxel is the
+// critical path either way; the passes remove the per-chunk barriers from it.
 
 __device__ __forceinline__ int find_item_global(const ItemDev* items, int n, long long g) {
   int lo = 0, hi = n - 1;
@@ -897,158 +965,268 @@ __device__ __forceinline__ int find_item_global(const ItemDev* items, int n, lon
   return lo;
 }
 
+__device__ __forceinline__ float apply_chain(float* sdf_io, float w, const float* d, int n, float maxw) {
+  // getWeightUpdate + update rule (tsdf_handler.cu:579-581, :648-654), in order
+  float sdf = *sdf_io;
+  int a = 0;
+  for (; a + 4 <= n; a += 4) {
+    const float d0 = d[a], d1 = d[a + 1], d2 = d[a + 2], d3 = d[a + 3];
+    const float dd[4] = {d0, d1, d2, d3};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float wt = fdiv(1.0f, fadd(fabsf(dd[q]), 1.0f));
+      const float wd = fmul(wt, dd[q]);
+      const float nw = fadd(w, wt);
+      sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
+      w = fminf(nw, maxw);
+    }
+  }
+  for (; a < n; ++a) {
+    const float wt = fdiv(1.0f, fadd(fabsf(d[a]), 1.0f));
+    const float wd = fmul(wt, d[a]);
+    const float nw = fadd(w, wt);
+    sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
+    w = fminf(nw, maxw);
+  }
+  *sdf_io = sdf;
+  return w;
+}
+
 __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
   __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
   __shared__ float s_d[UPD_T * kUpdEntries];
   __shared__ unsigned short s_l[UPD_T * kUpdEntries];
   __shared__ unsigned short s_bin[UPD_T * kUpdEntries];
-  __shared__ int s_cnt[kVoxelsPerBlock];
-  __shared__ int s_off[kVoxelsPerBlock];
-  __shared__ int s_cur[kVoxelsPerBlock];
+  __shared__ unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];
+  __shared__ int s_off[kVoxelsPerBlock + 1];
+  __shared__ int s_run[kVoxelsPerBlock];
   __shared__ unsigned s_touch[kVoxelsPerBlock / 32];
   __shared__ int s_warp[32];
   __shared__ long long s_seg;
+  __shared__ unsigned long long s_base;
   const BatchHdr h = *c.hdr;
   const int t = threadIdx.x;
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
+  const long long nheavy = c.ctr->n_heavy;
   const unsigned* rk = c.rec_key[rec_sel];
   const unsigned* rv = c.rec_val[rec_sel];
+  const unsigned lt_bits = (1u << (t & 31)) - 1u;
   while (true) {
     if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
     __syncthreads();
-    const long long sj = s_seg;
+    long long q = s_seg;
     __syncthreads();
-    if (sj >= nseg) break;
+    if (q >= nheavy + nseg) break;
+    long long sj;
+    bool heavy;
+    if (q < nheavy) {
+      sj = c.heavy[q];
+      heavy = true;
+    } else {
+      sj = q - nheavy;
+      const long long e1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
+      if (e1 - c.seg_start[sj] > UPD_T) continue;  // already done on the heavy path
+      heavy = false;
+    }
     const long long b0 = c.seg_start[sj];
     const long long b1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
     const long long phys = h.key_lo + rk[b0];
-    const int item = find_item_global(c.items, h.n_items, (long long)rv[b0]);
-    const ItemDev& it = c.items[item];
-    const MapDev& m = c.maps[it.map];
-    int tkx, tky, tkz;
-    unpack_key(c.slot_key[phys], &tkx, &tky, &tkz);
-    // block centre and bottom-left corner (tsdf_handler.cu:612-624)
-    const float bcx = fadd(fdiv((float)tkx, m.scale_b), m.half_bs);
-    const float bcy = fadd(fdiv((float)tky, m.scale_b), m.half_bs);
-    const float bcz = fadd(fdiv((float)tkz, m.scale_b), m.half_bs);
-    const float blx = fsub(bcx, m.half_bs), bly = fsub(bcy, m.half_bs), blz = fsub(bcz, m.half_bs);
+    const int item = find_item_global(c.items, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+    const MapDev& m = c.maps[c.items[item].map];
+    const float maxw = m.maxw;
     float4* gv = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
     float4* sv4 = reinterpret_cast<float4*>(s_vox);
     sv4[t] = gv[t];
     sv4[t + UPD_T] = gv[t + UPD_T];
     if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
-    unsigned n_upd = 0, n_bad = 0;
-    for (long long cb = b0; cb < b1; cb += UPD_T) {
-      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_cnt[l] = 0;
+    unsigned n_upd = 0;
+    if (!heavy) {
+      // ---- light path: the whole segment in one chunk
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+#pragma unroll
+        for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
+      }
+      __syncthreads();
       int ne = 0;
-      if (cb + t < b1) {
-        const long long g = rv[cb + t];
-        const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
-        const float px = p[0], py = p[1], pz = p[2];
-        Seg seg;
-        if (make_segment(px, py, pz, it.ox, it.oy, it.oz, m, &seg)) {
-          Dda dda;
-          dda.init(seg, m.vs, m.scale_v, m.half_vs, m.vmax);
-          bool seen = false;
-          float x, y, z;
-          int kx, ky, kz;
-          while (dda.next(&x, &y, &z, &kx, &ky, &kz)) {
-            float fbx = floorf(fmul(x, m.scale_b));
-            float fby = floorf(fmul(y, m.scale_b));
-            float fbz = floorf(fmul(z, m.scale_b));
-            bool in = (int)fbx == tkx && (int)fby == tky && (int)fbz == tkz;
-            if (!in) {
-              if (seen) break;
-              continue;
-            }
-            seen = true;
-            // getLocalVoxelIndex (tsdf_handler.cu:507-512)
-            float dx = fdiv(fsub(x, blx), m.vs), dy = fdiv(fsub(y, bly), m.vs), dz = fdiv(fsub(z, blz), m.vs);
-            float ix = floorf(dx), iy = floorf(dy), iz = floorf(dz);
-            if (!(ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f) || ne >= kUpdEntries) {
-              ++n_bad;
-              continue;
-            }
-            int local = (int)ix + (int)iy * 8 + (int)iz * 64;
-            s_d[t * kUpdEntries + ne] = distance_update(x, y, z, px, py, pz, it.ox, it.oy, it.oz);
-            s_l[t * kUpdEntries + ne] = (unsigned short)local;
-            ++ne;
-          }
+      if (b0 + t < b1) {
+        const unsigned v = rv[b0 + t];
+        const int cnt = (int)(v & 31u);
+        const uint2* e = c.entries + (v >> 5);
+        uint2 xs[kUpdEntries];
+#pragma unroll
+        for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
+#pragma unroll
+        for (int k = 0; k < kUpdEntries; ++k) {
+          const uint2 x = xs[k];
+          if (x.y == kBadLocal) continue;
+          s_d[t * kUpdEntries + ne] = __uint_as_float(x.x);
+          s_l[t * kUpdEntries + ne] = (unsigned short)x.y;
+          atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
+          ++ne;
         }
       }
       n_upd += ne;
       __syncthreads();
-      for (int k = 0; k < ne; ++k) atomicAdd(&s_cnt[s_l[t * kUpdEntries + k]], 1);
+      {
+        int a[4];
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) {
+          const int l = 4 * t + qq;
+          int cnt = 0;
+#pragma unroll
+          for (int w = 0; w < UPD_T / 32; ++w) cnt += __popc(s_mask[l][w]);
+          a[qq] = cnt;
+        }
+        int tot;
+        int ex = block_excl_scan(a[0] + a[1] + a[2] + a[3], s_warp, &tot);
+        s_off[4 * t] = ex;
+        s_off[4 * t + 1] = ex + a[0];
+        s_off[4 * t + 2] = ex + a[0] + a[1];
+        s_off[4 * t + 3] = ex + a[0] + a[1] + a[2];
+        if (t == 0) s_off[kVoxelsPerBlock] = tot;
+      }
+      __syncthreads();
+      for (int k = 0; k < ne; ++k) {
+        const int l = s_l[t * kUpdEntries + k];
+        int rank = __popc(s_mask[l][t >> 5] & lt_bits);
+        for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+        s_bin[s_off[l] + rank] = (unsigned short)(t * kUpdEntries + k);
+      }
+      __syncthreads();
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+        const int b = s_off[l], e = s_off[l + 1];
+        if (e == b) continue;
+        float sdf = s_vox[l].x, w = s_vox[l].y;
+        for (int a = b; a < e; ++a) {
+          const float d = s_d[s_bin[a]];
+          const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
+          const float wd = fmul(wt, d);
+          const float nw = fadd(w, wt);
+          sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
+          w = fminf(nw, maxw);
+        }
+        s_vox[l] = make_float2(sdf, w);
+        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+      }
+      __syncthreads();
+    } else {
+      // ---- heavy path, pass 0: per-voxel update counts over all records
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_run[l] = 0;
+      __syncthreads();
+      for (long long cb = b0; cb < b1; cb += UPD_T) {
+        if (cb + t < b1) {
+          const unsigned v = rv[cb + t];
+          const int cnt = (int)(v & 31u);
+          const uint2* e = c.entries + (v >> 5);
+          uint2 xs[kUpdEntries];
+#pragma unroll
+          for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
+#pragma unroll
+          for (int k = 0; k < kUpdEntries; ++k)
+            if (xs[k].y != kBadLocal) atomicAdd(&s_run[xs[k].y], 1);
+        }
+      }
       __syncthreads();
       {
-        // exclusive scan of 512 counters, 4 per thread
-        int a0 = s_cnt[4 * t], a1 = s_cnt[4 * t + 1], a2 = s_cnt[4 * t + 2], a3 = s_cnt[4 * t + 3];
+        const int a0 = s_run[4 * t], a1 = s_run[4 * t + 1], a2 = s_run[4 * t + 2], a3 = s_run[4 * t + 3];
         int tot;
         int ex = block_excl_scan(a0 + a1 + a2 + a3, s_warp, &tot);
         s_off[4 * t] = ex;
         s_off[4 * t + 1] = ex + a0;
         s_off[4 * t + 2] = ex + a0 + a1;
         s_off[4 * t + 3] = ex + a0 + a1 + a2;
-        s_cur[4 * t] = ex;
-        s_cur[4 * t + 1] = ex + a0;
-        s_cur[4 * t + 2] = ex + a0 + a1;
-        s_cur[4 * t + 3] = ex + a0 + a1 + a2;
+        if (t == 0) {
+          s_off[kVoxelsPerBlock] = tot;
+          s_base = atomicAdd(&c.ctr->bin_cursor, (unsigned long long)tot);
+        }
       }
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_run[l] = 0;
       __syncthreads();
-      for (int k = 0; k < ne; ++k) {
-        int l = s_l[t * kUpdEntries + k];
-        int pos = atomicAdd(&s_cur[l], 1);
-        s_bin[pos] = (unsigned short)(t * kUpdEntries + k);
-      }
-      __syncthreads();
-      // owners: voxel l by thread l % UPD_T, entries in ascending point order
-      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-        const int cnt = s_cnt[l];
-        if (!cnt) continue;
-        unsigned short* bin = s_bin + s_off[l];
-        for (int a = 1; a < cnt; ++a) {
-          unsigned short v = bin[a];
-          int b = a - 1;
-          while (b >= 0 && bin[b] > v) {
-            bin[b + 1] = bin[b];
-            --b;
+      const unsigned long long base = s_base;
+      const bool fits = base + (unsigned long long)s_off[kVoxelsPerBlock] <= (unsigned long long)c.entry_cap;
+      if (!fits && t == 0) set_error(c.ctr, ERR_CAPACITY);
+      // pass 1: ordered placement into the bins
+      for (long long cb = b0; cb < b1 && fits; cb += UPD_T) {
+        for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+#pragma unroll
+          for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
+        }
+        __syncthreads();
+        int ne = 0;
+        if (cb + t < b1) {
+          const unsigned v = rv[cb + t];
+          const int cnt = (int)(v & 31u);
+          const uint2* e = c.entries + (v >> 5);
+          uint2 xs[kUpdEntries];
+#pragma unroll
+          for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
+#pragma unroll
+          for (int k = 0; k < kUpdEntries; ++k) {
+            const uint2 x = xs[k];
+            if (x.y == kBadLocal) continue;
+            s_d[t * kUpdEntries + ne] = __uint_as_float(x.x);
+            s_l[t * kUpdEntries + ne] = (unsigned short)x.y;
+            atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
+            ++ne;
           }
-          bin[b + 1] = v;
         }
-        float sdf = s_vox[l].x, w = s_vox[l].y;
-        for (int a = 0; a < cnt; ++a) {
-          const float d = s_d[bin[a]];
-          // getWeightUpdate + update rule (tsdf_handler.cu:579-581, :648-654)
-          const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
-          const float wd = fmul(wt, d);
-          const float nw = fadd(w, wt);
-          sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
-          w = fminf(nw, m.maxw);
+        n_upd += ne;
+        __syncthreads();
+        for (int k = 0; k < ne; ++k) {
+          const int l = s_l[t * kUpdEntries + k];
+          int rank = __popc(s_mask[l][t >> 5] & lt_bits);
+          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+          c.bin_d[base + s_off[l] + s_run[l] + rank] = s_d[t * kUpdEntries + k];
         }
-        s_vox[l] = make_float2(sdf, w);
-        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+        __syncthreads();
+        for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+          int cnt = 0;
+#pragma unroll
+          for (int w = 0; w < UPD_T / 32; ++w) cnt += __popc(s_mask[l][w]);
+          s_run[l] += cnt;
+        }
+        __syncthreads();
+      }
+      // pass 2: one chain per voxel
+      if (fits) {
+        for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+          const int b = s_off[l], e = s_off[l + 1];
+          if (e == b) continue;
+          float sdf = s_vox[l].x;
+          const float w = apply_chain(&sdf, s_vox[l].y, c.bin_d + base + b, e - b, maxw);
+          s_vox[l] = make_float2(sdf, w);
+          atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+        }
       }
       __syncthreads();
     }
-    gv[t] = sv4[t];
-    gv[t + UPD_T] = sv4[t + UPD_T];
-    int nz = 0;
-    for (int l = t; l < kVoxelsPerBlock; l += UPD_T) nz += s_vox[l].y != 0.0f;
-    int tot;
-    block_excl_scan(nz, s_warp, &tot);
+    const float4 va = sv4[t], vb = sv4[t + UPD_T];
+    gv[t] = va;
+    gv[t + UPD_T] = vb;
+    // one reduction for the three block totals: non-zero weights, touched
+    // voxels, applied updates
+    int nz = (va.y != 0.0f) + (va.w != 0.0f) + (vb.y != 0.0f) + (vb.w != 0.0f);
     int touched = t < kVoxelsPerBlock / 32 ? __popc(s_touch[t]) : 0;
-    int ttot;
-    block_excl_scan(touched, s_warp, &ttot);
-    int upd_tot;
-    block_excl_scan((int)n_upd, s_warp, &upd_tot);
-    int bad_tot;
-    block_excl_scan((int)n_bad, s_warp, &bad_tot);
+    int upd = (int)n_upd;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      nz += __shfl_xor_sync(kFull, nz, o);
+      touched += __shfl_xor_sync(kFull, touched, o);
+      upd += __shfl_xor_sync(kFull, upd, o);
+    }
+    if ((t & 31) == 0) {
+      s_warp[(t >> 5) * 3 + 0] = nz;
+      s_warp[(t >> 5) * 3 + 1] = touched;
+      s_warp[(t >> 5) * 3 + 2] = upd;
+    }
+    __syncthreads();
     if (t == 0) {
-      c.nnz[phys] = tot;
-      stat_add(c.item_stats, item, ST_UPD, upd_tot);
-      stat_add(c.item_stats, item, ST_BADLOCAL, bad_tot);
-      stat_add(c.item_stats, item, ST_DVOX, ttot);
+      int a = 0, b = 0, u = 0;
+      for (int w = 0; w < UPD_T / 32; ++w) a += s_warp[3 * w], b += s_warp[3 * w + 1], u += s_warp[3 * w + 2];
+      c.nnz[phys] = a;
+      stat_add(c.item_stats, item, ST_UPD, u);
+      stat_add(c.item_stats, item, ST_DVOX, b);
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
     }
     __syncthreads();
@@ -1310,7 +1488,8 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums);
   k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_rec_live, &c.ctr->n_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
-  *launches += 3;
+  k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c);
+  *launches += 4;
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {

@@ -1,0 +1,346 @@
+"""GPU parity of the engine against the CPU oracle, through the C-ABI.
+
+Bar (from the benchmark spec): block set, hash contents (key -> slot), heap
+occupancy / free list and published voxel set bit-exact; weights exact; sdf
+within 1e-5 * truncation_distance.  The engine applies every voxel's updates
+in the oracle's order, so sdf is asserted bit-exact too (a stronger check).
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(params, heap):
+    from oracle import OracleMap
+
+    return OracleMap(params, heap, detail=True)
+
+
+def assert_scan_equal(r, orc_out, T, what=""):
+    pos, data, cnt, st, _ = orc_out
+    assert r.count == cnt, f"{what} publish count {r.count} != {cnt}"
+    assert np.array_equal(r.pos, pos), f"{what} published positions differ"
+    assert np.array_equal(r.data[:, 1], data[:, 1]), f"{what} weights differ"
+    if len(data):
+        assert np.max(np.abs(r.data[:, 0] - data[:, 0])) <= 1e-5 * T, f"{what} sdf beyond 1e-5*T"
+    assert np.array_equal(r.data, data), f"{what} sdf not bit-exact"
+    for k in st:
+        assert r.stats[k] == st[k], f"{what} stat {k}: {r.stats[k]} != {st[k]}"
+
+
+def assert_state_equal(eng, mid, orc, heap, voxels=True):
+    kg, sg = eng.dump_blocks(mid)
+    ko, so = orc.dump_blocks()
+    assert np.array_equal(kg, ko) and np.array_equal(sg, so), "block table (key -> slot) differs"
+    fg, bcg = eng.dump_free_list(mid)
+    fo, bco = orc.dump_free_list(heap)
+    assert bcg == bco and np.array_equal(fg, fo), "free list / block count differ"
+    if voxels:
+        for s in sg:
+            assert np.array_equal(eng.dump_block_voxels(mid, s), orc.dump_block_voxels(s)), f"voxels of slot {s}"
+
+
+def test_plain_path_matches_oracle(built):
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = W.plain_small(seed=0, heap_blocks=8192)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, spec.heap_blocks)
+    with Engine(max_maps=4, pool_blocks=8192, max_batch_points=1 << 16) as eng:
+        mid = eng.create_map(spec.params, spec.heap_blocks)
+        for k in range(8):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 20)
+            assert r.status == 0
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 20), spec.params.truncation_distance, f"scan {k}")
+        assert_state_equal(eng, mid, orc, spec.heap_blocks)
+
+
+def test_gc_churn_and_slot_reuse(built):
+    from ros_tsdf_gb300 import Engine, TsdfParams, workloads as W
+
+    spec = replace(W.plain_small(seed=9, heap_blocks=2048), params=TsdfParams(0.5, 4.0, 1000.0, 400.0, 625.0),
+                   traj=W.Traj(0, 40.0, 5.0, 8.0, 4.0))
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, spec.heap_blocks)
+    gcs = 0
+    with Engine(max_maps=2, pool_blocks=2048, max_batch_points=1 << 16) as eng:
+        mid = eng.create_map(spec.params, spec.heap_blocks)
+        for k in range(20):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 20)
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 20), 4.0, f"scan {k}")
+            gcs += r.stats["gc_blocks"]
+        assert gcs > 1000
+        assert_state_equal(eng, mid, orc, spec.heap_blocks)
+
+
+def _mixed_specs():
+    """Maps with uneven lidars and per-map parameters, including two whose
+    sensors stand inside or next to a box (heavy blocks)."""
+    from ros_tsdf_gb300 import TsdfParams, workloads as W
+
+    mm = W.multimap32(32, base_seed=1000, heap_blocks=1 << 14)
+    specs = [mm[14], mm[2], mm[10], mm[5], mm[30]]
+    specs.append(replace(W.large_stream(seed=2100, heap_blocks=1 << 16),
+                         lidar=replace(W.LIDAR_LARGE, channels=16, azimuths=512)))
+    specs.append(replace(mm[7], params=TsdfParams(0.2, 0.8, 50.0, 900.0, 40000.0)))
+    specs.append(replace(mm[8], params=TsdfParams(0.05, 0.2, 1000.0, 400.0, 2500.0), heap_blocks=1 << 16))
+    return specs
+
+
+def test_batched_multimap_matches_oracle(built):
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    specs = _mixed_specs()
+    srcs = [W.ScanSource(s) for s in specs]
+    orcs = [_oracle(s.params, s.heap_blocks) for s in specs]
+    pool = sum(s.heap_blocks for s in specs)
+    heavy_seen = False
+    with Engine(max_maps=16, pool_blocks=pool, max_batch_points=1 << 18, max_publish=1 << 23) as eng:
+        mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+        for k in range(4):
+            scans = [src.scan(k) for src in srcs]
+            rs = eng.integrate_batch([(mids[i], *scans[i]) for i in range(len(specs))], pub_cap=1 << 20)
+            for i, r in enumerate(rs):
+                assert_scan_equal(r, orcs[i].integrate(*scans[i], pub_cap=1 << 20),
+                                  specs[i].params.truncation_distance, f"step {k} map {i}")
+                heavy_seen |= r.stats["voxel_updates"] > 20 * max(r.stats["blocks_touched"], 1)
+        for i in range(len(specs)):
+            assert_state_equal(eng, mids[i], orcs[i], specs[i].heap_blocks, voxels=(i < 3))
+    assert heavy_seen
+
+
+@pytest.mark.parametrize("cfg", [dict(bucket_size=4), dict(bucket_size=16), dict(ray_threads=128, ray_chunk=256),
+                                 dict(graphs=False), dict(ray_chunk=64, bucket_size=4, graphs=False)])
+def test_engine_configs_give_identical_results(built, cfg):
+    """Tuning knobs (bucket size, CTA size, work-queue chunk, graphs) change
+    nothing in the results."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    specs = _mixed_specs()[:4]
+    srcs = [W.ScanSource(s) for s in specs]
+    scans = [[src.scan(k) for src in srcs] for k in range(3)]
+    pool = sum(s.heap_blocks for s in specs)
+    outs = []
+    for kw in ({}, cfg):
+        with Engine(max_maps=8, pool_blocks=pool, max_batch_points=1 << 18, **kw) as eng:
+            mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+            res = []
+            for k in range(3):
+                rs = eng.integrate_batch([(mids[i], *scans[k][i]) for i in range(len(specs))], pub_cap=1 << 20)
+                res.append([(r.count, r.pos.copy(), r.data.copy()) for r in rs])
+            outs.append((res, [eng.dump_blocks(m) for m in mids]))
+    for a, b in zip(outs[0][0], outs[1][0]):
+        for (ca, pa, da), (cb, pb, db) in zip(a, b):
+            assert ca == cb and np.array_equal(pa, pb) and np.array_equal(da, db)
+    for (ka, sa), (kb, sb) in zip(outs[0][1], outs[1][1]):
+        assert np.array_equal(ka, kb) and np.array_equal(sa, sb)
+
+
+def test_heap_full_matches_oracle(built):
+    from ros_tsdf_gb300 import Engine, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    spec = W.plain_small(seed=1, heap_blocks=300)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, 300)
+    with Engine(max_maps=2, pool_blocks=300, max_batch_points=1 << 16) as eng:
+        mid = eng.create_map(spec.params, 300)
+        drops = 0
+        for k in range(3):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 20)
+            o = orc.integrate(xyz, org, pub_cap=1 << 20)
+            assert_scan_equal(r, o, 4.0, f"scan {k}")
+            drops += r.stats["heap_full_drops"]
+            if r.stats["heap_full_drops"]:
+                assert r.status == L.ERR_HEAP_FULL
+        assert drops > 0
+        assert_state_equal(eng, mid, orc, 300)
+
+
+def test_publish_overflow_truncates(built):
+    from ros_tsdf_gb300 import Engine, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    spec = W.plain_small(seed=2, heap_blocks=4096)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, 4096)
+    with Engine(max_maps=2, pool_blocks=4096, max_batch_points=1 << 16) as eng:
+        mid = eng.create_map(spec.params, 4096)
+        xyz, org = src.scan(0)
+        r = eng.integrate(mid, xyz, org, pub_cap=1000)
+        pos, data, cnt, st, _ = orc.integrate(xyz, org, pub_cap=1000)
+        assert r.status == L.WARN_PUBLISH_OVERFLOW
+        assert r.count == cnt > 1000 and len(r.pos) == 1000
+        assert np.array_equal(r.pos, pos) and np.array_equal(r.data, data)
+
+
+def test_bad_points_empty_scan_and_pcl_stride(built):
+    from ros_tsdf_gb300 import Engine, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    spec = W.plain_small(seed=5, heap_blocks=4096)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, 4096)
+    with Engine(max_maps=2, pool_blocks=4096, max_batch_points=1 << 16) as eng:
+        mid = eng.create_map(spec.params, 4096)
+        xyz, org = src.scan(0)
+        bad = np.concatenate([xyz, np.array([[np.nan, 0, 0], [np.inf, 1, 1], org, [1e9, 0, 0]], np.float32)])
+        pcl = np.zeros((len(bad), 4), np.float32)
+        pcl[:, :3] = bad
+        r = eng.integrate(mid, pcl, org, pub_cap=1 << 20)
+        assert r.status == L.ERR_BAD_POINTS and r.stats["bad_points"] == 4
+        assert_scan_equal(r, orc.integrate(bad, org, pub_cap=1 << 20), 4.0, "bad points")
+        empty = np.zeros((0, 3), np.float32)
+        org2 = org + np.float32(3.0)
+        r = eng.integrate(mid, empty, org2, pub_cap=1 << 20)
+        assert r.status == 0 and r.stats["n_points"] == 0
+        assert_scan_equal(r, orc.integrate(empty, org2, pub_cap=1 << 20), 4.0, "empty scan")
+        assert_state_equal(eng, mid, orc, 4096)
+
+
+def test_map_lifecycle_and_admission(built):
+    from ros_tsdf_gb300 import Engine, TsdfError, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    p = W.PARAMS_SMALL
+    with Engine(max_maps=3, pool_blocks=1000, max_batch_points=1 << 14) as eng:
+        a = eng.create_map(p, 600)
+        with pytest.raises(TsdfError) as e:
+            eng.create_map(p, 600)  # admission: 400 blocks left
+        assert e.value.status == L.ERR_HEAP_FULL
+        b = eng.create_map(p, 400)
+        eng.destroy_map(a)
+        c = eng.create_map(p, 500)  # reuses the freed range
+        assert c == a
+        with pytest.raises(TsdfError):
+            eng.integrate(7, np.zeros((1, 3), np.float32), [0, 0, 0])
+        xyz = np.array([[10, 0, 0]], np.float32)
+        with pytest.raises(TsdfError) as e:
+            eng.integrate_batch([(b, xyz, [0, 0, 0]), (b, xyz, [0, 0, 0])])
+        assert e.value.status == L.ERR_INVALID_ARG
+        with pytest.raises(TsdfError) as e:
+            eng.create_map(replace(p, truncation_distance=40.0), 100)  # routes cap
+        assert e.value.status == L.ERR_INVALID_ARG
+        # a fresh map after destroy starts empty
+        r = eng.integrate(c, xyz, [0, 0, 0])
+        assert r.stats["alloc_blocks_before"] == 0
+
+
+def test_served_mode_isolation(built):
+    """Scans submitted asynchronously from many maps (continuous batching over
+    two lanes) give each map exactly its alone-and-in-order result."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    specs = _mixed_specs()[:6]
+    srcs = [W.ScanSource(s) for s in specs]
+    scans = [[srcs[i].scan(k) for k in range(3)] for i in range(len(specs))]
+    pool = sum(s.heap_blocks for s in specs)
+    rng = np.random.default_rng(0)
+    with Engine(max_maps=8, pool_blocks=pool, max_batch_points=1 << 18, lanes=2) as eng:
+        mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+        order = [(i, k) for k in range(3) for i in rng.permutation(len(specs))]
+        tickets = {}
+        for i, k in order:
+            tickets[(i, k)] = eng.submit(mids[i], *scans[i][k], pub_cap=1 << 20)
+            time.sleep(float(rng.uniform(0, 0.002)))
+        results = {key: eng.wait(t, timeout_ms=60000) for key, t in tickets.items()}
+    for i, s in enumerate(specs):
+        orc = _oracle(s.params, s.heap_blocks)
+        for k in range(3):
+            r = results[(i, k)]
+            assert r.stats["t_done_ns"] >= r.stats["t_launch_ns"] >= r.stats["t_submit_ns"] > 0
+            assert_scan_equal(r, orc.integrate(*scans[i][k], pub_cap=1 << 20), s.params.truncation_distance,
+                              f"map {i} scan {k}")
+
+
+def test_handler_mirror(built):
+    import ros_tsdf_gb300 as tsdf
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = W.plain_small(seed=6, heap_blocks=4096)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, 4096)
+    p = spec.params
+    tsdf.initGlobalVars(p.voxel_size, p.truncation_distance, p.max_weight, p.publish_distance_squared,
+                        p.garbage_collect_distance_squared)
+    with Engine(max_maps=2, pool_blocks=4096, max_batch_points=1 << 16) as eng:
+        h = tsdf.TSDFHandler(engine=eng, heap_blocks=4096)
+        cap = tsdf.PUBLISH_VOXELS_MAX_SIZE
+        pos = np.zeros((cap, 3), np.float32)
+        data = np.zeros((cap, 2), np.float32)
+        size = np.array([0], np.int32)
+        xyz, org = src.scan(0)
+        cloud = np.zeros((len(xyz), 4), np.float32)
+        cloud[:, :3] = xyz
+        h.processPointCloudAndUpdateVoxels(cloud, org, pos, size, data)
+        opos, odata, cnt, _, _ = orc.integrate(xyz, org)
+        assert size[0] == cnt and np.array_equal(pos[:cnt], opos) and np.array_equal(data[:cnt], odata)
+        # in/out count: a second call appends after the current count
+        xyz, org = src.scan(1)
+        h.processPointCloudAndUpdateVoxels(xyz, org, pos, size, data)
+        opos, odata, cnt2, _, _ = orc.integrate(xyz, org)
+        assert size[0] == cnt + cnt2 and np.array_equal(pos[cnt:cnt + cnt2], opos)
+        h.close()
+
+
+def test_full_size_large_stream(built):
+    """64x1024 lidar, voxel 0.1 m, truncation 0.4 m, 2M-block heap (the large
+    single-stream config) against the oracle."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = W.large_stream(seed=2000)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, spec.heap_blocks)
+    with Engine(max_maps=2, pool_blocks=spec.heap_blocks, max_batch_points=1 << 17, max_publish=1 << 22) as eng:
+        mid = eng.create_map(spec.params, spec.heap_blocks)
+        for k in range(3):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 22)
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 22), 0.4, f"scan {k}")
+            assert r.stats["n_points"] > 30000
+        assert_state_equal(eng, mid, orc, spec.heap_blocks, voxels=False)
+
+
+def test_full_size_stress_scan(built):
+    """128x2048 lidar (262,144 rays), voxel 0.05 m: one map, two scans."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = replace(W.stress8(1)[0], heap_blocks=1 << 20)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, spec.heap_blocks)
+    with Engine(max_maps=2, pool_blocks=spec.heap_blocks, max_batch_points=1 << 18, max_publish=1 << 22) as eng:
+        mid = eng.create_map(spec.params, spec.heap_blocks)
+        for k in range(2):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 22)
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 22), 0.2, f"scan {k}")
+        assert_state_equal(eng, mid, orc, spec.heap_blocks, voxels=False)
+
+
+def test_rehash_keeps_parity(built):
+    """A tiny hash table under heavy gc churn fills with tombstones and is
+    rebuilt between steps; key -> slot stays identical to the oracle."""
+    from ros_tsdf_gb300 import Engine, TsdfParams, workloads as W
+
+    spec = replace(W.plain_small(seed=12, heap_blocks=700), params=TsdfParams(0.5, 4.0, 1000.0, 400.0, 625.0),
+                   traj=W.Traj(0, 40.0, 5.0, 8.0, 4.0))
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, 700)
+    with Engine(max_maps=2, pool_blocks=700, max_batch_points=1 << 16) as eng:
+        mid = eng.create_map(spec.params, 700)
+        for k in range(25):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 20)
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 20), 4.0, f"scan {k}")
+        info = eng.map_info(mid)
+        assert info["rehashes"] > 0
+        assert_state_equal(eng, mid, orc, 700)
