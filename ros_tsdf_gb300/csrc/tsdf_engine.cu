@@ -271,6 +271,11 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.entries, entry_cap, tr));
   TRY(dalloc(eng, &x.bin_d, entry_cap, tr));
   TRY(dalloc(eng, &x.heavy, rec_cap, tr));
+  x.hchunk_cap = (int)std::min<long long>(rec_cap / 128 + 64, 1 << 15);
+  TRY(dalloc(eng, &x.hchunk_base, x.hchunk_cap, tr));
+  TRY(dalloc(eng, &x.hcnt, (long long)x.hchunk_cap * kVoxelsPerBlock, tr));
+  TRY(dalloc(eng, &x.hvoff, (long long)(x.hchunk_cap / 2 + 1) * (kVoxelsPerBlock + 1), tr));
+  TRY(dalloc(eng, &x.hbin_base, x.hchunk_cap / 2 + 1, tr));
   x.entry_cap = entry_cap;
   TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
   TRY(dalloc(eng, &x.digit_tot, 256, tr));

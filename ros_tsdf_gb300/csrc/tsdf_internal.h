@@ -109,6 +109,8 @@ struct LaneCounters {
   long long scan_total;   // scratch for scans
   long long n_heavy;      // segments with more records than one update chunk
   unsigned long long bin_cursor;  // bump allocator of the heavy-segment bins
+  long long n_hplanned;   // heavy segments whose bins are built by the multi-CTA passes
+  long long n_hchunks;    // their 128-record chunks
   int error;              // bit flags, see ERR_*
   int pad;
 };
@@ -148,6 +150,11 @@ struct Ctx {
   int* gc_prefix;
   int* heavy;                    // segment ids of heavy segments
   float* bin_d;                  // heavy-segment bins (entry_cap floats)
+  int* hchunk_base;              // [heavy] first chunk of each planned heavy segment
+  int* hcnt;                     // [hchunk_cap][512] per-chunk voxel counts, then offsets
+  int* hvoff;                    // [hchunk_cap/2][513] per-voxel bin offsets of a heavy segment
+  unsigned long long* hbin_base; // [hchunk_cap/2] bin base of a heavy segment
+  int hchunk_cap;
   int max_tiles_rank;
   int max_tiles_rec;
   int max_tiles_scan;

@@ -695,14 +695,14 @@ __global__ void k_gather_ranks(Ctx c) {
   }
 }
 
-__global__ void k_alloc_prefix(Ctx c) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(1024) k_alloc_prefix(Ctx c) {
+  __shared__ int s_warp[32];
   const int n = c.hdr->n_items;
-  int acc = 0;
-  for (int i = 0; i < n; ++i) {
-    c.item_i[i * II_COUNT + II_NEW_BASE] = acc;
-    acc += c.item_i[i * II_COUNT + II_NEW];
-  }
+  const int i = threadIdx.x;
+  const int v = i < n ? c.item_i[i * II_COUNT + II_NEW] : 0;
+  int tot;
+  const int ex = block_excl_scan(v, s_warp, &tot);
+  if (i < n) c.item_i[i * II_COUNT + II_NEW_BASE] = ex;
 }
 
 // One warp per new block, in first-touch order: pop the free list, resolve
@@ -753,23 +753,26 @@ __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel) {
 }
 
 // block_count += allocated; slot enumeration bases for publish / gc.
-__global__ void k_alloc_finalize(Ctx c) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(1024) k_alloc_finalize(Ctx c) {
+  __shared__ int s_warp[32];
   const int n = c.hdr->n_items;
-  long long acc = 0;
-  for (int i = 0; i < n; ++i) {
-    int mi = c.items[i].map;
-    const MapDev& m = c.maps[mi];
-    int bc = c.mctr[mi].block_count;
-    int nn = c.item_i[i * II_COUNT + II_NEW];
-    int room = m.heap_cap - bc;
+  const int i = threadIdx.x;
+  int hw = 0;
+  if (i < n) {
+    const int mi = c.items[i].map;
+    const int bc = c.mctr[mi].block_count;
+    const int nn = c.item_i[i * II_COUNT + II_NEW];
+    const int room = c.maps[mi].heap_cap - bc;
     c.mctr[mi].block_count = bc + (nn < room ? nn : room);
-    int hw = c.mctr[mi].hw;
-    c.item_i[i * II_COUNT + II_SLOT_BASE] = (int)acc;
-    c.item_i[i * II_COUNT + II_SLOT_N] = hw;
-    acc += hw;
+    hw = c.mctr[mi].hw;
   }
-  c.ctr->n_enum = acc;
+  int tot;
+  const int ex = block_excl_scan(hw, s_warp, &tot);
+  if (i < n) {
+    c.item_i[i * II_COUNT + II_SLOT_BASE] = ex;
+    c.item_i[i * II_COUNT + II_SLOT_N] = hw;
+  }
+  if (i == 0) c.ctr->n_enum = tot;
 }
 
 // ----------------------------------------------------------------------------
@@ -936,6 +939,180 @@ __global__ void k_seg_classify(Ctx c) {
   }
 }
 
+// Heavy segments: a multi-CTA counting sort of their updates into per-voxel
+// bins, ordered by point index.  plan -> per-chunk voxel counts -> per-voxel
+// scan over chunks -> ordered placement.  Segments whose chunks exceed the
+// scratch capacity fall back to the single-CTA passes in k_update.
+__global__ void __launch_bounds__(1024) k_heavy_plan(Ctx c) {
+  __shared__ int s_warp[32];
+  __shared__ int s_stop;
+  const long long nh = c.ctr->n_heavy;
+  const long long nseg = c.ctr->n_seg;
+  const long long nrec = c.ctr->n_rec_live;
+  const long long hcap = c.hchunk_cap / 2;
+  long long carry = 0, planned = 0;
+  if (threadIdx.x == 0) s_stop = 0;
+  __syncthreads();
+  for (long long b = 0; b < nh; b += blockDim.x) {
+    const long long h = b + threadIdx.x;
+    int nch = 0;
+    if (h < nh) {
+      const long long j = c.heavy[h];
+      const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+      nch = (int)((b1 - c.seg_start[j] + UPD_T - 1) / UPD_T);
+    }
+    int tot;
+    const int ex = block_excl_scan(nch, s_warp, &tot);
+    const bool ok = h < nh && carry + ex + nch <= c.hchunk_cap && h < hcap;
+    if (ok) c.hchunk_base[h] = (int)(carry + ex);
+    const int nok = __syncthreads_count(ok);
+    planned += nok;
+    carry += tot;
+    if (nok < (int)min((long long)blockDim.x, nh - b)) break;
+  }
+  if (threadIdx.x == 0) {
+    c.ctr->n_hplanned = planned;
+    long long n = 0;
+    if (planned > 0) {
+      const long long h = planned - 1;
+      const long long j = c.heavy[h];
+      const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+      n = c.hchunk_base[h] + (b1 - c.seg_start[j] + UPD_T - 1) / UPD_T;
+    }
+    c.ctr->n_hchunks = n;
+  }
+}
+
+__device__ __forceinline__ int find_heavy(const int* base, int n, long long gc) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= gc)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int load_chunk_entries(const Ctx& c, const unsigned* rv, long long r, long long b1,
+                                                  float* s_d, unsigned short* s_l, int t) {
+  int ne = 0;
+  if (r < b1) {
+    const unsigned v = rv[r];
+    const int cnt = (int)(v & 31u);
+    const uint2* e = c.entries + (v >> 5);
+    uint2 xs[kUpdEntries];
+#pragma unroll
+    for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
+#pragma unroll
+    for (int k = 0; k < kUpdEntries; ++k) {
+      const uint2 x = xs[k];
+      if (x.y == kBadLocal) continue;
+      s_d[t * kUpdEntries + ne] = __uint_as_float(x.x);
+      s_l[t * kUpdEntries + ne] = (unsigned short)x.y;
+      ++ne;
+    }
+  }
+  return ne;
+}
+
+__global__ void __launch_bounds__(UPD_T) k_heavy_count(Ctx c, int rec_sel) {
+  __shared__ float s_d[UPD_T * kUpdEntries];
+  __shared__ unsigned short s_l[UPD_T * kUpdEntries];
+  __shared__ int s_cnt[kVoxelsPerBlock];
+  const int t = threadIdx.x;
+  const long long nch = c.ctr->n_hchunks;
+  const int np = (int)c.ctr->n_hplanned;
+  const long long nseg = c.ctr->n_seg;
+  const long long nrec = c.ctr->n_rec_live;
+  const unsigned* rv = c.rec_val[rec_sel];
+  for (long long gc = blockIdx.x; gc < nch; gc += gridDim.x) {
+    const int h = find_heavy(c.hchunk_base, np, gc);
+    const long long j = c.heavy[h];
+    const long long b0 = c.seg_start[j];
+    const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+    const long long r0 = b0 + (gc - c.hchunk_base[h]) * UPD_T;
+    for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_cnt[l] = 0;
+    __syncthreads();
+    const int ne = load_chunk_entries(c, rv, r0 + t, b1, s_d, s_l, t);
+    for (int k = 0; k < ne; ++k) atomicAdd(&s_cnt[s_l[t * kUpdEntries + k]], 1);
+    __syncthreads();
+    int* out = c.hcnt + gc * kVoxelsPerBlock;
+    for (int l = t; l < kVoxelsPerBlock; l += UPD_T) out[l] = s_cnt[l];
+    __syncthreads();
+  }
+}
+
+// One CTA of 512 threads per planned heavy segment: per voxel, exclusive scan
+// of its counts over the segment's chunks; per-voxel bin offsets; bin base.
+__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c) {
+  __shared__ int s_warp[32];
+  const int l = threadIdx.x;
+  const int np = (int)c.ctr->n_hplanned;
+  const long long nch = c.ctr->n_hchunks;
+  for (int h = blockIdx.x; h < np; h += gridDim.x) {
+    const long long c0 = c.hchunk_base[h];
+    const long long c1 = (h + 1 < np) ? c.hchunk_base[h + 1] : nch;
+    int run = 0;
+    for (long long gc = c0; gc < c1; ++gc) {
+      int* p = c.hcnt + gc * kVoxelsPerBlock + l;
+      const int v = *p;
+      *p = run;
+      run += v;
+    }
+    int tot;
+    const int ex = block_excl_scan(run, s_warp, &tot);
+    int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
+    vo[l] = ex;
+    if (l == 0) {
+      vo[kVoxelsPerBlock] = tot;
+      c.hbin_base[h] = atomicAdd(&c.ctr->bin_cursor, (unsigned long long)tot);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
+  __shared__ float s_d[UPD_T * kUpdEntries];
+  __shared__ unsigned short s_l[UPD_T * kUpdEntries];
+  __shared__ unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];
+  const int t = threadIdx.x;
+  const unsigned lt_bits = (1u << (t & 31)) - 1u;
+  const long long nch = c.ctr->n_hchunks;
+  const int np = (int)c.ctr->n_hplanned;
+  const long long nseg = c.ctr->n_seg;
+  const long long nrec = c.ctr->n_rec_live;
+  const unsigned* rv = c.rec_val[rec_sel];
+  for (long long gc = blockIdx.x; gc < nch; gc += gridDim.x) {
+    const int h = find_heavy(c.hchunk_base, np, gc);
+    const long long j = c.heavy[h];
+    const long long b0 = c.seg_start[j];
+    const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+    const long long r0 = b0 + (gc - c.hchunk_base[h]) * UPD_T;
+    for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+#pragma unroll
+      for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
+    }
+    __syncthreads();
+    const int ne = load_chunk_entries(c, rv, r0 + t, b1, s_d, s_l, t);
+    for (int k = 0; k < ne; ++k) atomicOr(&s_mask[s_l[t * kUpdEntries + k]][t >> 5], 1u << (t & 31));
+    __syncthreads();
+    const int* hc = c.hcnt + gc * kVoxelsPerBlock;
+    const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
+    const unsigned long long base = c.hbin_base[h];
+    const bool fits = base + (unsigned long long)vo[kVoxelsPerBlock] <= (unsigned long long)c.entry_cap;
+    for (int k = 0; k < ne && fits; ++k) {
+      const int l = s_l[t * kUpdEntries + k];
+      int rank = __popc(s_mask[l][t >> 5] & lt_bits);
+      for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+      c.bin_d[base + vo[l] + hc[l] + rank] = s_d[t * kUpdEntries + k];
+    }
+    if (!fits && t == 0) set_error(c.ctr, ERR_CAPACITY);
+    __syncthreads();
+  }
+}
+
 // ----------------------------------------------------------------------------
 // update: one CTA per block touched (updateVoxelsCuda, tsdf_handler.cu:
 // 604-665).  The block's 512 voxels are staged in shared memory with 16-byte
@@ -1040,6 +1217,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
     sv4[t] = gv[t];
     sv4[t + UPD_T] = gv[t + UPD_T];
     if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
+    __syncthreads();  // the staged block and touch mask are shared by every path below
     unsigned n_upd = 0;
     if (!heavy) {
       // ---- light path: the whole segment in one chunk
@@ -1110,8 +1288,44 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
         atomicOr(&s_touch[l >> 5], 1u << (l & 31));
       }
       __syncthreads();
+    } else if (q < c.ctr->n_hplanned) {
+      // ---- planned heavy segment: bins already built; each owner runs its
+      // voxels' chains with the next loads in flight
+      const int* vo = c.hvoff + q * (kVoxelsPerBlock + 1);
+      const float* bins = c.bin_d + c.hbin_base[q];
+      const bool fits = c.hbin_base[q] + (unsigned long long)vo[kVoxelsPerBlock] <= (unsigned long long)c.entry_cap;
+      for (int l = t; l < kVoxelsPerBlock && fits; l += UPD_T) {
+        const int b = vo[l], e = vo[l + 1];
+        if (e == b) continue;
+        float sdf = s_vox[l].x, w = s_vox[l].y;
+        float cur[8], nxt[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cur[k] = b + k < e ? bins[b + k] : 0.0f;
+        for (int i = b; i < e; i += 8) {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) nxt[k] = i + 8 + k < e ? bins[i + 8 + k] : 0.0f;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            if (i + k < e) {
+              const float d = cur[k];
+              const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
+              const float wd = fmul(wt, d);
+              const float nw = fadd(w, wt);
+              sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
+              w = fminf(nw, maxw);
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 8; ++k) cur[k] = nxt[k];
+        }
+        n_upd += (unsigned)(e - b);
+        s_vox[l] = make_float2(sdf, w);
+        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+      }
+      __syncthreads();
     } else {
-      // ---- heavy path, pass 0: per-voxel update counts over all records
+      // ---- heavy segment beyond the planning capacity, pass 0: per-voxel
+      // update counts over all records
       for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_run[l] = 0;
       __syncthreads();
       for (long long cb = b0; cb < b1; cb += UPD_T) {
@@ -1287,21 +1501,20 @@ struct PrefixOut {
 };
 
 // per-item bases of a scanned enumeration array
-__global__ void k_item_bases(Ctx c, const int* prefix, const long long* total, int base_field, int count_field,
-                             int stat_field) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(1024) k_item_bases(Ctx c, const int* prefix, const long long* total,
+                                                     int base_field, int count_field, int stat_field) {
   const int n = c.hdr->n_items;
+  const int i = threadIdx.x;
+  if (i >= n) return;
   const long long ne = c.ctr->n_enum;
   const long long tot = *total;
-  for (int i = 0; i < n; ++i) {
-    long long sb = c.item_i[i * II_COUNT + II_SLOT_BASE];
-    long long se = sb + c.item_i[i * II_COUNT + II_SLOT_N];
-    long long b = sb < ne ? prefix[sb] : tot;
-    long long e = se < ne ? prefix[se] : tot;
-    c.item_i[i * II_COUNT + base_field] = (int)b;
-    if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
-    if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
-  }
+  const long long sb = c.item_i[i * II_COUNT + II_SLOT_BASE];
+  const long long se = sb + c.item_i[i * II_COUNT + II_SLOT_N];
+  const long long b = sb < ne ? prefix[sb] : tot;
+  const long long e = se < ne ? prefix[se] : tot;
+  c.item_i[i * II_COUNT + base_field] = (int)b;
+  if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
+  if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
 }
 
 // publish write: one warp per publishing block; voxels in ascending local
@@ -1387,16 +1600,16 @@ __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
   }
 }
 
-__global__ void k_gc_finalize(Ctx c) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(1024) k_gc_finalize(Ctx c) {
   const int n = c.hdr->n_items;
-  for (int i = 0; i < n; ++i) {
-    int mi = c.items[i].map;
-    int g = c.item_i[i * II_COUNT + II_GC_N];
-    c.mctr[mi].block_count -= g;
-    c.item_stats[i * ST_COUNT + ST_GC] = g;
-    c.item_stats[i * ST_COUNT + ST_BC] = c.mctr[mi].block_count;
-  }
+  const int i = threadIdx.x;
+  if (i >= n) return;
+  const int mi = c.items[i].map;
+  const int g = c.item_i[i * II_COUNT + II_GC_N];
+  const int bc = c.mctr[mi].block_count - g;
+  c.mctr[mi].block_count = bc;
+  c.item_stats[i * ST_COUNT + ST_GC] = g;
+  c.item_stats[i * ST_COUNT + ST_BC] = bc;
 }
 
 // ----------------------------------------------------------------------------
@@ -1458,13 +1671,13 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
   *launches += 1;
   radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
              lc.rank_passes, c.max_tiles_rank, lc.sm_count, s, launches);
-  k_alloc_prefix<<<1, 32, 0, s>>>(c);
+  k_alloc_prefix<<<1, 1024, 0, s>>>(c);
   *launches += 1;
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1);
-  k_alloc_finalize<<<1, 32, 0, s>>>(c);
+  k_alloc_finalize<<<1, 1024, 0, s>>>(c);
   *launches += 2;
 }
 
@@ -1489,7 +1702,11 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_rec_live, &c.ctr->n_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
   k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c);
-  *launches += 4;
+  k_heavy_plan<<<1, 1024, 0, s>>>(c);
+  k_heavy_count<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
+  k_heavy_scan<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c);
+  k_heavy_place<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
+  *launches += 8;
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
@@ -1505,7 +1722,7 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
   k_scan_reduce<<<grid, SC_T, 0, s>>>(cin, &c.ctr->n_enum, c.tile_sums);
   k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_enum, &c.ctr->scan_total);
   k_scan_apply<<<grid, SC_T, 0, s>>>(cin, pout, &c.ctr->n_enum, c.tile_sums);
-  k_item_bases<<<1, 32, 0, s>>>(c, c.pub_prefix, &c.ctr->scan_total, II_PUB_BASE, -1, ST_PUB);
+  k_item_bases<<<1, 1024, 0, s>>>(c, c.pub_prefix, &c.ctr->scan_total, II_PUB_BASE, -1, ST_PUB);
   k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c);
   *launches += 6;
 }
@@ -1517,9 +1734,9 @@ void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* laun
   k_scan_reduce<<<grid, SC_T, 0, s>>>(gin, &c.ctr->n_enum, c.tile_sums);
   k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_enum, &c.ctr->scan_total);
   k_scan_apply<<<grid, SC_T, 0, s>>>(gin, gout, &c.ctr->n_enum, c.tile_sums);
-  k_item_bases<<<1, 32, 0, s>>>(c, c.gc_prefix, &c.ctr->scan_total, II_GC_BASE, II_GC_N, -1);
+  k_item_bases<<<1, 1024, 0, s>>>(c, c.gc_prefix, &c.ctr->scan_total, II_GC_BASE, II_GC_N, -1);
   k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
-  k_gc_finalize<<<1, 32, 0, s>>>(c);
+  k_gc_finalize<<<1, 1024, 0, s>>>(c);
   *launches += 6;
 }
 
