@@ -189,6 +189,19 @@ tsdf_status tsdf_ticket_times(tsdf_engine* eng, uint64_t ticket, int64_t* t_subm
                               int64_t* t_done);
 tsdf_status tsdf_forget(tsdf_engine* eng, uint64_t ticket);
 
+/* ---- block enumeration (replaces TSDFHandler::getVoxelBlocks) ---------- */
+/* The distinct blocks the block DDA of every point visits (getVoxelBlocks +
+ * removeRedundantVoxels, tsdf_handler.cu:1071-1094, :255-272, :717-741), as
+ * integer block coordinates floor(centre / block size), 3 ints each, in
+ * first-touch order (points in input order, DDA order within a point; the
+ * order an empty map allocates them).  No map is touched.  xyz and kxyz may
+ * be host or device memory.  *count = total (kxyz holds min(total, cap)).
+ * TSDF_ERR_BAD_POINTS when points were skipped; TSDF_ERR_CAPACITY when
+ * n_points x block-DDA cap exceeds the engine's scratch. */
+tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, const float* xyz, int64_t n_points,
+                                  int stride_bytes, const float origin[3], int32_t* kxyz, int64_t cap,
+                                  int64_t* count);
+
 /* ---- inspection for parity tests ------------------------------------- */
 /* Allocated blocks in ascending heap slot: integer block coordinates
  * (3 ints each, floor(centre / block size)) and heap slot.  *count = total. */

@@ -69,7 +69,8 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     nvcc = _nvcc()
     eng = LIB / "libtsdf_gb300.so"
     gen = LIB / "libscangen.so"
-    eng_srcs = [CSRC / "tsdf_kernels.cu", CSRC / "tsdf_engine.cu", CSRC / "tsdf_internal.h", INCLUDE / "tsdf_c.h"]
+    eng_srcs = [CSRC / "tsdf_kernels.cu", CSRC / "tsdf_engine.cu", CSRC / "tsdf_blocks.cu", CSRC / "tsdf_internal.h",
+                INCLUDE / "tsdf_c.h"]
     gen_srcs = [CSRC / "scangen.cpp"]
     build_dir = LIB / "_obj"
     build_dir.mkdir(exist_ok=True)
@@ -81,12 +82,14 @@ def build(verbose: bool = False, force: bool = False) -> dict:
                        "-o", str(build_dir / "tsdf_kernels.o")])
         stage1.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / "tsdf_engine.cu"),
                        "-o", str(build_dir / "tsdf_engine.o")])
+        stage1.append([nvcc, *ARCH, *NVCC_FLAGS, *KERNEL_FLAGS, "-c", str(CSRC / "tsdf_blocks.cu"),
+                       "-o", str(build_dir / "tsdf_blocks.o")])
     if need_gen:
         stage1.append(["g++", *CXX_FLAGS, "-shared", "-o", str(gen), str(CSRC / "scangen.cpp")])
     _run_all(stage1, verbose)
     if need_eng:
         _run_all([[nvcc, *ARCH, "-shared", "-o", str(eng), str(build_dir / "tsdf_kernels.o"),
-                   str(build_dir / "tsdf_engine.o"), "-lcudart", "-lpthread"]], verbose)
+                   str(build_dir / "tsdf_engine.o"), str(build_dir / "tsdf_blocks.o"), "-lcudart", "-lpthread"]], verbose)
         _write_stamp(eng)
     if need_gen:
         _write_stamp(gen)

@@ -170,6 +170,9 @@ struct tsdf_engine {
   long long hash_pool = 0;
   void* flush_buf = nullptr;
   int* d_tmp = nullptr;  // rehash scratch (2 ints)
+  void* eb_scratch = nullptr;  // block enumeration scratch (allocated on first use)
+  long long eb_max_inc = 0;
+  int32_t* eb_out = nullptr;
   RangeAlloc heap_ranges, hash_ranges;
   std::vector<MapHost> maps;
   Lane lanes[kMaxLanes];
@@ -779,6 +782,8 @@ tsdf_status tsdf_engine_destroy(tsdf_engine* eng) {
   cudaFree(eng->d_mctr);
   cudaFree(eng->d_tmp);
   if (eng->flush_buf) cudaFree(eng->flush_buf);
+  if (eng->eb_scratch) cudaFree(eng->eb_scratch);
+  if (eng->eb_out) cudaFree(eng->eb_out);
   delete eng;
   return TSDF_OK;
 }
@@ -1004,6 +1009,57 @@ tsdf_status tsdf_forget(tsdf_engine* eng, uint64_t ticket) {
   if (!it->second->done) return TSDF_ERR_NOT_READY;
   eng->tickets.erase(it);
   return TSDF_OK;
+}
+
+tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, const float* xyz, int64_t n_points,
+                                  int stride_bytes, const float origin[3], int32_t* kxyz, int64_t cap,
+                                  int64_t* count) {
+  if (!eng || !params || !origin || !count || n_points < 0 || (n_points > 0 && !xyz) || cap < 0 ||
+      (cap > 0 && !kxyz) || stride_bytes < 12 || (stride_bytes & 3))
+    return TSDF_ERR_INVALID_ARG;
+  if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f)) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (eng->sched_running) return fail(eng, TSDF_ERR_BUSY, "served mode owns the lanes");
+  CK(cudaSetDevice(eng->device));
+  Lane& L = eng->lanes[0];
+  if (!eng->eb_scratch) {
+    eng->eb_max_inc = eng->cfg.max_batch_points * (long long)(eng->cfg.max_routes - 4);
+    CK(cudaMalloc(&eng->eb_scratch, (size_t)eb_scratch_bytes(eng->eb_max_inc, nullptr)));
+    CK(cudaMalloc(&eng->eb_out, (size_t)eng->eb_max_inc * 3 * sizeof(int32_t)));
+  }
+  const float* xin = nullptr;
+  const void* dp = nullptr;
+  if (n_points == 0) {
+    xin = reinterpret_cast<const float*>(L.d_points);
+  } else if (device_accessible(xyz, &dp)) {
+    xin = static_cast<const float*>(dp);
+  } else {
+    const long long nb = n_points * (long long)stride_bytes;
+    if (nb > eng->cfg.max_batch_points * 16) return fail(eng, TSDF_ERR_CAPACITY, "point staging full");
+    CK(cudaMemcpyAsync(L.d_points, xyz, nb, cudaMemcpyHostToDevice, L.stream));
+    xin = reinterpret_cast<const float*>(L.d_points);
+  }
+  const void* op = nullptr;
+  const bool direct = cap > 0 && device_accessible(kxyz, &op);
+  int32_t* out = direct ? (int32_t*)op : eng->eb_out;
+  const long long dcap = direct ? cap : std::min<long long>(cap, eng->eb_max_inc);
+  const int rc = eb_launch(eng->eb_scratch, eng->eb_max_inc, xin, n_points, stride_bytes, origin,
+                           params->voxel_size, params->truncation_distance, out, dcap, eng->sm_count, L.stream);
+  if (rc == 1) return fail(eng, TSDF_ERR_CAPACITY, "points x block-DDA cap exceed the enumeration scratch");
+  if (rc != 0) return fail(eng, TSDF_ERR_CUDA, "block enumeration launch failed");
+  eng->launches += 5;
+  long long total = 0, bad = 0;
+  int err = 0;
+  if (eb_read_counts(eng->eb_scratch, eng->eb_max_inc, &total, &bad, &err, L.stream) != 0)
+    return fail(eng, TSDF_ERR_CUDA, "block enumeration failed");
+  *count = total;
+  if (!direct && cap > 0 && total > 0) {
+    const long long k = std::min<long long>(total, dcap);
+    CK(cudaMemcpyAsync(kxyz, eng->eb_out, sizeof(int32_t) * 3 * k, cudaMemcpyDeviceToHost, L.stream));
+    CK(cudaStreamSynchronize(L.stream));
+  }
+  if (err) return fail(eng, TSDF_ERR_HASH_FULL, "block enumeration key set full");
+  return bad > 0 ? TSDF_ERR_BAD_POINTS : TSDF_OK;
 }
 
 tsdf_status tsdf_dump_blocks(tsdf_engine* eng, int map_id, int32_t* kxyz, int32_t* slots, int64_t cap,

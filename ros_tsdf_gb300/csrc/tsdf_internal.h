@@ -200,4 +200,11 @@ void launch_map_rehash(const Ctx& c, int map, int bucket_size, long long heap_ba
                        cudaStream_t s);
 void launch_flush(void* buf, long long bytes, int value, cudaStream_t s);
 
+// Block enumeration of one scan (tsdf_blocks.cu).
+long long eb_scratch_bytes(long long max_inc, long long* set_cap_out);
+int eb_launch(void* scratch, long long max_inc, const float* xyz_dev, long long n, int stride, const float origin[3],
+              float voxel_size, float truncation_distance, int32_t* kxyz_dev, long long cap, int sm_count,
+              cudaStream_t s);
+int eb_read_counts(void* scratch, long long max_inc, long long* total, long long* bad, int* error, cudaStream_t s);
+
 }  // namespace tsdfg

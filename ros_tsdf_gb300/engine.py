@@ -192,6 +192,25 @@ class Engine:
         r.stats["t_submit_ns"], r.stats["t_launch_ns"], r.stats["t_done_ns"] = (x.value for x in times)
         return r
 
+    # -- block enumeration ----------------------------------------------------
+    def enumerate_blocks(self, params: TsdfParams, xyz, origin, cap: int | None = None):
+        """Distinct blocks of one scan in first-touch order: (kxyz (n,3) int32, status).
+        xyz may be a host array or a DeviceBuffer."""
+        if isinstance(xyz, DeviceBuffer):
+            ptr, n, stride = xyz.ptr, xyz.shape[0], xyz.shape[1] * 4
+        else:
+            a, stride = _as_points(xyz)
+            self._keep["eb"] = a
+            ptr, n = (a.ctypes.data if a.shape[0] else None), a.shape[0]
+        cap = cap if cap is not None else max(n * 16, 1)
+        out = np.empty((max(cap, 1), 3), np.int32)
+        cnt = C.c_int64()
+        org = (C.c_float * 3)(*[float(v) for v in origin])
+        st = self.lib.tsdf_enumerate_blocks(self.h, C.byref(params.c()), ptr, n, stride, org, out.ctypes.data, cap,
+                                            C.byref(cnt))
+        self._check(st, "tsdf_enumerate_blocks", soft=True)
+        return out[:min(cnt.value, cap)], st
+
     # -- inspection -----------------------------------------------------------
     def dump_blocks(self, map_id: int):
         """(kxyz (n,3) int32, slots (n,) int32) in ascending slot."""

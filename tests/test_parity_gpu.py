@@ -344,3 +344,32 @@ def test_rehash_keeps_parity(built):
         info = eng.map_info(mid)
         assert info["rehashes"] > 0
         assert_state_equal(eng, mid, orc, 700)
+
+
+def test_enumerate_blocks_is_fresh_map_allocation_order(built):
+    """tsdf_enumerate_blocks (getVoxelBlocks + removeRedundantVoxels) lists a
+    scan's blocks in first-touch order: the order an empty map allocates them
+    (slot i holds the i-th), for host and device inputs alike."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    spec = W.plain_small(seed=13, heap_blocks=8192)
+    src = W.ScanSource(spec)
+    with Engine(max_maps=2, pool_blocks=8192, max_batch_points=1 << 16) as eng:
+        for k in range(3):
+            xyz, org = src.scan(k)
+            if k == 2:
+                xyz = np.concatenate([xyz, np.array([[np.nan, 0, 0], org], np.float32)])
+            orc = _oracle(spec.params, 8192)
+            orc.integrate(xyz, org, pub_cap=1)
+            ko, so = orc.dump_blocks()
+            expect = ko[np.argsort(so)]
+            got, st = eng.enumerate_blocks(spec.params, xyz, org)
+            assert np.array_equal(got, expect)
+            assert st == (L.ERR_BAD_POINTS if k == 2 else L.OK)
+            d = eng.device_array(xyz)
+            got_d, _ = eng.enumerate_blocks(spec.params, d, org)
+            d.free()
+            assert np.array_equal(got_d, expect)
+            small, _ = eng.enumerate_blocks(spec.params, xyz, org, cap=5)
+            assert np.array_equal(small, expect[:5])
