@@ -202,6 +202,22 @@ tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, c
                                   int stride_bytes, const float origin[3], int32_t* kxyz, int64_t cap,
                                   int64_t* count);
 
+/* Same result as tsdf_enumerate_blocks, for callers that may not allocate
+ * device memory at call time (a real-time callback that must not stall on
+ * cudaMalloc, a plugin whose host framework owns all device allocation, a
+ * caller without an engine).  No counterpart in the reference.  Allocates
+ * nothing: xyz_dev and kxyz_dev are caller-owned device buffers and the
+ * scratch is a fixed file-scope device array (about 1.2 MB per GPU that loads
+ * the library, kept until exit).  Limit: n_points x ceil(2T / (8 vs)) * 4 <=
+ * 32768, else TSDF_ERR_CAPACITY.  Runs on the current device, on `stream`
+ * (a cudaStream_t; NULL = default stream), and returns after *count is known.
+ * The first call on a device resolves the array's address there and should
+ * come before any stream capture.  Calls share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller. */
+tsdf_status tsdf_enumerate_blocks_noalloc(const tsdf_params* params, const float* xyz_dev, int64_t n_points,
+                                          int stride_bytes, const float origin[3], int32_t* kxyz_dev, int64_t cap,
+                                          int64_t* count, void* stream);
+
 /* ---- inspection for parity tests ------------------------------------- */
 /* Allocated blocks in ascending heap slot: integer block coordinates
  * (3 ints each, floor(centre / block size)) and heap slot.  *count = total. */

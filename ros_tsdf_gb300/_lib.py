@@ -85,6 +85,9 @@ SIGNATURES = [
     ("tsdf_forget", C.c_int, [C.c_void_p, C.c_uint64]),
     ("tsdf_enumerate_blocks", C.c_int, [C.c_void_p, C.POINTER(Params), C.c_void_p, C.c_int64, C.c_int,
                                         C.POINTER(C.c_float), C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    ("tsdf_enumerate_blocks_noalloc", C.c_int, [C.POINTER(Params), C.c_void_p, C.c_int64, C.c_int,
+                                                C.POINTER(C.c_float), C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
+                                                C.c_void_p]),
     ("tsdf_dump_blocks", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_free_list", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_block_voxels", C.c_int, [C.c_void_p, C.c_int, C.c_int32, C.c_void_p]),

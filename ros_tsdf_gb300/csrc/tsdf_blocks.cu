@@ -21,7 +21,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
+#include "../../include/tsdf_c.h"
 #include "tsdf_internal.h"
 
 namespace tsdfg {
@@ -399,3 +401,84 @@ int eb_read_counts(void* scratch, long long max_inc, long long* total, long long
 
 }  // namespace tsdfg
 
+// ===========================================================================
+// Block enumeration that allocates nothing.
+//
+// Who needs it: callers that may not allocate device memory when they call in.
+// A real-time lidar callback must not stall on cudaMalloc (it can synchronize
+// the device and take milliseconds); a plugin inside a host framework that owns
+// every device allocation (a memory-pool-only process) may not allocate behind
+// that framework's back; a caller that only needs the block list should not
+// have to create an engine, whose creation allocates.  This entry point takes
+// device input and output buffers from the caller and keeps its scratch in a
+// file-scope __device__ array, so no call makes any allocation.
+//
+// Limits and rules:
+//   * at most kNoAllocMaxInc = 32768 block incidences per call (points x
+//     block-DDA cap ceil(2T / (8 vs)) * 4, e.g. 4096 points at vs 0.5, T 4);
+//     larger calls return TSDF_ERR_CAPACITY without running;
+//   * the array (about 1.2 MB) is part of the library's device image: every
+//     GPU that loads the library holds it until the process exits;
+//   * it runs on the calling thread's current device; the first call on a
+//     device looks up the array's device address there (cudaGetSymbolAddress,
+//     which may load the module), so make that first call before any stream
+//     capture;
+//   * every call shares the one array, which keeps the previous call's
+//     contents; each call clears what must start empty, but calls whose work
+//     overlaps on the GPU (different streams or threads without ordering)
+//     race on the array and give wrong results.
+namespace tsdfg {
+namespace {
+
+constexpr long long kNoAllocMaxInc = 32768;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[eb_bytes(kNoAllocMaxInc)];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+int g_noalloc_sms[kNoAllocMaxDevices] = {};
+
+}  // namespace
+}  // namespace tsdfg
+
+extern "C" tsdf_status tsdf_enumerate_blocks_noalloc(const tsdf_params* params, const float* xyz_dev,
+                                                     int64_t n_points, int stride_bytes, const float origin[3],
+                                                     int32_t* kxyz_dev, int64_t cap, int64_t* count, void* stream) {
+  using namespace tsdfg;
+  if (!params || !origin || !count || n_points < 0 || (n_points > 0 && !xyz_dev) || cap < 0 ||
+      (cap > 0 && !kxyz_dev) || stride_bytes < 12 || (stride_bytes & 3))
+    return TSDF_ERR_INVALID_ARG;
+  if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f)) return TSDF_ERR_INVALID_ARG;
+  const float bs = params->voxel_size * (float)kVoxelsPerSide;
+  const int amax = (int)(std::ceil(params->truncation_distance * 2.0f / bs) * 4.0f);
+  if (amax <= 0 || n_points * (long long)amax > kNoAllocMaxInc) return TSDF_ERR_CAPACITY;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return TSDF_ERR_CUDA;
+  void* scratch = nullptr;
+  int sms = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return TSDF_ERR_CUDA;
+      int sm = 0;
+      if (cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return TSDF_ERR_CUDA;
+      g_noalloc_ptr[dev] = p;
+      g_noalloc_sms[dev] = sm;
+    }
+    scratch = g_noalloc_ptr[dev];
+    sms = g_noalloc_sms[dev];
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int rc = eb_launch(scratch, kNoAllocMaxInc, xyz_dev, n_points, stride_bytes, origin, params->voxel_size,
+                           params->truncation_distance, kxyz_dev, cap, sms, s);
+  if (rc == 1) return TSDF_ERR_CAPACITY;
+  if (rc != 0) return TSDF_ERR_CUDA;
+  long long total = 0, bad = 0;
+  int err = 0;
+  if (eb_read_counts(scratch, kNoAllocMaxInc, &total, &bad, &err, s) != 0) return TSDF_ERR_CUDA;
+  *count = total;
+  if (err) return TSDF_ERR_HASH_FULL;
+  return bad > 0 ? TSDF_ERR_BAD_POINTS : TSDF_OK;
+}
