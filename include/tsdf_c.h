@@ -228,6 +228,12 @@ tsdf_status tsdf_dump_free_list(tsdf_engine* eng, int map_id, int32_t* out, int6
 /* The 512 voxels of one heap slot. */
 tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, tsdf_voxel* out512);
 
+/* Device self-check of the voxel-update arithmetic: n seeded operand pairs,
+ * the engine's division (correction step from a correctly rounded
+ * reciprocal) against CUDA's __fdiv_rn, bit for bit.  *mismatches = count;
+ * first_ab (may be NULL) receives the first mismatching (a, b). */
+tsdf_status tsdf_check_division(tsdf_engine* eng, uint64_t seed, int64_t n, int64_t* mismatches, float* first_ab);
+
 /* ---- measurement helpers --------------------------------------------- */
 /* Record CUDA events around every pipeline stage of later steps. */
 tsdf_status tsdf_set_stage_timing(tsdf_engine* eng, int on);

@@ -91,6 +91,8 @@ SIGNATURES = [
     ("tsdf_dump_blocks", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_free_list", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_block_voxels", C.c_int, [C.c_void_p, C.c_int, C.c_int32, C.c_void_p]),
+    ("tsdf_check_division", C.c_int, [C.c_void_p, C.c_uint64, C.c_int64, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_float)]),
     ("tsdf_set_stage_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("tsdf_stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int)]),

@@ -279,6 +279,9 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.hcnt, (long long)x.hchunk_cap * kVoxelsPerBlock, tr));
   TRY(dalloc(eng, &x.hvoff, (long long)(x.hchunk_cap / 2 + 1) * (kVoxelsPerBlock + 1), tr));
   TRY(dalloc(eng, &x.hbin_base, x.hchunk_cap / 2 + 1, tr));
+  TRY(dalloc(eng, &x.hfit, x.hchunk_cap / 2 + 1, tr));
+  x.hbin_cap = std::min<long long>(entry_cap, 1ll << 23);
+  TRY(dalloc(eng, &x.hbin, x.hbin_cap, tr));
   x.entry_cap = entry_cap;
   TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
   TRY(dalloc(eng, &x.digit_tot, 256, tr));
@@ -1121,6 +1124,24 @@ tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, t
   CK(cudaSetDevice(eng->device));
   CK(cudaMemcpy(out512, eng->voxels + (m.dev.heap_base + slot) * kVoxelsPerBlock, sizeof(float2) * kVoxelsPerBlock,
                 cudaMemcpyDeviceToHost));
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_check_division(tsdf_engine* eng, uint64_t seed, int64_t n, int64_t* mismatches, float* first_ab) {
+  if (!eng || !mismatches || n < 0) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  Lane& L = eng->lanes[0];
+  unsigned long long* d_m = reinterpret_cast<unsigned long long*>(L.ctx.ctr);  // lane counters as scratch
+  float* d_first = reinterpret_cast<float*>(d_m + 1);
+  CK(cudaMemsetAsync(d_m, 0, 16, L.stream));
+  launch_check_div(seed, n, d_m, d_first, eng->sm_count, L.stream);
+  CK(cudaGetLastError());
+  unsigned long long h[2] = {0, 0};
+  CK(cudaMemcpyAsync(h, d_m, 16, cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  *mismatches = (int64_t)h[0];
+  if (first_ab) std::memcpy(first_ab, &h[1], 2 * sizeof(float));
   return TSDF_OK;
 }
 

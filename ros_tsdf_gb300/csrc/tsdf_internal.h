@@ -101,6 +101,7 @@ struct LaneCounters {
   unsigned long long q_voxels;
   unsigned long long q_update;
   unsigned long long q_pubwrite;
+  unsigned long long q_heavy;    // work queue of k_update_heavy
   long long n_new;        // new keys appended
   long long n_rank_live;  // after the rank sort (== n_new)
   long long n_rec_live;   // live routing records after the first sort pass
@@ -111,6 +112,7 @@ struct LaneCounters {
   unsigned long long bin_cursor;  // bump allocator of the heavy-segment bins
   long long n_hplanned;   // heavy segments whose bins are built by the multi-CTA passes
   long long n_hchunks;    // their 128-record chunks
+  unsigned long long hbin_cursor;  // bump allocator of hbin
   int error;              // bit flags, see ERR_*
   int pad;
 };
@@ -154,6 +156,9 @@ struct Ctx {
   int* hcnt;                     // [hchunk_cap][512] per-chunk voxel counts, then offsets
   int* hvoff;                    // [hchunk_cap/2][513] per-voxel bin offsets of a heavy segment
   unsigned long long* hbin_base; // [hchunk_cap/2] bin base of a heavy segment
+  int* hfit;                     // [hchunk_cap/2] 1 when the segment's bins fit in hbin
+  float4* hbin;                  // planned heavy bins, per update: {w d, W', RN(1/W'), w}
+  long long hbin_cap;
   int hchunk_cap;
   int max_tiles_rank;
   int max_tiles_rec;
@@ -199,6 +204,8 @@ void launch_map_rehash(const Ctx& c, int map, int bucket_size, long long heap_ba
                        long long hash_base, long long hash_entries, unsigned hash_mask, int* d_used, int* d_err,
                        cudaStream_t s);
 void launch_flush(void* buf, long long bytes, int value, cudaStream_t s);
+void launch_check_div(unsigned long long seed, long long n, unsigned long long* mism, float* first, int sm_count,
+                      cudaStream_t s);
 
 // Block enumeration of one scan (tsdf_blocks.cu).
 long long eb_scratch_bytes(long long max_inc, long long* set_cap_out);

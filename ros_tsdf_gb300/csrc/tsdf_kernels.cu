@@ -241,6 +241,40 @@ __device__ __forceinline__ float distance_update(float x, float y, float z, floa
   return mag;
 }
 
+// True when |x| is within 2^-60 .. 2^60 (biased exponent 67..187), tested on
+// the exponent bits with integer compares.
+__device__ __forceinline__ bool markstein_range(float x) {
+  const unsigned ex = (__float_as_uint(x) >> 23) & 0xFFu;
+  return (ex >= 67u) & (ex <= 187u);
+}
+
+// a / b rounded to nearest even, given y = RN(1/b).  Markstein's correction
+// step: q = RN(a*y) is within one ulp of a/b, r = a - b*q is exact with an
+// fma, and RN(q + r*y) is the correctly rounded quotient (P. W. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed., 2018, sec. 4.7).  The theorem needs
+// normal operands and no underflow or overflow: zeros, tiny, huge and
+// non-finite operands take __fdiv_rn.  y depends only on the divisor, so in an
+// update chain it is computed off the critical path.
+__device__ __forceinline__ float div_rn_recip(float a, float b, float y) {
+  if (!(markstein_range(a) & markstein_range(b))) return __fdiv_rn(a, b);
+  const float q = __fmul_rn(a, y);
+  const float r = __fmaf_rn(-b, q, a);
+  return __fmaf_rn(r, y, q);
+}
+
+// getWeightUpdate + the update rule (tsdf_handler.cu:579-581, :648-654):
+//   w = 1 / (|d| + 1);  W' = W + w;  sdf = (W sdf + w d) / W';  W = min(W', max)
+// with IEEE round-to-nearest quotients, as in the float reference.
+__device__ __forceinline__ void update_voxel(float* sdf, float* w, float d, float maxw) {
+  const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
+  const float wd = fmul(wt, d);
+  const float nw = fadd(*w, wt);
+  *sdf = fdiv(fadd(fmul(*w, *sdf), wd), nw);
+  *w = fminf(nw, maxw);
+}
+
 __device__ __forceinline__ int find_item(const long long* pb, int n, long long g) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
@@ -939,6 +973,19 @@ __global__ void k_seg_classify(Ctx c) {
   }
 }
 
+__device__ __forceinline__ int find_item_global(const ItemDev* items, int n, long long g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (items[mid].point_base <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+
 // Heavy segments: a multi-CTA counting sort of their updates into per-voxel
 // bins, ordered by point index.  plan -> per-chunk voxel counts -> per-voxel
 // scan over chunks -> ordered placement.  Segments whose chunks exceed the
@@ -1067,7 +1114,9 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c) {
     vo[l] = ex;
     if (l == 0) {
       vo[kVoxelsPerBlock] = tot;
-      c.hbin_base[h] = atomicAdd(&c.ctr->bin_cursor, (unsigned long long)tot);
+      const unsigned long long base = atomicAdd(&c.ctr->hbin_cursor, (unsigned long long)tot);
+      c.hbin_base[h] = base;
+      c.hfit[h] = base + (unsigned long long)tot <= (unsigned long long)c.hbin_cap ? 1 : 0;
     }
     __syncthreads();
   }
@@ -1101,14 +1150,21 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
     const int* hc = c.hcnt + gc * kVoxelsPerBlock;
     const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
     const unsigned long long base = c.hbin_base[h];
-    const bool fits = base + (unsigned long long)vo[kVoxelsPerBlock] <= (unsigned long long)c.entry_cap;
+    const bool fits = c.hfit[h] != 0;
+    const int item = find_item_global(c.items, c.hdr->n_items, (long long)((rv[b0] >> 5) / (unsigned)c.hdr->vox_stride));
+    const float maxw = c.maps[c.items[item].map].maxw;
     for (int k = 0; k < ne && fits; ++k) {
       const int l = s_l[t * kUpdEntries + k];
       int rank = __popc(s_mask[l][t >> 5] & lt_bits);
       for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
-      c.bin_d[base + vo[l] + hc[l] + rank] = s_d[t * kUpdEntries + k];
+      // getWeightUpdate (tsdf_handler.cu:579-581): w = 1/(|d|+1), and w d.
+      // A voxel already at max_weight stays there (min(RN(max + w), max) =
+      // max for w > 0), so its W' = RN(max + w) and 1/W' are known now.
+      const float d = s_d[t * kUpdEntries + k];
+      const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
+      const float nw = fadd(maxw, wt);
+      c.hbin[base + vo[l] + hc[l] + rank] = make_float4(fmul(wt, d), nw, __frcp_rn(nw), wt);
     }
-    if (!fits && t == 0) set_error(c.ctr, ERR_CAPACITY);
     __syncthreads();
   }
 }
@@ -1130,43 +1186,69 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
 // with its loads issued ahead.  The chain of the most-updated voxel is the
 // critical path either way; the passes remove the per-chunk barriers from it.
 
-__device__ __forceinline__ int find_item_global(const ItemDev* items, int n, long long g) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (items[mid].point_base <= g)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ float apply_chain(float* sdf_io, float w, const float* d, int n, float maxw) {
-  // getWeightUpdate + update rule (tsdf_handler.cu:579-581, :648-654), in order
   float sdf = *sdf_io;
   int a = 0;
   for (; a + 4 <= n; a += 4) {
     const float d0 = d[a], d1 = d[a + 1], d2 = d[a + 2], d3 = d[a + 3];
-    const float dd[4] = {d0, d1, d2, d3};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const float wt = fdiv(1.0f, fadd(fabsf(dd[q]), 1.0f));
-      const float wd = fmul(wt, dd[q]);
-      const float nw = fadd(w, wt);
-      sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
-      w = fminf(nw, maxw);
-    }
+    update_voxel(&sdf, &w, d0, maxw);
+    update_voxel(&sdf, &w, d1, maxw);
+    update_voxel(&sdf, &w, d2, maxw);
+    update_voxel(&sdf, &w, d3, maxw);
   }
-  for (; a < n; ++a) {
-    const float wt = fdiv(1.0f, fadd(fabsf(d[a]), 1.0f));
-    const float wd = fmul(wt, d[a]);
-    const float nw = fadd(w, wt);
-    sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
-    w = fminf(nw, maxw);
-  }
+  for (; a < n; ++a) update_voxel(&sdf, &w, d[a], maxw);
   *sdf_io = sdf;
   return w;
+}
+
+constexpr int kHotChain = 128;
+
+// One update of a voxel at max_weight with precomputed x = {w d, W', RN(1/W')}:
+// sdf = RN(RN(RN(max sdf) + w d) / W') by Markstein's step.  *ok is cleared
+// when an operand leaves 2^-60..2^60, where the step is exact (zero
+// numerators are exact and pass through).
+__device__ __forceinline__ float sat_step(float sdf, const float4& x, float maxw, bool* ok) {
+  const float a = fadd(fmul(maxw, sdf), x.x);
+  const float qq = __fmul_rn(a, x.z);
+  const float rr = __fmaf_rn(-x.y, qq, a);
+  const float q1 = __fmaf_rn(rr, x.z, qq);
+  *ok = *ok & ((a == 0.0f) | markstein_range(a)) & markstein_range(x.y);
+  return (a == 0.0f) ? a : q1;
+}
+
+// One voxel's chain read straight from its bins (short chains), same
+// arithmetic as the warp path below.
+__device__ __forceinline__ void chain_direct(float* sdf_io, float* w_io, const float4* bins, int b, int e,
+                                             float maxw) {
+  float sdf = *sdf_io, W = *w_io;
+  if (W == maxw) {
+    // Markstein steps only; the range flag is checked once, after the chain,
+    // so the loop body stays branch-free (exact redo if it ever fails)
+    const float s_start = sdf;
+    bool ok = true;
+    int i = b;
+    for (; i + 4 <= e; i += 4) {
+      float4 x[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x[k] = bins[i + k];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sdf = sat_step(sdf, x[k], maxw, &ok);
+    }
+    for (; i < e; ++i) sdf = sat_step(sdf, bins[i], maxw, &ok);
+    if (!ok) {
+      sdf = s_start;
+      for (int j = b; j < e; ++j) sdf = fdiv(fadd(fmul(maxw, sdf), bins[j].x), bins[j].y);
+    }
+  } else {
+    for (int i = b; i < e; ++i) {
+      const float4 x = bins[i];
+      const float nw = fadd(W, x.w);
+      sdf = fdiv(fadd(fmul(W, sdf), x.x), nw);
+      W = fminf(nw, maxw);
+    }
+  }
+  *sdf_io = sdf;
+  *w_io = W;
 }
 
 __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
@@ -1181,6 +1263,9 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
   __shared__ int s_warp[32];
   __shared__ long long s_seg;
   __shared__ unsigned long long s_base;
+  __shared__ short s_hot[kVoxelsPerBlock];
+  __shared__ int s_nhot;
+  __shared__ __align__(16) float4 s_tile[UPD_T / 32][2][32];
   const BatchHdr h = *c.hdr;
   const int t = threadIdx.x;
   const long long nseg = c.ctr->n_seg;
@@ -1276,51 +1361,92 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
         const int b = s_off[l], e = s_off[l + 1];
         if (e == b) continue;
         float sdf = s_vox[l].x, w = s_vox[l].y;
-        for (int a = b; a < e; ++a) {
-          const float d = s_d[s_bin[a]];
-          const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
-          const float wd = fmul(wt, d);
-          const float nw = fadd(w, wt);
-          sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
-          w = fminf(nw, maxw);
-        }
+        for (int a = b; a < e; ++a) update_voxel(&sdf, &w, s_d[s_bin[a]], maxw);
         s_vox[l] = make_float2(sdf, w);
         atomicOr(&s_touch[l >> 5], 1u << (l & 31));
       }
       __syncthreads();
-    } else if (q < c.ctr->n_hplanned) {
-      // ---- planned heavy segment: bins already built; each owner runs its
-      // voxels' chains with the next loads in flight
+    } else if (q < c.ctr->n_hplanned && c.hfit[q]) {
+      // ---- planned heavy segment.  Per update the bins hold {w d, W' =
+      // RN(max + w), y = RN(1/W'), w}.  A voxel at max_weight (the hot voxels
+      // of a sensor standing in an object reach it in their first scan) only
+      // needs its sdf chain, 5 dependent operations per update:
+      //   sdf = RN(RN(RN(max sdf) + w d) / W')   (div_rn_recip, Markstein)
+      // a group of 4 whose operands leave Markstein's range is recomputed with
+      // __fdiv_rn.  A voxel below max_weight runs the plain update chain.
+      // Voxels with up to kHotChain updates: one owner thread each.  Longer
+      // chains: one warp each; its 32 lanes keep four coalesced 32-entry
+      // batches in flight and stage them through shared memory while lane 0
+      // runs the chain, so the chain never waits on global memory.
       const int* vo = c.hvoff + q * (kVoxelsPerBlock + 1);
-      const float* bins = c.bin_d + c.hbin_base[q];
-      const bool fits = c.hbin_base[q] + (unsigned long long)vo[kVoxelsPerBlock] <= (unsigned long long)c.entry_cap;
-      for (int l = t; l < kVoxelsPerBlock && fits; l += UPD_T) {
+      const float4* bins = c.hbin + c.hbin_base[q];
+      if (t == 0) s_nhot = 0;
+      __syncthreads();
+      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
         const int b = vo[l], e = vo[l + 1];
         if (e == b) continue;
-        float sdf = s_vox[l].x, w = s_vox[l].y;
-        float cur[8], nxt[8];
+        n_upd += (unsigned)(e - b);
+        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+        if (e - b > kHotChain) {
+          s_hot[atomicAdd(&s_nhot, 1)] = (short)l;
+          continue;
+        }
+        float sdf = s_vox[l].x, W = s_vox[l].y;
+        chain_direct(&sdf, &W, bins, b, e, maxw);
+        s_vox[l] = make_float2(sdf, W);
+      }
+      __syncthreads();
+      const int lane = t & 31, warp = t >> 5;
+      for (int hi = warp; hi < s_nhot; hi += UPD_T / 32) {
+        const int l = s_hot[hi];
+        const int b = vo[l], e = vo[l + 1];
+        float sdf = s_vox[l].x, W = s_vox[l].y;
+        const bool sat = W == maxw;
+        const float s_start = sdf;
+        bool ok = true;
+        float4 reg[4];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) cur[k] = b + k < e ? bins[b + k] : 0.0f;
-        for (int i = b; i < e; i += 8) {
+        for (int j = 0; j < 4; ++j) {
+          const int i = b + 32 * j + lane;
+          reg[j] = i < e ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
+        }
+        int buf = 0;
+        for (int base = b; base < e; base += 32) {
+          s_tile[warp][buf][lane] = reg[0];
+          reg[0] = reg[1];
+          reg[1] = reg[2];
+          reg[2] = reg[3];
+          {
+            const int i = base + 128 + lane;
+            reg[3] = i < e ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
+          }
+          __syncwarp();
+          if (lane == 0) {
+            const int n = min(32, e - base);
+            const float4* tl = s_tile[warp][buf];
+            if (sat && n == 32) {
 #pragma unroll
-          for (int k = 0; k < 8; ++k) nxt[k] = i + 8 + k < e ? bins[i + 8 + k] : 0.0f;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            if (i + k < e) {
-              const float d = cur[k];
-              const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
-              const float wd = fmul(wt, d);
-              const float nw = fadd(w, wt);
-              sdf = fdiv(fadd(fmul(w, sdf), wd), nw);
-              w = fminf(nw, maxw);
+              for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+            } else if (sat) {
+              for (int k = 0; k < n; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+            } else {
+              for (int k = 0; k < n; ++k) {
+                const float nw = fadd(W, tl[k].w);
+                sdf = fdiv(fadd(fmul(W, sdf), tl[k].x), nw);
+                W = fminf(nw, maxw);
+              }
             }
           }
-#pragma unroll
-          for (int k = 0; k < 8; ++k) cur[k] = nxt[k];
+          buf ^= 1;
+          __syncwarp();
         }
-        n_upd += (unsigned)(e - b);
-        s_vox[l] = make_float2(sdf, w);
-        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+        if (lane == 0) {
+          if (sat && !ok) {
+            sdf = s_start;
+            for (int j = b; j < e; ++j) sdf = fdiv(fadd(fmul(maxw, sdf), bins[j].x), bins[j].y);
+          }
+          s_vox[l] = make_float2(sdf, W);
+        }
       }
       __syncthreads();
     } else {
@@ -1647,7 +1773,49 @@ __global__ void k_map_rehash(Ctx c, int G, long long heap_base, long long hw, lo
   }
 }
 
+// Self-check of the update arithmetic against CUDA's own correctly rounded
+// division: div_rn_recip(a, b, __frcp_rn(b)) == __fdiv_rn(a, b) and
+// __frcp_rn(x) == __fdiv_rn(1, x), bit for bit, on seeded pseudo-random
+// operands (SplitMix64) spread over 2^-40..2^40 plus divisors near powers of
+// two and near 1.
+__device__ __forceinline__ unsigned long long sm64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_check_div(unsigned long long seed, long long n, unsigned long long* mism, float* first) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long r0 = sm64(seed ^ (unsigned long long)i), r1 = sm64(r0);
+    const int mode = (int)(r1 >> 60) & 3;
+    const unsigned ma = (unsigned)(r0 & 0x7FFFFFu), mb = (unsigned)((r0 >> 23) & 0x7FFFFFu);
+    const int ea = 127 + (int)((r1 >> 8) % 81) - 40;
+    int eb = 127 + (int)((r1 >> 16) % 81) - 40;
+    unsigned bb = ((unsigned)eb << 23) | mb;
+    if (mode == 1) bb = ((unsigned)eb << 23) | (0x7FFFFFu - (mb & 0xFFu));  // just below a power of two
+    if (mode == 2) bb = (127u << 23) | (mb & 0x3FFu);                        // just above 1
+    const float a = __uint_as_float(((unsigned)((r1 >> 40) & 1u) << 31) | ((unsigned)ea << 23) | ma);
+    const float b = __uint_as_float(bb);
+    const float ref = __fdiv_rn(a, b);
+    const float got = div_rn_recip(a, b, __frcp_rn(b));
+    const bool bad = __float_as_uint(ref) != __float_as_uint(got) ||
+                     __float_as_uint(__frcp_rn(b)) != __float_as_uint(__fdiv_rn(1.0f, b));
+    if (bad) {
+      if (atomicAdd(mism, 1ull) == 0ull) {
+        first[0] = a;
+        first[1] = b;
+      }
+    }
+  }
+}
+
 }  // namespace
+
+void launch_check_div(unsigned long long seed, long long n, unsigned long long* mism, float* first, int sm_count,
+                      cudaStream_t s) {
+  k_check_div<<<sm_count * 8, 256, 0, s>>>(seed, n, mism, first);
+}
 
 // ----------------------------------------------------------------------------
 // stage launchers

@@ -373,3 +373,17 @@ def test_enumerate_blocks_is_fresh_map_allocation_order(built):
             assert np.array_equal(got_d, expect)
             small, _ = eng.enumerate_blocks(spec.params, xyz, org, cap=5)
             assert np.array_equal(small, expect[:5])
+
+
+def test_update_division_matches_cuda_fdiv(built):
+    """The update rule's division (Markstein correction from a correctly
+    rounded reciprocal) equals CUDA's __fdiv_rn bit for bit."""
+    import ctypes as C
+
+    from ros_tsdf_gb300 import Engine
+
+    with Engine(max_maps=1, pool_blocks=64, max_batch_points=1024) as eng:
+        mism = C.c_int64(-1)
+        first = (C.c_float * 2)()
+        eng._check(eng.lib.tsdf_check_division(eng.h, 12345, 1 << 28, C.byref(mism), first), "check_division")
+        assert mism.value == 0, f"first mismatch a={first[0]!r} b={first[1]!r}"
