@@ -808,6 +808,8 @@ tsdf_status tsdf_map_create(tsdf_engine* eng, const tsdf_params* p, int64_t heap
       !std::isfinite(p->voxel_size) || !std::isfinite(p->truncation_distance))
     return fail(eng, TSDF_ERR_INVALID_ARG, "voxel_size, truncation_distance and max_weight must be positive");
   if (heap_blocks <= 0 || heap_blocks >= (1ll << 31)) return fail(eng, TSDF_ERR_INVALID_ARG, "heap_blocks out of range");
+  if (!(p->voxel_size >= 1e-6f && p->voxel_size <= 1e6f))
+    return fail(eng, TSDF_ERR_INVALID_ARG, "voxel_size outside 1e-6 .. 1e6");
   int id = -1;
   for (int i = 0; i < (int)eng->maps.size(); ++i)
     if (!eng->maps[i].live) {
@@ -827,6 +829,9 @@ tsdf_status tsdf_map_create(tsdf_engine* eng, const tsdf_params* p, int64_t heap
   d.half_bs = d.bs / 2.0f;
   d.scale_v = 1.0f / d.vs;
   d.scale_b = 1.0f / d.bs;
+  d.rs_v = 1.0f / d.scale_v;  // IEEE division: the correctly rounded reciprocal
+  d.rs_b = 1.0f / d.scale_b;
+  d.r_vs = 1.0f / d.vs;
   const float t2 = d.T * 2.0f;
   d.vmax = (int)(std::ceil(t2 / d.vs) * 4.0f);
   d.amax = (int)(std::ceil(t2 / d.bs) * 4.0f);

@@ -34,6 +34,8 @@ struct __align__(16) HEntry {
 struct MapDev {
   float vs, T, maxw, pub_d2, gc_d2;
   float half_vs, bs, half_bs, scale_v, scale_b;
+  float rs_v, rs_b, r_vs;  // RN(1/scale_v), RN(1/scale_b), RN(1/vs): divisors' reciprocals
+  int pad2;
   int vmax, amax, rmax, margin;
   int heap_cap, live;
   long long heap_base;   // first physical slot of the map's heap range

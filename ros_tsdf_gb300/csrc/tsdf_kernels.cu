@@ -50,11 +50,26 @@ __device__ __forceinline__ float sq3(float a, float b, float c) {
   return fadd(fadd(fmul(a, a), fmul(b, b)), fmul(c, c));
 }
 
+// a / b for a per-map constant divisor b with y = RN(1/b) precomputed:
+// Markstein's correction step (q = RN(a y); r = a - b q exact by fma;
+// RN(q + r y) = RN(a / b)), exact for normal a and b without underflow or
+// overflow of the quotient.  Every use here divides a cell index (an integer
+// below 2^25 in magnitude) or an in-block offset (between vs/2 and 8 vs) by a
+// voxel or block size or its inverse, with voxel_size in 1e-6..1e6 (checked at
+// map creation), so the theorem always applies.  A zero numerator gives +0
+// where IEEE gives -0 for -0; every use adds a half cell or floors the result,
+// where the sign of zero vanishes.
+__device__ __forceinline__ float div_const(float a, float b, float y) {
+  const float q = __fmul_rn(a, y);
+  const float r = __fmaf_rn(-b, q, a);
+  return __fmaf_rn(r, y, q);
+}
+
 // getVolumeCenterFromPoint (tsdf_handler.cu:65-85): floor(x*scale)/scale + half
-__device__ __forceinline__ float cell_center(float x, float scale, float half, float* fk) {
+__device__ __forceinline__ float cell_center(float x, float scale, float ys, float half, float* fk) {
   float f = floorf(fmul(x, scale));
   *fk = f;
-  return fadd(fdiv(f, scale), half);
+  return fadd(div_const(f, scale, ys), half);
 }
 
 __device__ __forceinline__ unsigned long long pack_key(int kx, int ky, int kz) {
@@ -123,13 +138,14 @@ struct Dda {
   float tmx, tmy, tmz, tdx, tdy, tdz, stx, sty, stz;
   float ccx, ccy, ccz, fx, fy, fz;
   float ecx, ecy, ecz;
-  float vs, scale, half, eps, vpe, vme;
+  float vs, scale, ys, half, eps, vpe, vme;
   int n, cap;
   bool done, ovf;
 
-  __device__ __forceinline__ void init(const Seg& s, float vs_, float scale_, float half_, int cap_) {
+  __device__ __forceinline__ void init(const Seg& s, float vs_, float scale_, float ys_, float half_, int cap_) {
     vs = vs_;
     scale = scale_;
+    ys = ys_;
     half = half_;
     eps = fdiv(vs, 4.0f);
     vpe = fadd(vs, eps);
@@ -139,9 +155,9 @@ struct Dda {
     sty = vy > 0.0f ? vs : fmul(-1.0f, vs);
     stz = vz > 0.0f ? vs : fmul(-1.0f, vs);
     float d;
-    float scx = cell_center(s.ax, scale, half, &d);
-    float scy = cell_center(s.ay, scale, half, &d);
-    float scz = cell_center(s.az, scale, half, &d);
+    float scx = cell_center(s.ax, scale, ys, half, &d);
+    float scy = cell_center(s.ay, scale, ys, half, &d);
+    float scz = cell_center(s.az, scale, ys, half, &d);
     tmx = fabsf(vx < 0.0f ? fdiv(fsub(fsub(scx, half), s.ax), vx) : fdiv(fsub(fadd(scx, half), s.ax), vx));
     tmy = fabsf(vy < 0.0f ? fdiv(fsub(fsub(scy, half), s.ay), vy) : fdiv(fsub(fadd(scy, half), s.ay), vy));
     tmz = fabsf(vz < 0.0f ? fdiv(fsub(fsub(scz, half), s.az), vz) : fdiv(fsub(fadd(scz, half), s.az), vz));
@@ -149,12 +165,12 @@ struct Dda {
     tdy = fabsf(fdiv(vs, vy));
     tdz = fabsf(fdiv(vs, vz));
     cx = s.ax, cy = s.ay, cz = s.az;
-    ccx = cell_center(cx, scale, half, &fx);
-    ccy = cell_center(cy, scale, half, &fy);
-    ccz = cell_center(cz, scale, half, &fz);
-    ecx = cell_center(s.bx, scale, half, &d);
-    ecy = cell_center(s.by, scale, half, &d);
-    ecz = cell_center(s.bz, scale, half, &d);
+    ccx = cell_center(cx, scale, ys, half, &fx);
+    ccy = cell_center(cy, scale, ys, half, &fy);
+    ccz = cell_center(cz, scale, ys, half, &fz);
+    ecx = cell_center(s.bx, scale, ys, half, &d);
+    ecy = cell_center(s.by, scale, ys, half, &d);
+    ecz = cell_center(s.bz, scale, ys, half, &d);
     n = 0;
     cap = cap_;
     done = false;
@@ -221,9 +237,9 @@ struct Dda {
       }
     }
     float px = ccx, py = ccy, pz = ccz;
-    ccx = cell_center(cx, scale, half, &fx);
-    ccy = cell_center(cy, scale, half, &fy);
-    ccz = cell_center(cz, scale, half, &fz);
+    ccx = cell_center(cx, scale, ys, half, &fx);
+    ccy = cell_center(cy, scale, ys, half, &fy);
+    ccz = cell_center(cz, scale, ys, half, &fz);
     float d0 = fabsf(fsub(px, ccx)), d1 = fabsf(fsub(py, ccy)), d2 = fabsf(fsub(pz, ccz));
     if ((d0 < vme && d1 < vme && d2 < vme) || (d0 > vpe || d1 > vpe || d2 > vpe)) done = true;
     return true;
@@ -461,7 +477,7 @@ __global__ void __launch_bounds__(256) k_ray_blocks(Ctx c) {
         valid = make_segment(p[0], p[1], p[2], it.ox, it.oy, it.oz, m, &seg);
       }
       Dda dda;
-      if (valid) dda.init(seg, m.bs, m.scale_b, m.half_bs, m.amax);
+      if (valid) dda.init(seg, m.bs, m.scale_b, m.rs_b, m.half_bs, m.amax);
       HEntry* tab = c.hash + m.hash_base;
       const unsigned mask = m.hash_mask;
       unsigned inc = 0;
@@ -854,7 +870,7 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
         valid = make_segment(px, py, pz, it.ox, it.oy, it.oz, m, &seg);
       }
       Dda dda;
-      if (valid) dda.init(seg, m.vs, m.scale_v, m.half_vs, m.vmax);
+      if (valid) dda.init(seg, m.vs, m.scale_v, m.rs_v, m.half_vs, m.vmax);
       const HEntry* tab = c.hash + m.hash_base;
       const unsigned mask = m.hash_mask;
       const long long kbase = m.heap_base - h.key_lo;
@@ -889,9 +905,9 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
           run_start = j;
           run_cnt = 0;
           // block centre and bottom-left corner (tsdf_handler.cu:612-624)
-          blx = fsub(fadd(fdiv(fbx, m.scale_b), m.half_bs), m.half_bs);
-          bly = fsub(fadd(fdiv(fby, m.scale_b), m.half_bs), m.half_bs);
-          blz = fsub(fadd(fdiv(fbz, m.scale_b), m.half_bs), m.half_bs);
+          blx = fsub(fadd(div_const(fbx, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
+          bly = fsub(fadd(div_const(fby, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
+          blz = fsub(fadd(div_const(fbz, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
         }
         const bool need = newrun && run < m.rmax;
         const unsigned nm = __ballot_sync(kFull, need);
@@ -914,9 +930,9 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
             ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
           } else {
             // getLocalVoxelIndex (tsdf_handler.cu:507-512)
-            float ix = floorf(fdiv(fsub(x, blx), m.vs));
-            float iy = floorf(fdiv(fsub(y, bly), m.vs));
-            float iz = floorf(fdiv(fsub(z, blz), m.vs));
+            float ix = floorf(div_const(fsub(x, blx), m.vs, m.r_vs));
+            float iy = floorf(div_const(fsub(y, bly), m.vs, m.r_vs));
+            float iz = floorf(div_const(fsub(z, blz), m.vs, m.r_vs));
             unsigned local = kBadLocal;
             if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
               local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
@@ -1603,9 +1619,9 @@ __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
     if (key != kEmptyKey) {
       int kx, ky, kz;
       unpack_key(key, &kx, &ky, &kz);
-      float cx = fadd(fdiv((float)kx, m.scale_b), m.half_bs);
-      float cy = fadd(fdiv((float)ky, m.scale_b), m.half_bs);
-      float cz = fadd(fdiv((float)kz, m.scale_b), m.half_bs);
+      float cx = fadd(div_const((float)kx, m.scale_b, m.rs_b), m.half_bs);
+      float cy = fadd(div_const((float)ky, m.scale_b, m.rs_b), m.half_bs);
+      float cz = fadd(div_const((float)kz, m.scale_b, m.rs_b), m.half_bs);
       // withinDistanceSquared (tsdf_handler.cu:749-757): diff = lidar - block
       float d2 = sq3(fsub(it.ox, cx), fsub(it.oy, cy), fsub(it.oz, cz));
       if (d2 <= m.pub_d2) cnt = c.nnz[phys];
@@ -1643,8 +1659,9 @@ __global__ void __launch_bounds__(1024) k_item_bases(Ctx c, const int* prefix, c
   if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
 }
 
-// publish write: one warp per publishing block; voxels in ascending local
-// index (getVoxelCoordinatesFromLocalVoxelIndex, tsdf_handler.cu:520-534)
+// publish write: one warp per enumerated slot (grid-strided), the block's 4 KiB
+// loaded by the warp at once; voxels in ascending local index
+// (getVoxelCoordinatesFromLocalVoxelIndex, tsdf_handler.cu:520-534)
 __global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
   __shared__ int s_sb[kMaxItems];
   const BatchHdr h = *c.hdr;
@@ -1654,42 +1671,38 @@ __global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
   const long long n = c.ctr->n_enum;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
-  for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
-    long long e0 = base + lane;
-    int cnt = e0 < n ? c.enum_cnt[e0] : 0;
-    unsigned work = __ballot_sync(kFull, cnt > 0);
-    while (work) {
-      int src = __ffs(work) - 1;
-      work &= work - 1;
-      long long e = base + src;
-      int item = find_item_i(s_sb, h.n_items, e);
-      const ItemDev& it = c.items[item];
-      const MapDev& m = c.maps[it.map];
-      long long phys = m.heap_base + (e - s_sb[item]);
-      int kx, ky, kz;
-      unpack_key(c.slot_key[phys], &kx, &ky, &kz);
-      const float blx = fsub(fadd(fdiv((float)kx, m.scale_b), m.half_bs), m.half_bs);
-      const float bly = fsub(fadd(fdiv((float)ky, m.scale_b), m.half_bs), m.half_bs);
-      const float blz = fsub(fadd(fdiv((float)kz, m.scale_b), m.half_bs), m.half_bs);
-      long long out = (long long)c.pub_prefix[e] - c.item_i[item * II_COUNT + II_PUB_BASE];
-      const float2* vox = c.voxels + phys * kVoxelsPerBlock;
-      for (int r = 0; r < kVoxelsPerBlock / 32; ++r) {
-        const int l = r * 32 + lane;
-        float2 v = vox[l];
-        bool nzv = v.y != 0.0f;
-        unsigned bm = __ballot_sync(kFull, nzv);
-        if (nzv) {
-          long long o = out + __popc(bm & lt_mask);
-          if (o < it.out_cap) {
-            float x = (float)(l & 7), y = (float)((l >> 3) & 7), z = (float)(l >> 6);
-            it.out_pos[3 * o + 0] = fadd(fadd(fmul(x, m.vs), m.half_vs), blx);
-            it.out_pos[3 * o + 1] = fadd(fadd(fmul(y, m.vs), m.half_vs), bly);
-            it.out_pos[3 * o + 2] = fadd(fadd(fmul(z, m.vs), m.half_vs), blz);
-            it.out_data[o] = v;
-          }
+  for (long long e = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; e < n; e += nw) {
+    if (c.enum_cnt[e] == 0) continue;
+    const int item = find_item_i(s_sb, h.n_items, e);
+    const ItemDev& it = c.items[item];
+    const MapDev& m = c.maps[it.map];
+    const long long phys = m.heap_base + (e - s_sb[item]);
+    const float2* vox = c.voxels + phys * kVoxelsPerBlock;
+    float2 v[kVoxelsPerBlock / 32];
+#pragma unroll
+    for (int r = 0; r < kVoxelsPerBlock / 32; ++r) v[r] = vox[r * 32 + lane];
+    int kx, ky, kz;
+    unpack_key(c.slot_key[phys], &kx, &ky, &kz);
+    const float blx = fsub(fadd(div_const((float)kx, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
+    const float bly = fsub(fadd(div_const((float)ky, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
+    const float blz = fsub(fadd(div_const((float)kz, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
+    long long out = (long long)c.pub_prefix[e] - c.item_i[item * II_COUNT + II_PUB_BASE];
+#pragma unroll
+    for (int r = 0; r < kVoxelsPerBlock / 32; ++r) {
+      const int l = r * 32 + lane;
+      const bool nzv = v[r].y != 0.0f;
+      const unsigned bm = __ballot_sync(kFull, nzv);
+      if (nzv) {
+        const long long o = out + __popc(bm & lt_mask);
+        if (o < it.out_cap) {
+          const float x = (float)(l & 7), y = (float)((l >> 3) & 7), z = (float)(l >> 6);
+          it.out_pos[3 * o + 0] = fadd(fadd(fmul(x, m.vs), m.half_vs), blx);
+          it.out_pos[3 * o + 1] = fadd(fadd(fmul(y, m.vs), m.half_vs), bly);
+          it.out_pos[3 * o + 2] = fadd(fadd(fmul(z, m.vs), m.half_vs), blz);
+          it.out_data[o] = v[r];
         }
-        out += __popc(bm);
       }
+      out += __popc(bm);
     }
   }
 }
@@ -1799,8 +1812,16 @@ __global__ void k_check_div(unsigned long long seed, long long n, unsigned long 
     const float b = __uint_as_float(bb);
     const float ref = __fdiv_rn(a, b);
     const float got = div_rn_recip(a, b, __frcp_rn(b));
+    // constant divisors of the DDA: a cell index over scale = RN(1/vs), and an
+    // in-block offset over vs (values compared; the sign of zero is not used)
+    const float vs = __uint_as_float(((unsigned)(117 + (r1 >> 52) % 21) << 23) | (unsigned)((r0 >> 3) & 0x7FFFFFu));
+    const float sc = __fdiv_rn(1.0f, vs);
+    const float ci = (float)((long long)(r0 >> 39) - (1ll << 24));
+    const float off = __fmul_rn(vs, __fadd_rn(0.25f, __fmul_rn((float)((r1 >> 20) & 0xFFFFu), 1.0f / 8192.0f)));
+    const bool bad_const = div_const(ci, sc, __frcp_rn(sc)) != __fdiv_rn(ci, sc) ||
+                           div_const(off, vs, __frcp_rn(vs)) != __fdiv_rn(off, vs);
     const bool bad = __float_as_uint(ref) != __float_as_uint(got) ||
-                     __float_as_uint(__frcp_rn(b)) != __float_as_uint(__fdiv_rn(1.0f, b));
+                     __float_as_uint(__frcp_rn(b)) != __float_as_uint(__fdiv_rn(1.0f, b)) || bad_const;
     if (bad) {
       if (atomicAdd(mism, 1ull) == 0ull) {
         first[0] = a;
