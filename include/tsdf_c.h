@@ -90,6 +90,9 @@ typedef struct tsdf_engine_cfg {
   int lanes;                /* batches in flight at once (default 1, max 4)   */
   int no_graphs;            /* 1: launch kernels directly; 0 (default): each
                                step replays one captured CUDA graph           */
+  int hot_chains;           /* capacity of the grid-wide list of long voxel
+                               update chains per step (default 65536, even;
+                               chains beyond it run inside their block's CTA) */
 } tsdf_engine_cfg;
 
 /* Per-scan counters; the field order matches the oracle's. */

@@ -282,6 +282,8 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.hfit, x.hchunk_cap / 2 + 1, tr));
   x.hbin_cap = std::min<long long>(entry_cap, 1ll << 23);
   TRY(dalloc(eng, &x.hbin, x.hbin_cap, tr));
+  x.hot_cap = c.hot_chains;
+  TRY(dalloc(eng, &x.hot, x.hot_cap, tr));
   x.entry_cap = entry_cap;
   TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
   TRY(dalloc(eng, &x.digit_tot, 256, tr));
@@ -716,6 +718,9 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   c.ray_chunk = ((c.ray_chunk + 31) / 32) * 32;
   if (c.max_routes <= 0) c.max_routes = 16;
   if (c.lanes <= 0) c.lanes = 1;
+  if (c.hot_chains <= 0) c.hot_chains = 1 << 16;
+  if (c.hot_chains < 2 || c.hot_chains > (1 << 24)) return TSDF_ERR_INVALID_ARG;
+  c.hot_chains &= ~1;
   if (c.lanes > kMaxLanes) c.lanes = kMaxLanes;
   if (c.max_routes < 8 || c.max_routes > 64) return TSDF_ERR_INVALID_ARG;
   if (c.pool_blocks >= (1ll << 31) || c.max_batch_points * (long long)c.max_routes >= (1ll << 31) ||

@@ -103,7 +103,7 @@ struct LaneCounters {
   unsigned long long q_voxels;
   unsigned long long q_update;
   unsigned long long q_pubwrite;
-  unsigned long long q_heavy;    // work queue of k_update_heavy
+  unsigned long long q_hot;      // work queue of the hot-chain kernel
   long long n_new;        // new keys appended
   long long n_rank_live;  // after the rank sort (== n_new)
   long long n_rec_live;   // live routing records after the first sort pass
@@ -115,11 +115,23 @@ struct LaneCounters {
   long long n_hplanned;   // heavy segments whose bins are built by the multi-CTA passes
   long long n_hchunks;    // their 128-record chunks
   unsigned long long hbin_cursor;  // bump allocator of hbin
+  unsigned long long n_hot_long;   // hot chains pushed (may exceed the list's half capacity)
+  unsigned long long n_hot_short;
   int error;              // bit flags, see ERR_*
   int pad;
 };
 
 enum { ERR_HASH_FULL = 1, ERR_SPIN = 2, ERR_CAPACITY = 4 };
+
+// One voxel whose update chain in a heavy segment is long enough to run as a
+// warp of its own, grid-wide, after the segment's other voxels.
+struct HotChain {
+  unsigned long long bin;  // first of its n bins in hbin
+  int n;
+  int phys;                // physical block slot
+  int local;               // voxel index in the block
+  float maxw;
+};
 
 // Everything a kernel can reach.  Passed by value; identical for every launch
 // of one lane, so a step can be captured once as a CUDA graph.
@@ -161,6 +173,8 @@ struct Ctx {
   int* hfit;                     // [hchunk_cap/2] 1 when the segment's bins fit in hbin
   float4* hbin;                  // planned heavy bins, per update: {w d, W', RN(1/W'), w}
   long long hbin_cap;
+  HotChain* hot;                 // [hot_cap]: long chains in the first half, the rest in the second
+  long long hot_cap;
   int hchunk_cap;
   int max_tiles_rank;
   int max_tiles_rec;

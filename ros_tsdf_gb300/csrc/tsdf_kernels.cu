@@ -1008,14 +1008,11 @@ __device__ __forceinline__ int find_item_global(const ItemDev* items, int n, lon
 // scratch capacity fall back to the single-CTA passes in k_update.
 __global__ void __launch_bounds__(1024) k_heavy_plan(Ctx c) {
   __shared__ int s_warp[32];
-  __shared__ int s_stop;
   const long long nh = c.ctr->n_heavy;
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
   const long long hcap = c.hchunk_cap / 2;
   long long carry = 0, planned = 0;
-  if (threadIdx.x == 0) s_stop = 0;
-  __syncthreads();
   for (long long b = 0; b < nh; b += blockDim.x) {
     const long long h = b + threadIdx.x;
     int nch = 0;
@@ -1179,7 +1176,8 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
       const float d = s_d[t * kUpdEntries + k];
       const float wt = fdiv(1.0f, fadd(fabsf(d), 1.0f));
       const float nw = fadd(maxw, wt);
-      c.hbin[base + vo[l] + hc[l] + rank] = make_float4(fmul(wt, d), nw, __frcp_rn(nw), wt);
+      const float y = markstein_range(nw) ? __frcp_rn(nw) : __uint_as_float(0x7FC00000u);
+      c.hbin[base + vo[l] + hc[l] + rank] = make_float4(fmul(wt, d), nw, y, wt);
     }
     __syncthreads();
   }
@@ -1217,19 +1215,35 @@ __device__ __forceinline__ float apply_chain(float* sdf_io, float w, const float
   return w;
 }
 
-constexpr int kHotChain = 128;
+constexpr int kHotChain = 128;    // longer chains run as a warp each
+constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
-// One update of a voxel at max_weight with precomputed x = {w d, W', RN(1/W')}:
-// sdf = RN(RN(RN(max sdf) + w d) / W') by Markstein's step.  *ok is cleared
-// when an operand leaves 2^-60..2^60, where the step is exact (zero
-// numerators are exact and pass through).
+// One update of a voxel at max_weight with precomputed x = {w d, W', y}, where
+// y = RN(1/W') (NaN when W' is outside 2^-60..2^60): sdf = RN(RN(RN(max sdf)
+// + w d) / W') by Markstein's step, which is exact when a = RN(max sdf) + w d
+// and W' lie in 2^-60..2^60.  *ok is cleared when a leaves that range (zero
+// included: the step would lose the sign of -0); a NaN y makes the result NaN
+// and keeps it NaN.  Either way the caller redoes the chain with __fdiv_rn.
 __device__ __forceinline__ float sat_step(float sdf, const float4& x, float maxw, bool* ok) {
   const float a = fadd(fmul(maxw, sdf), x.x);
   const float qq = __fmul_rn(a, x.z);
   const float rr = __fmaf_rn(-x.y, qq, a);
-  const float q1 = __fmaf_rn(rr, x.z, qq);
-  *ok = *ok & ((a == 0.0f) | markstein_range(a)) & markstein_range(x.y);
-  return (a == 0.0f) ? a : q1;
+  *ok = *ok & markstein_range(a);
+  return __fmaf_rn(rr, x.z, qq);
+}
+
+// The reference update rule over a chain's bins, with __fdiv_rn (the exact
+// path every fast path falls back to).
+__device__ __forceinline__ void chain_exact(float* sdf_io, float* w_io, const float4* bins, int n, float maxw) {
+  float sdf = *sdf_io, W = *w_io;
+  for (int i = 0; i < n; ++i) {
+    const float4 x = bins[i];
+    const float nw = fadd(W, x.w);
+    sdf = fdiv(fadd(fmul(W, sdf), x.x), nw);
+    W = fminf(nw, maxw);
+  }
+  *sdf_io = sdf;
+  *w_io = W;
 }
 
 // One voxel's chain read straight from its bins (short chains), same
@@ -1240,7 +1254,6 @@ __device__ __forceinline__ void chain_direct(float* sdf_io, float* w_io, const f
   if (W == maxw) {
     // Markstein steps only; the range flag is checked once, after the chain,
     // so the loop body stays branch-free (exact redo if it ever fails)
-    const float s_start = sdf;
     bool ok = true;
     int i = b;
     for (; i + 4 <= e; i += 4) {
@@ -1251,20 +1264,71 @@ __device__ __forceinline__ void chain_direct(float* sdf_io, float* w_io, const f
       for (int k = 0; k < 4; ++k) sdf = sat_step(sdf, x[k], maxw, &ok);
     }
     for (; i < e; ++i) sdf = sat_step(sdf, bins[i], maxw, &ok);
-    if (!ok) {
-      sdf = s_start;
-      for (int j = b; j < e; ++j) sdf = fdiv(fadd(fmul(maxw, sdf), bins[j].x), bins[j].y);
+    if (!ok || sdf != sdf) {
+      sdf = *sdf_io;
+      chain_exact(&sdf, &W, bins + b, e - b, maxw);
     }
   } else {
-    for (int i = b; i < e; ++i) {
-      const float4 x = bins[i];
-      const float nw = fadd(W, x.w);
-      sdf = fdiv(fadd(fmul(W, sdf), x.x), nw);
-      W = fminf(nw, maxw);
-    }
+    chain_exact(&sdf, &W, bins + b, e - b, maxw);
   }
   *sdf_io = sdf;
   *w_io = W;
+}
+
+// One voxel's chain run by a warp: the 32 lanes keep four coalesced 32-bin
+// batches in flight and stage them through shared memory (tile: 2 x 32
+// float4 of this warp) while lane 0 runs the chain, so the chain never waits
+// on global memory.  Below max_weight lane 0 applies the reference rule; from
+// the batch where the voxel reaches max_weight on, the Markstein steps.  The
+// result is valid in lane 0.
+__device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* bins, int n, float maxw,
+                                             float4 (*tile)[32], int lane) {
+  const float s0 = sdf, w0 = W;
+  bool ok = true;
+  bool sat = W == maxw;
+  float4 reg[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = 32 * j + lane;
+    reg[j] = i < n ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
+  }
+  int buf = 0;
+  for (int base = 0; base < n; base += 32) {
+    tile[buf][lane] = reg[0];
+    reg[0] = reg[1];
+    reg[1] = reg[2];
+    reg[2] = reg[3];
+    {
+      const int i = base + 128 + lane;
+      reg[3] = i < n ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const int m = min(32, n - base);
+      const float4* tl = tile[buf];
+      if (sat && m == 32) {
+#pragma unroll
+        for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+      } else if (sat) {
+        for (int k = 0; k < m; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+      } else {
+        for (int k = 0; k < m; ++k) {
+          const float nw = fadd(W, tl[k].w);
+          sdf = fdiv(fadd(fmul(W, sdf), tl[k].x), nw);
+          W = fminf(nw, maxw);
+        }
+        sat = W == maxw;
+      }
+    }
+    buf ^= 1;
+    __syncwarp();
+  }
+  if (lane == 0 && (!ok || sdf != sdf)) {
+    sdf = s0;
+    W = w0;
+    chain_exact(&sdf, &W, bins, n, maxw);
+  }
+  return make_float2(sdf, W);
 }
 
 __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
@@ -1281,6 +1345,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
   __shared__ unsigned long long s_base;
   __shared__ short s_hot[kVoxelsPerBlock];
   __shared__ int s_nhot;
+  __shared__ unsigned s_gh[kVoxelsPerBlock / 32];  // voxels left to the hot-chain kernel
   __shared__ __align__(16) float4 s_tile[UPD_T / 32][2][32];
   const BatchHdr h = *c.hdr;
   const int t = threadIdx.x;
@@ -1317,7 +1382,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
     float4* sv4 = reinterpret_cast<float4*>(s_vox);
     sv4[t] = gv[t];
     sv4[t + UPD_T] = gv[t + UPD_T];
-    if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
+    if (t < kVoxelsPerBlock / 32) s_touch[t] = 0, s_gh[t] = 0;
     __syncthreads();  // the staged block and touch mask are shared by every path below
     unsigned n_upd = 0;
     if (!heavy) {
@@ -1386,16 +1451,14 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
       // ---- planned heavy segment.  Per update the bins hold {w d, W' =
       // RN(max + w), y = RN(1/W'), w}.  A voxel at max_weight (the hot voxels
       // of a sensor standing in an object reach it in their first scan) only
-      // needs its sdf chain, 5 dependent operations per update:
-      //   sdf = RN(RN(RN(max sdf) + w d) / W')   (div_rn_recip, Markstein)
-      // a group of 4 whose operands leave Markstein's range is recomputed with
-      // __fdiv_rn.  A voxel below max_weight runs the plain update chain.
-      // Voxels with up to kHotChain updates: one owner thread each.  Longer
-      // chains: one warp each; its 32 lanes keep four coalesced 32-entry
-      // batches in flight and stage them through shared memory while lane 0
-      // runs the chain, so the chain never waits on global memory.
+      // needs its sdf chain, 5 dependent operations per update (sat_step).
+      // Voxels with up to kHotChain updates: one owner thread each, here.
+      // Longer chains go to the grid-wide hot list and run one warp each in
+      // k_hot_chains, after this kernel has written the block back; only
+      // when that list is full do this CTA's warps run them.
       const int* vo = c.hvoff + q * (kVoxelsPerBlock + 1);
       const float4* bins = c.hbin + c.hbin_base[q];
+      const long long half = c.hot_cap / 2;
       if (t == 0) s_nhot = 0;
       __syncthreads();
       for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
@@ -1404,7 +1467,20 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
         n_upd += (unsigned)(e - b);
         atomicOr(&s_touch[l >> 5], 1u << (l & 31));
         if (e - b > kHotChain) {
-          s_hot[atomicAdd(&s_nhot, 1)] = (short)l;
+          const bool lng = e - b >= kLongChain;
+          const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
+          if (idx < half) {
+            HotChain hc;
+            hc.bin = c.hbin_base[q] + (unsigned long long)b;
+            hc.n = e - b;
+            hc.phys = (int)phys;
+            hc.local = l;
+            hc.maxw = maxw;
+            c.hot[(lng ? 0 : half) + idx] = hc;
+            atomicOr(&s_gh[l >> 5], 1u << (l & 31));
+          } else {
+            s_hot[atomicAdd(&s_nhot, 1)] = (short)l;
+          }
           continue;
         }
         float sdf = s_vox[l].x, W = s_vox[l].y;
@@ -1416,53 +1492,8 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
       for (int hi = warp; hi < s_nhot; hi += UPD_T / 32) {
         const int l = s_hot[hi];
         const int b = vo[l], e = vo[l + 1];
-        float sdf = s_vox[l].x, W = s_vox[l].y;
-        const bool sat = W == maxw;
-        const float s_start = sdf;
-        bool ok = true;
-        float4 reg[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int i = b + 32 * j + lane;
-          reg[j] = i < e ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
-        }
-        int buf = 0;
-        for (int base = b; base < e; base += 32) {
-          s_tile[warp][buf][lane] = reg[0];
-          reg[0] = reg[1];
-          reg[1] = reg[2];
-          reg[2] = reg[3];
-          {
-            const int i = base + 128 + lane;
-            reg[3] = i < e ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
-          }
-          __syncwarp();
-          if (lane == 0) {
-            const int n = min(32, e - base);
-            const float4* tl = s_tile[warp][buf];
-            if (sat && n == 32) {
-#pragma unroll
-              for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
-            } else if (sat) {
-              for (int k = 0; k < n; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
-            } else {
-              for (int k = 0; k < n; ++k) {
-                const float nw = fadd(W, tl[k].w);
-                sdf = fdiv(fadd(fmul(W, sdf), tl[k].x), nw);
-                W = fminf(nw, maxw);
-              }
-            }
-          }
-          buf ^= 1;
-          __syncwarp();
-        }
-        if (lane == 0) {
-          if (sat && !ok) {
-            sdf = s_start;
-            for (int j = b; j < e; ++j) sdf = fdiv(fadd(fmul(maxw, sdf), bins[j].x), bins[j].y);
-          }
-          s_vox[l] = make_float2(sdf, W);
-        }
+        const float2 r = warp_chain(s_vox[l].x, s_vox[l].y, bins + b, e - b, maxw, s_tile[warp], lane);
+        if (lane == 0) s_vox[l] = r;
       }
       __syncthreads();
     } else {
@@ -1561,8 +1592,12 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
     gv[t] = va;
     gv[t + UPD_T] = vb;
     // one reduction for the three block totals: non-zero weights, touched
-    // voxels, applied updates
-    int nz = (va.y != 0.0f) + (va.w != 0.0f) + (vb.y != 0.0f) + (vb.w != 0.0f);
+    // voxels, applied updates.  A voxel left to the hot-chain kernel counts
+    // as non-zero: every update leaves a positive weight.
+    const unsigned gl = s_gh[(2 * t) >> 5] >> ((2 * t) & 31);
+    const unsigned gh = s_gh[(2 * t + 2 * UPD_T) >> 5] >> ((2 * t + 2 * UPD_T) & 31);
+    int nz = ((va.y != 0.0f) | (gl & 1u)) + ((va.w != 0.0f) | ((gl >> 1) & 1u)) + ((vb.y != 0.0f) | (gh & 1u)) +
+             ((vb.w != 0.0f) | ((gh >> 1) & 1u));
     int touched = t < kVoxelsPerBlock / 32 ? __popc(s_touch[t]) : 0;
     int upd = (int)n_upd;
 #pragma unroll
@@ -1586,6 +1621,30 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
     }
     __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------------------
+// hot chains: one warp per chain, grid-wide, long chains dequeued first.  The
+// voxel was written back unchanged by k_update; no other update touches it.
+constexpr int HOT_T = 128;
+
+__global__ void __launch_bounds__(HOT_T) k_hot_chains(Ctx c) {
+  __shared__ __align__(16) float4 s_tile[HOT_T / 32][2][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long half = c.hot_cap / 2;
+  const long long nl = min((long long)c.ctr->n_hot_long, half);
+  const long long ns = min((long long)c.ctr->n_hot_short, half);
+  while (true) {
+    long long q = 0;
+    if (lane == 0) q = (long long)atomicAdd(&c.ctr->q_hot, 1ull);
+    q = __shfl_sync(kFull, q, 0);
+    if (q >= nl + ns) break;
+    const HotChain hc = q < nl ? c.hot[q] : c.hot[half + (q - nl)];
+    float2* v = c.voxels + (long long)hc.phys * kVoxelsPerBlock + hc.local;
+    const float2 v0 = *v;
+    const float2 r = warp_chain(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, s_tile[warp], lane);
+    if (lane == 0) *v = r;
   }
 }
 
@@ -1900,7 +1959,8 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, lc.rec_passes & 1);
-  *launches += 1;
+  k_hot_chains<<<lc.sm_count * 4, HOT_T, 0, s>>>(c);
+  *launches += 2;
 }
 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {

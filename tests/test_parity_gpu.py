@@ -118,10 +118,12 @@ def test_batched_multimap_matches_oracle(built):
 
 
 @pytest.mark.parametrize("cfg", [dict(bucket_size=4), dict(bucket_size=16), dict(ray_threads=128, ray_chunk=256),
-                                 dict(graphs=False), dict(ray_chunk=64, bucket_size=4, graphs=False)])
+                                 dict(graphs=False), dict(ray_chunk=64, bucket_size=4, graphs=False),
+                                 dict(hot_chains=2)])
 def test_engine_configs_give_identical_results(built, cfg):
-    """Tuning knobs (bucket size, CTA size, work-queue chunk, graphs) change
-    nothing in the results."""
+    """Tuning knobs (bucket size, CTA size, work-queue chunk, graphs, the
+    hot-chain list, whose overflow runs long chains inside their block's CTA)
+    change nothing in the results."""
     from ros_tsdf_gb300 import Engine, workloads as W
 
     specs = _mixed_specs()[:4]
