@@ -284,6 +284,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.hbin, x.hbin_cap, tr));
   x.hot_cap = c.hot_chains;
   TRY(dalloc(eng, &x.hot, x.hot_cap, tr));
+  TRY(dalloc(eng, &x.hmask, (long long)(x.hchunk_cap / 2 + 1) * (kVoxelsPerBlock / 32), tr));
   x.entry_cap = entry_cap;
   TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
   TRY(dalloc(eng, &x.digit_tot, 256, tr));
@@ -733,6 +734,7 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess) return TSDF_ERR_CUDA;
   eng->sm_count = sms;
+  if (kernels_init() != cudaSuccess) return TSDF_ERR_CUDA;
   // global state
   eng->hash_pool = c.pool_blocks * 4 + 4096;
   if (dalloc(eng, &eng->voxels, c.pool_blocks * kVoxelsPerBlock, nullptr) != TSDF_OK ||

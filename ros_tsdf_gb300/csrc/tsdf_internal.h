@@ -174,6 +174,7 @@ struct Ctx {
   float4* hbin;                  // planned heavy bins, per update: {w d, W', RN(1/W'), w}
   long long hbin_cap;
   HotChain* hot;                 // [hot_cap]: long chains in the first half, the rest in the second
+  unsigned* hmask;               // [hchunk_cap/2][16] voxels of a planned heavy segment on the hot list
   long long hot_cap;
   int hchunk_cap;
   int max_tiles_rank;
@@ -202,6 +203,7 @@ struct LaunchCfg {
   int rec_passes;
 };
 
+cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice
 void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);

@@ -975,6 +975,8 @@ struct SegHeadOut {
 
 // segments with more records than one update chunk go to the heavy list
 constexpr int UPD_T = 128;
+constexpr int kHotChain = 128;    // longer voxel chains of a heavy segment run as a warp each
+constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
 __global__ void k_seg_classify(Ctx c) {
   const long long nseg = c.ctr->n_seg;
@@ -1106,21 +1108,40 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_count(Ctx c, int rec_sel) {
 
 // One CTA of 512 threads per planned heavy segment: per voxel, exclusive scan
 // of its counts over the segment's chunks; per-voxel bin offsets; bin base.
-__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c) {
+// A voxel with more than kHotChain updates goes on the grid-wide hot list
+// (long chains in the first half) and is marked in the segment's hot mask;
+// when its half of the list is full, k_heavy_update runs it instead.
+__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c, int rec_sel) {
   __shared__ int s_warp[32];
+  __shared__ unsigned long long s_base;
+  __shared__ int s_fit;
+  __shared__ unsigned s_hm[kVoxelsPerBlock / 32];
   const int l = threadIdx.x;
   const int np = (int)c.ctr->n_hplanned;
   const long long nch = c.ctr->n_hchunks;
+  const long long half = c.hot_cap / 2;
   for (int h = blockIdx.x; h < np; h += gridDim.x) {
     const long long c0 = c.hchunk_base[h];
     const long long c1 = (h + 1 < np) ? c.hchunk_base[h + 1] : nch;
     int run = 0;
-    for (long long gc = c0; gc < c1; ++gc) {
+    long long gc = c0;
+    for (; gc + 8 <= c1; gc += 8) {  // eight chunk counts in flight
+      int v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = c.hcnt[(gc + k) * kVoxelsPerBlock + l];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        c.hcnt[(gc + k) * kVoxelsPerBlock + l] = run;
+        run += v[k];
+      }
+    }
+    for (; gc < c1; ++gc) {
       int* p = c.hcnt + gc * kVoxelsPerBlock + l;
       const int v = *p;
       *p = run;
       run += v;
     }
+    if (l < kVoxelsPerBlock / 32) s_hm[l] = 0;
     int tot;
     const int ex = block_excl_scan(run, s_warp, &tot);
     int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
@@ -1128,9 +1149,32 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c) {
     if (l == 0) {
       vo[kVoxelsPerBlock] = tot;
       const unsigned long long base = atomicAdd(&c.ctr->hbin_cursor, (unsigned long long)tot);
+      const int fit = base + (unsigned long long)tot <= (unsigned long long)c.hbin_cap ? 1 : 0;
       c.hbin_base[h] = base;
-      c.hfit[h] = base + (unsigned long long)tot <= (unsigned long long)c.hbin_cap ? 1 : 0;
+      c.hfit[h] = fit;
+      s_base = base;
+      s_fit = fit;
     }
+    __syncthreads();
+    if (s_fit && run > kHotChain) {
+      const bool lng = run >= kLongChain;
+      const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
+      if (idx < half) {
+        const long long b0 = c.seg_start[c.heavy[h]];
+        const unsigned v0 = c.rec_val[rec_sel][b0];
+        const int item = find_item_global(c.items, c.hdr->n_items, (long long)((v0 >> 5) / (unsigned)c.hdr->vox_stride));
+        HotChain hc;
+        hc.bin = s_base + (unsigned long long)ex;
+        hc.n = run;
+        hc.phys = (int)(c.hdr->key_lo + c.rec_key[rec_sel][b0]);
+        hc.local = l;
+        hc.maxw = c.maps[c.items[item].map].maxw;
+        c.hot[(lng ? 0 : half) + idx] = hc;
+        atomicOr(&s_hm[l >> 5], 1u << (l & 31));
+      }
+    }
+    __syncthreads();
+    if (l < kVoxelsPerBlock / 32) c.hmask[(long long)h * (kVoxelsPerBlock / 32) + l] = s_hm[l];
     __syncthreads();
   }
 }
@@ -1193,12 +1237,12 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
 // them sequentially: the reference's update rule, in a fixed order.
 //
 // Segments longer than one chunk (a block that many points update, e.g. the
-// blocks around a sensor standing inside an object) are taken first and
-// handled in three passes: per-voxel counts over all records, ordered
-// placement of every update into per-voxel bins in global scratch (mask
-// popcount + running per-voxel cursor), then one sequential chain per voxel
-// with its loads issued ahead.  The chain of the most-updated voxel is the
-// critical path either way; the passes remove the per-chunk barriers from it.
+// blocks around a sensor standing inside an object) are binned per voxel by
+// the multi-CTA counting sort of the routing stage and updated by
+// k_heavy_update and the hot-chain warps.  Only heavy segments beyond that sort's
+// capacity stay here, in three passes: per-voxel counts over all records,
+// ordered placement of every update into per-voxel bins in global scratch
+// (mask popcount + running per-voxel cursor), then one chain per voxel.
 
 __device__ __forceinline__ float apply_chain(float* sdf_io, float w, const float* d, int n, float maxw) {
   float sdf = *sdf_io;
@@ -1214,9 +1258,6 @@ __device__ __forceinline__ float apply_chain(float* sdf_io, float w, const float
   *sdf_io = sdf;
   return w;
 }
-
-constexpr int kHotChain = 128;    // longer chains run as a warp each
-constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
 // One update of a voxel at max_weight with precomputed x = {w d, W', y}, where
 // y = RN(1/W') (NaN when W' is outside 2^-60..2^60): sdf = RN(RN(RN(max sdf)
@@ -1246,41 +1287,16 @@ __device__ __forceinline__ void chain_exact(float* sdf_io, float* w_io, const fl
   *w_io = W;
 }
 
-// One voxel's chain read straight from its bins (short chains), same
-// arithmetic as the warp path below.
-__device__ __forceinline__ void chain_direct(float* sdf_io, float* w_io, const float4* bins, int b, int e,
-                                             float maxw) {
-  float sdf = *sdf_io, W = *w_io;
-  if (W == maxw) {
-    // Markstein steps only; the range flag is checked once, after the chain,
-    // so the loop body stays branch-free (exact redo if it ever fails)
-    bool ok = true;
-    int i = b;
-    for (; i + 4 <= e; i += 4) {
-      float4 x[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) x[k] = bins[i + k];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) sdf = sat_step(sdf, x[k], maxw, &ok);
-    }
-    for (; i < e; ++i) sdf = sat_step(sdf, bins[i], maxw, &ok);
-    if (!ok || sdf != sdf) {
-      sdf = *sdf_io;
-      chain_exact(&sdf, &W, bins + b, e - b, maxw);
-    }
-  } else {
-    chain_exact(&sdf, &W, bins + b, e - b, maxw);
-  }
-  *sdf_io = sdf;
-  *w_io = W;
-}
-
 // One voxel's chain run by a warp: the 32 lanes keep four coalesced 32-bin
 // batches in flight and stage them through shared memory (tile: 2 x 32
 // float4 of this warp) while lane 0 runs the chain, so the chain never waits
-// on global memory.  Below max_weight lane 0 applies the reference rule; from
-// the batch where the voxel reaches max_weight on, the Markstein steps.  The
-// result is valid in lane 0.
+// on global memory.  A batch of a voxel below max_weight runs in three
+// steps: lane 0 runs the weight chain W' = RN(W + w), W = min(W', max)
+// (independent of the sdf), every lane takes one reciprocal RN(1/W'), and
+// lane 0 runs the sdf chain with Markstein steps.  From the batch where the
+// voxel is at max_weight on, the precomputed saturated bins (sat_step).  The
+// range flag or a NaN sends the whole chain to the exact redo.  The result is
+// valid in lane 0.
 __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* bins, int n, float maxw,
                                              float4 (*tile)[32], int lane) {
   const float s0 = sdf, w0 = W;
@@ -1303,19 +1319,41 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
       reg[3] = i < n ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
     }
     __syncwarp();
-    if (lane == 0) {
-      const int m = min(32, n - base);
-      const float4* tl = tile[buf];
-      if (sat && m == 32) {
+    const int m = min(32, n - base);
+    float4* tl = tile[buf];
+    if (__shfl_sync(kFull, sat, 0)) {
+      if (lane == 0) {
+        if (m == 32) {
 #pragma unroll
-        for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
-      } else if (sat) {
-        for (int k = 0; k < m; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
-      } else {
+          for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+        } else {
+          for (int k = 0; k < m; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+        }
+      }
+    } else {
+      if (lane == 0) {
+        // tile entry becomes {w d, W', RN(1/W'), W before the update}
         for (int k = 0; k < m; ++k) {
           const float nw = fadd(W, tl[k].w);
-          sdf = fdiv(fadd(fmul(W, sdf), tl[k].x), nw);
+          tl[k].y = nw;
+          tl[k].w = W;
           W = fminf(nw, maxw);
+        }
+      }
+      __syncwarp();
+      if (lane < m) {
+        const float nw = tl[lane].y;
+        tl[lane].z = markstein_range(nw) ? __frcp_rn(nw) : __uint_as_float(0x7FC00000u);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        for (int k = 0; k < m; ++k) {
+          const float4 x = tl[k];
+          const float a = fadd(fmul(x.w, sdf), x.x);
+          const float qq = __fmul_rn(a, x.z);
+          const float rr = __fmaf_rn(-x.y, qq, a);
+          ok = ok & markstein_range(a);
+          sdf = __fmaf_rn(rr, x.z, qq);
         }
         sat = W == maxw;
       }
@@ -1331,9 +1369,32 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
   return make_float2(sdf, W);
 }
 
-__global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
+// Hot chains (voxels of binned heavy segments with more than kHotChain
+// updates, listed by k_heavy_scan): one warp per chain, long chains dequeued
+// first.  The voxel is on no other update path this step.
+__device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32], int lane) {
+  const long long half = c.hot_cap / 2;
+  const long long nl = min((long long)c.ctr->n_hot_long, half);
+  const long long ns = min((long long)c.ctr->n_hot_short, half);
+  while (true) {
+    long long q = 0;
+    if (lane == 0) q = (long long)atomicAdd(&c.ctr->q_hot, 1ull);
+    q = __shfl_sync(kFull, q, 0);
+    if (q >= nl + ns) break;
+    const HotChain hc = q < nl ? c.hot[q] : c.hot[half + (q - nl)];
+    float2* v = c.voxels + (long long)hc.phys * kVoxelsPerBlock + hc.local;
+    const float2 v0 = *v;
+    const float2 r = warp_chain(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, tile, lane);
+    if (lane == 0) *v = r;
+  }
+}
+
+// The first hot_ctas CTAs (one per SM: blocks are dispatched in index order)
+// start with the hot chains, so the longest serial chains run from the start
+// of the kernel, beside the segment work of the other CTAs.
+__global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ctas) {
   __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
-  __shared__ float s_d[UPD_T * kUpdEntries];
+  __shared__ __align__(16) float s_d[UPD_T * kUpdEntries];
   __shared__ unsigned short s_l[UPD_T * kUpdEntries];
   __shared__ unsigned short s_bin[UPD_T * kUpdEntries];
   __shared__ unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];
@@ -1343,10 +1404,6 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
   __shared__ int s_warp[32];
   __shared__ long long s_seg;
   __shared__ unsigned long long s_base;
-  __shared__ short s_hot[kVoxelsPerBlock];
-  __shared__ int s_nhot;
-  __shared__ unsigned s_gh[kVoxelsPerBlock / 32];  // voxels left to the hot-chain kernel
-  __shared__ __align__(16) float4 s_tile[UPD_T / 32][2][32];
   const BatchHdr h = *c.hdr;
   const int t = threadIdx.x;
   const long long nseg = c.ctr->n_seg;
@@ -1355,6 +1412,11 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
   const unsigned* rk = c.rec_key[rec_sel];
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned lt_bits = (1u << (t & 31)) - 1u;
+  if ((int)blockIdx.x < hot_ctas) {
+    float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(s_d) + 2 * (t >> 5);
+    run_hot_chains(c, tile, t & 31);
+    __syncthreads();
+  }
   while (true) {
     if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
     __syncthreads();
@@ -1364,6 +1426,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
     long long sj;
     bool heavy;
     if (q < nheavy) {
+      if (q < c.ctr->n_hplanned && c.hfit[q]) continue;  // k_heavy_update's
       sj = c.heavy[q];
       heavy = true;
     } else {
@@ -1382,7 +1445,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
     float4* sv4 = reinterpret_cast<float4*>(s_vox);
     sv4[t] = gv[t];
     sv4[t + UPD_T] = gv[t + UPD_T];
-    if (t < kVoxelsPerBlock / 32) s_touch[t] = 0, s_gh[t] = 0;
+    if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
     __syncthreads();  // the staged block and touch mask are shared by every path below
     unsigned n_upd = 0;
     if (!heavy) {
@@ -1445,55 +1508,6 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
         for (int a = b; a < e; ++a) update_voxel(&sdf, &w, s_d[s_bin[a]], maxw);
         s_vox[l] = make_float2(sdf, w);
         atomicOr(&s_touch[l >> 5], 1u << (l & 31));
-      }
-      __syncthreads();
-    } else if (q < c.ctr->n_hplanned && c.hfit[q]) {
-      // ---- planned heavy segment.  Per update the bins hold {w d, W' =
-      // RN(max + w), y = RN(1/W'), w}.  A voxel at max_weight (the hot voxels
-      // of a sensor standing in an object reach it in their first scan) only
-      // needs its sdf chain, 5 dependent operations per update (sat_step).
-      // Voxels with up to kHotChain updates: one owner thread each, here.
-      // Longer chains go to the grid-wide hot list and run one warp each in
-      // k_hot_chains, after this kernel has written the block back; only
-      // when that list is full do this CTA's warps run them.
-      const int* vo = c.hvoff + q * (kVoxelsPerBlock + 1);
-      const float4* bins = c.hbin + c.hbin_base[q];
-      const long long half = c.hot_cap / 2;
-      if (t == 0) s_nhot = 0;
-      __syncthreads();
-      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-        const int b = vo[l], e = vo[l + 1];
-        if (e == b) continue;
-        n_upd += (unsigned)(e - b);
-        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
-        if (e - b > kHotChain) {
-          const bool lng = e - b >= kLongChain;
-          const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
-          if (idx < half) {
-            HotChain hc;
-            hc.bin = c.hbin_base[q] + (unsigned long long)b;
-            hc.n = e - b;
-            hc.phys = (int)phys;
-            hc.local = l;
-            hc.maxw = maxw;
-            c.hot[(lng ? 0 : half) + idx] = hc;
-            atomicOr(&s_gh[l >> 5], 1u << (l & 31));
-          } else {
-            s_hot[atomicAdd(&s_nhot, 1)] = (short)l;
-          }
-          continue;
-        }
-        float sdf = s_vox[l].x, W = s_vox[l].y;
-        chain_direct(&sdf, &W, bins, b, e, maxw);
-        s_vox[l] = make_float2(sdf, W);
-      }
-      __syncthreads();
-      const int lane = t & 31, warp = t >> 5;
-      for (int hi = warp; hi < s_nhot; hi += UPD_T / 32) {
-        const int l = s_hot[hi];
-        const int b = vo[l], e = vo[l + 1];
-        const float2 r = warp_chain(s_vox[l].x, s_vox[l].y, bins + b, e - b, maxw, s_tile[warp], lane);
-        if (lane == 0) s_vox[l] = r;
       }
       __syncthreads();
     } else {
@@ -1592,12 +1606,8 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
     gv[t] = va;
     gv[t + UPD_T] = vb;
     // one reduction for the three block totals: non-zero weights, touched
-    // voxels, applied updates.  A voxel left to the hot-chain kernel counts
-    // as non-zero: every update leaves a positive weight.
-    const unsigned gl = s_gh[(2 * t) >> 5] >> ((2 * t) & 31);
-    const unsigned gh = s_gh[(2 * t + 2 * UPD_T) >> 5] >> ((2 * t + 2 * UPD_T) & 31);
-    int nz = ((va.y != 0.0f) | (gl & 1u)) + ((va.w != 0.0f) | ((gl >> 1) & 1u)) + ((vb.y != 0.0f) | (gh & 1u)) +
-             ((vb.w != 0.0f) | ((gh >> 1) & 1u));
+    // voxels, applied updates
+    int nz = (va.y != 0.0f) + (va.w != 0.0f) + (vb.y != 0.0f) + (vb.w != 0.0f);
     int touched = t < kVoxelsPerBlock / 32 ? __popc(s_touch[t]) : 0;
     int upd = (int)n_upd;
 #pragma unroll
@@ -1625,26 +1635,137 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel) {
 }
 
 // ----------------------------------------------------------------------------
-// hot chains: one warp per chain, grid-wide, long chains dequeued first.  The
-// voxel was written back unchanged by k_update; no other update touches it.
-constexpr int HOT_T = 128;
+// heavy segments binned by the counting sort: one CTA of 512 threads per
+// segment, one thread per voxel, every voxel's chain (up to kHotChain
+// updates) in its own lane.  The chains of a warp's 32 voxels are staged
+// through shared memory kRound bins at a time: eight lanes load eight
+// consecutive bins of one chain with one coalesced instruction, a round ahead
+// of the steps, and every lane then reads its own chain from the tile.  While
+// every active lane of the warp is at max_weight a round takes the saturated
+// Markstein steps (sat_step); otherwise each step runs the weight chain and
+// one reciprocal RN(1/W') in the lane, then the same Markstein step.  A range
+// flag or NaN makes the lane redo its chain exactly.  Voxels on the hot list
+// are left to the hot-chain warps of k_update; longer chains that did not fit
+// on the list run here, a
+// warp each (warp_chain), after the lanes.
+constexpr int HU_T = kVoxelsPerBlock;
+constexpr int kRound = 8;
+constexpr int kHuSmem = (HU_T / 32) * kRound * 33 * (int)sizeof(float4);
 
-__global__ void __launch_bounds__(HOT_T) k_hot_chains(Ctx c) {
-  __shared__ __align__(16) float4 s_tile[HOT_T / 32][2][32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long half = c.hot_cap / 2;
-  const long long nl = min((long long)c.ctr->n_hot_long, half);
-  const long long ns = min((long long)c.ctr->n_hot_short, half);
-  while (true) {
-    long long q = 0;
-    if (lane == 0) q = (long long)atomicAdd(&c.ctr->q_hot, 1ull);
-    q = __shfl_sync(kFull, q, 0);
-    if (q >= nl + ns) break;
-    const HotChain hc = q < nl ? c.hot[q] : c.hot[half + (q - nl)];
-    float2* v = c.voxels + (long long)hc.phys * kVoxelsPerBlock + hc.local;
-    const float2 v0 = *v;
-    const float2 r = warp_chain(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, s_tile[warp], lane);
-    if (lane == 0) *v = r;
+__global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c, int rec_sel) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  __shared__ short s_fb[kVoxelsPerBlock];
+  __shared__ int s_nfb;
+  __shared__ int s_red[3];
+  const int l = threadIdx.x, lane = l & 31, warp = l >> 5;
+  float4 (*tile)[33] = reinterpret_cast<float4 (*)[33]>(s_dyn + warp * kRound * 33);
+  const int np = (int)c.ctr->n_hplanned;
+  const BatchHdr hd = *c.hdr;
+  const unsigned* rk = c.rec_key[rec_sel];
+  const unsigned* rv = c.rec_val[rec_sel];
+  for (int h = blockIdx.x; h < np; h += gridDim.x) {
+    if (!c.hfit[h]) continue;  // k_update's fallback passes take it
+    const long long b0 = c.seg_start[c.heavy[h]];
+    const long long phys = hd.key_lo + rk[b0];
+    const int item = find_item_global(c.items, hd.n_items, (long long)((rv[b0] >> 5) / (unsigned)hd.vox_stride));
+    const float maxw = c.maps[c.items[item].map].maxw;
+    const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
+    const float4* bins = c.hbin + c.hbin_base[h];
+    const bool hot = (c.hmask[(long long)h * (kVoxelsPerBlock / 32) + (l >> 5)] >> (l & 31)) & 1u;
+    const int b = vo[l];
+    const int nfull = vo[l + 1] - b;
+    float2* gvox = c.voxels + phys * kVoxelsPerBlock + l;
+    const float2 v0 = *gvox;
+    if (l == 0) s_nfb = 0, s_red[0] = 0, s_red[1] = 0, s_red[2] = 0;
+    __syncthreads();
+    int n = nfull <= kHotChain ? nfull : 0;
+    if (nfull > kHotChain && !hot) s_fb[atomicAdd(&s_nfb, 1)] = (short)l;
+    // load slots of this lane: chain 4i + lane/8, bin lane%8 of the round
+    const int el = lane & 7;
+    int lb[4 * 2], ln[4 * 2];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int ch = 4 * i + (lane >> 3);
+      lb[i] = __shfl_sync(kFull, b, ch);
+      ln[i] = __shfl_sync(kFull, n, ch);
+    }
+    const int rounds = __reduce_max_sync(kFull, (unsigned)((n + kRound - 1) / kRound));
+    float sdf = v0.x, W = v0.y;
+    bool ok = true;
+    float4 nx[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) nx[i] = el < ln[i] ? bins[lb[i] + el] : make_float4(0.f, 1.f, 1.f, 0.f);
+    for (int r = 0; r < rounds; ++r) {
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < 8; ++i) tile[el][4 * i + (lane >> 3)] = nx[i];
+      if (r + 1 < rounds) {
+        const int k = (r + 1) * kRound + el;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) nx[i] = k < ln[i] ? bins[lb[i] + k] : make_float4(0.f, 1.f, 1.f, 0.f);
+      }
+      __syncwarp();
+      const int m = min(kRound, n - r * kRound);  // steps of this lane in the round (may be <= 0)
+      if (__all_sync(kFull, m <= 0 || W == maxw)) {
+#pragma unroll
+        for (int k = 0; k < kRound; ++k) {
+          bool okk = ok;
+          const float t2 = sat_step(sdf, tile[k][lane], maxw, &okk);
+          if (k < m) sdf = t2, ok = okk;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kRound; ++k) {
+          if (k < m) {
+            const float4 x = tile[k][lane];
+            const float nw = fadd(W, x.w);
+            const float y = __frcp_rn(nw);
+            const float a = fadd(fmul(W, sdf), x.x);
+            const float qq = __fmul_rn(a, y);
+            const float rr = __fmaf_rn(-nw, qq, a);
+            ok = ok & markstein_range(a) & markstein_range(nw);
+            sdf = __fmaf_rn(rr, y, qq);
+            W = fminf(nw, maxw);
+          }
+        }
+      }
+    }
+    if (n > 0) {
+      if (!ok || sdf != sdf) {
+        sdf = v0.x;
+        W = v0.y;
+        chain_exact(&sdf, &W, bins + b, n, maxw);
+      }
+      *gvox = make_float2(sdf, W);
+    }
+    __syncthreads();
+    // chains beyond kHotChain that the hot list had no room for: a warp each
+    for (int f = warp; f < s_nfb; f += HU_T / 32) {
+      const int lf = s_fb[f];
+      float2* g = c.voxels + phys * kVoxelsPerBlock + lf;
+      const float2 vf = *g;
+      float4 (*wt)[32] = reinterpret_cast<float4 (*)[32]>(s_dyn + warp * kRound * 33);
+      const float2 rf = warp_chain(vf.x, vf.y, bins + vo[lf], vo[lf + 1] - vo[lf], maxw, wt, lane);
+      if (lane == 0) *g = rf;
+    }
+    // block totals: non-zero weights (a voxel with an update has a positive
+    // weight), touched voxels, applied updates
+    const unsigned nz = __reduce_add_sync(kFull, (unsigned)((nfull > 0) | (v0.y != 0.0f)));
+    const unsigned tv = __reduce_add_sync(kFull, (unsigned)(nfull > 0));
+    const unsigned up = __reduce_add_sync(kFull, (unsigned)nfull);
+    if (lane == 0) {
+      atomicAdd(&s_red[0], (int)nz);
+      atomicAdd(&s_red[1], (int)tv);
+      atomicAdd(&s_red[2], (int)up);
+    }
+    __syncthreads();
+    if (l == 0) {
+      c.nnz[phys] = s_red[0];
+      stat_add(c.item_stats, item, ST_DVOX, s_red[1]);
+      stat_add(c.item_stats, item, ST_UPD, s_red[2]);
+      stat_add(c.item_stats, item, ST_BTOUCH, 1);
+    }
+    __syncthreads();
   }
 }
 
@@ -1899,6 +2020,10 @@ void launch_check_div(unsigned long long seed, long long n, unsigned long long* 
 
 // ----------------------------------------------------------------------------
 // stage launchers
+cudaError_t kernels_init() {
+  return cudaFuncSetAttribute(k_heavy_update, cudaFuncAttributeMaxDynamicSharedMemorySize, kHuSmem);
+}
+
 void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   k_step_init<<<8, 256, 0, s>>>(c);
   *launches += 1;
@@ -1952,14 +2077,15 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c);
   k_heavy_plan<<<1, 1024, 0, s>>>(c);
   k_heavy_count<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
-  k_heavy_scan<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c);
+  k_heavy_scan<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c, sel);
   k_heavy_place<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
   *launches += 8;
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, lc.rec_passes & 1);
-  k_hot_chains<<<lc.sm_count * 4, HOT_T, 0, s>>>(c);
+  const int sel = lc.rec_passes & 1;
+  k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, s>>>(c, sel);
+  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel, lc.sm_count);
   *launches += 2;
 }
 
