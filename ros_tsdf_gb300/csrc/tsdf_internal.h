@@ -160,6 +160,7 @@ struct Ctx {
   int* digit_tot;                // [256]
   int* tile_sums;                // scan tiles
   int* seg_start;
+  int* seg_item;                 // batch item (map scan) of each segment
   int* enum_cnt;                 // publish counts per enumerated slot
   int* enum_gc;                  // gc flags per enumerated slot
   int* pub_prefix;

@@ -978,30 +978,28 @@ constexpr int UPD_T = 128;
 constexpr int kHotChain = 128;    // longer voxel chains of a heavy segment run as a warp each
 constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
-__global__ void k_seg_classify(Ctx c) {
+// Per segment: its batch item (the scan of the entry of its first record) and,
+// for segments longer than one update chunk, a place on the heavy list.
+__global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
+  __shared__ long long s_pb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
+  const unsigned* rv = c.rec_val[rec_sel];
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nseg;
        j += (long long)gridDim.x * blockDim.x) {
+    const long long b0 = c.seg_start[j];
     const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
-    if (b1 - c.seg_start[j] > UPD_T) {
+    c.seg_item[j] = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+    if (b1 - b0 > UPD_T) {
       unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_heavy), 1ull);
       c.heavy[k] = (int)j;
     }
   }
 }
 
-__device__ __forceinline__ int find_item_global(const ItemDev* items, int n, long long g) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (items[mid].point_base <= g)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
 
 
 // Heavy segments: a multi-CTA counting sort of their updates into per-voxel
@@ -1161,8 +1159,7 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c, int rec_s
       const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
       if (idx < half) {
         const long long b0 = c.seg_start[c.heavy[h]];
-        const unsigned v0 = c.rec_val[rec_sel][b0];
-        const int item = find_item_global(c.items, c.hdr->n_items, (long long)((v0 >> 5) / (unsigned)c.hdr->vox_stride));
+        const int item = c.seg_item[c.heavy[h]];
         HotChain hc;
         hc.bin = s_base + (unsigned long long)ex;
         hc.n = run;
@@ -1208,7 +1205,7 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
     const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
     const unsigned long long base = c.hbin_base[h];
     const bool fits = c.hfit[h] != 0;
-    const int item = find_item_global(c.items, c.hdr->n_items, (long long)((rv[b0] >> 5) / (unsigned)c.hdr->vox_stride));
+    const int item = c.seg_item[j];
     const float maxw = c.maps[c.items[item].map].maxw;
     for (int k = 0; k < ne && fits; ++k) {
       const int l = s_l[t * kUpdEntries + k];
@@ -1287,6 +1284,12 @@ __device__ __forceinline__ void chain_exact(float* sdf_io, float* w_io, const fl
   *w_io = W;
 }
 
+// The exact redo of a chain, out of line so that it does not shape the
+// register allocation of the fast loops.
+__device__ __noinline__ void chain_redo(float* sdf, float* W, const float4* bins, int n, float maxw) {
+  chain_exact(sdf, W, bins, n, maxw);
+}
+
 // One voxel's chain run by a warp: the 32 lanes keep four coalesced 32-bin
 // batches in flight and stage them through shared memory (tile: 2 x 32
 // float4 of this warp) while lane 0 runs the chain, so the chain never waits
@@ -1294,14 +1297,14 @@ __device__ __forceinline__ void chain_exact(float* sdf_io, float* w_io, const fl
 // steps: lane 0 runs the weight chain W' = RN(W + w), W = min(W', max)
 // (independent of the sdf), every lane takes one reciprocal RN(1/W'), and
 // lane 0 runs the sdf chain with Markstein steps.  From the batch where the
-// voxel is at max_weight on, the precomputed saturated bins (sat_step).  The
-// range flag or a NaN sends the whole chain to the exact redo.  The result is
-// valid in lane 0.
+// voxel is at max_weight on, the precomputed saturated bins (sat_step) in a
+// loop of full batches of its own, then the partial batch.  The range flag
+// or a NaN sends the whole chain to the exact redo.  The result is valid in
+// lane 0.
 __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* bins, int n, float maxw,
                                              float4 (*tile)[32], int lane) {
   const float s0 = sdf, w0 = W;
   bool ok = true;
-  bool sat = W == maxw;
   float4 reg[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -1309,7 +1312,8 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
     reg[j] = i < n ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
   }
   int buf = 0;
-  for (int base = 0; base < n; base += 32) {
+  int base = 0;
+  for (; base < n && __shfl_sync(kFull, W, 0) != maxw; base += 32) {
     tile[buf][lane] = reg[0];
     reg[0] = reg[1];
     reg[1] = reg[2];
@@ -1321,50 +1325,65 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
     __syncwarp();
     const int m = min(32, n - base);
     float4* tl = tile[buf];
-    if (__shfl_sync(kFull, sat, 0)) {
-      if (lane == 0) {
-        if (m == 32) {
-#pragma unroll
-          for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
-        } else {
-          for (int k = 0; k < m; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
-        }
+    if (lane == 0) {
+      // tile entry becomes {w d, W', RN(1/W'), W before the update}
+      for (int k = 0; k < m; ++k) {
+        const float nw = fadd(W, tl[k].w);
+        tl[k].y = nw;
+        tl[k].w = W;
+        W = fminf(nw, maxw);
       }
-    } else {
-      if (lane == 0) {
-        // tile entry becomes {w d, W', RN(1/W'), W before the update}
-        for (int k = 0; k < m; ++k) {
-          const float nw = fadd(W, tl[k].w);
-          tl[k].y = nw;
-          tl[k].w = W;
-          W = fminf(nw, maxw);
-        }
-      }
-      __syncwarp();
-      if (lane < m) {
-        const float nw = tl[lane].y;
-        tl[lane].z = markstein_range(nw) ? __frcp_rn(nw) : __uint_as_float(0x7FC00000u);
-      }
-      __syncwarp();
-      if (lane == 0) {
-        for (int k = 0; k < m; ++k) {
-          const float4 x = tl[k];
-          const float a = fadd(fmul(x.w, sdf), x.x);
-          const float qq = __fmul_rn(a, x.z);
-          const float rr = __fmaf_rn(-x.y, qq, a);
-          ok = ok & markstein_range(a);
-          sdf = __fmaf_rn(rr, x.z, qq);
-        }
-        sat = W == maxw;
+    }
+    __syncwarp();
+    if (lane < m) {
+      const float nw = tl[lane].y;
+      tl[lane].z = markstein_range(nw) ? __frcp_rn(nw) : __uint_as_float(0x7FC00000u);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      for (int k = 0; k < m; ++k) {
+        const float4 x = tl[k];
+        const float a = fadd(fmul(x.w, sdf), x.x);
+        const float qq = __fmul_rn(a, x.z);
+        const float rr = __fmaf_rn(-x.y, qq, a);
+        ok = ok & markstein_range(a);
+        sdf = __fmaf_rn(rr, x.z, qq);
       }
     }
     buf ^= 1;
     __syncwarp();
   }
+  for (; base + 32 <= n; base += 32) {
+    tile[buf][lane] = reg[0];
+    reg[0] = reg[1];
+    reg[1] = reg[2];
+    reg[2] = reg[3];
+    {
+      const int i = base + 128 + lane;
+      reg[3] = i < n ? bins[i] : make_float4(0.f, 1.f, 1.f, 0.f);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const float4* tl = tile[buf];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+    }
+    buf ^= 1;
+    __syncwarp();
+  }
+  if (base < n) {
+    tile[buf][lane] = reg[0];
+    __syncwarp();
+    if (lane == 0) {
+      const float4* tl = tile[buf];
+      for (int k = 0; k < n - base; ++k) sdf = sat_step(sdf, tl[k], maxw, &ok);
+    }
+    __syncwarp();
+  }
   if (lane == 0 && (!ok || sdf != sdf)) {
     sdf = s0;
     W = w0;
-    chain_exact(&sdf, &W, bins, n, maxw);
+    chain_redo(&sdf, &W, bins, n, maxw);
   }
   return make_float2(sdf, W);
 }
@@ -1438,7 +1457,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
     const long long b0 = c.seg_start[sj];
     const long long b1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
     const long long phys = h.key_lo + rk[b0];
-    const int item = find_item_global(c.items, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+    const int item = c.seg_item[sj];
     const MapDev& m = c.maps[c.items[item].map];
     const float maxw = m.maxw;
     float4* gv = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
@@ -1665,9 +1684,10 @@ __global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c, int rec_sel) {
   const unsigned* rv = c.rec_val[rec_sel];
   for (int h = blockIdx.x; h < np; h += gridDim.x) {
     if (!c.hfit[h]) continue;  // k_update's fallback passes take it
-    const long long b0 = c.seg_start[c.heavy[h]];
+    const int j = c.heavy[h];
+    const long long b0 = c.seg_start[j];
     const long long phys = hd.key_lo + rk[b0];
-    const int item = find_item_global(c.items, hd.n_items, (long long)((rv[b0] >> 5) / (unsigned)hd.vox_stride));
+    const int item = c.seg_item[j];
     const float maxw = c.maps[c.items[item].map].maxw;
     const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
     const float4* bins = c.hbin + c.hbin_base[h];
@@ -2074,7 +2094,7 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums);
   k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_rec_live, &c.ctr->n_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
-  k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c);
+  k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c, sel);
   k_heavy_plan<<<1, 1024, 0, s>>>(c);
   k_heavy_count<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
   k_heavy_scan<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c, sel);
