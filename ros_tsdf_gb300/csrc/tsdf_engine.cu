@@ -390,6 +390,22 @@ bool device_accessible(const void* p, const void** dev_ptr) {
   return false;
 }
 
+// Device or managed memory, which kernels read in place.  Host memory, pinned
+// or not, is copied in by the DMA engine instead: kernels reading it over the
+// host link would see its latency on every point load.
+bool device_resident(const void* p, const void** dev_ptr) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+    *dev_ptr = a.devicePointer ? a.devicePointer : p;
+    return true;
+  }
+  return false;
+}
+
 // Validate a batch and enqueue it on lane L (asynchronous).  On success the
 // lane is busy until finish_batch.
 tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans, tsdf_scan_result* res) {
@@ -439,7 +455,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     const void* dp = nullptr;
     if (s.n_points == 0) {
       it.pts = L.d_points;
-    } else if (device_accessible(s.xyz, &dp)) {
+    } else if (device_resident(s.xyz, &dp)) {
       it.pts = (const char*)dp;
     } else {
       long long nb = s.n_points * (long long)s.stride_bytes;
