@@ -370,9 +370,10 @@ def cpu_baseline_run(specs, scans, n_steps, warmup, threads):
     return pts / t, t
 
 
-def traffic_from_profiles(kernel: str):
-    """Per-unit DRAM bytes of `kernel` from a committed ncu summary, if present."""
-    p = ROOT / "profiles" / f"{kernel}.md"
+def traffic_from_profiles(kernel: str, workload: str):
+    """Per-unit DRAM bytes of `kernel` from its committed ncu summary
+    (profiles/<kernel>_<workload>.md), or None."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -382,6 +383,27 @@ def traffic_from_profiles(kernel: str):
             except ValueError:
                 return None
     return None
+
+
+# stage -> (kernels, unit counter in the per-step stats) for the roofline line
+STAGE_KERNELS = {
+    "update": (["k_heavy_update", "k_update"], "blocks_touched"),
+    "publish": (["k_pub_write"], "published_blocks"),
+    "ray_voxels": (["k_ray_voxels"], "n_points"),
+    "ray_blocks": (["k_ray_blocks"], "n_points"),
+}
+
+
+def stage_traffic(stage: str, workload: str, stats: dict):
+    """DRAM bytes per step of a stage's kernels: per-unit traffic from the ncu
+    summaries times this step's units (traffic grows with the units)."""
+    if stage not in STAGE_KERNELS:
+        return None
+    kernels, unit = STAGE_KERNELS[stage]
+    per = [traffic_from_profiles(k, workload) for k in kernels]
+    if any(v is None for v in per):
+        return None
+    return sum(per) * stats[unit]
 
 
 def main():
@@ -416,11 +438,12 @@ def main():
     stage_ms = {k: v[0] / max(v[1], 1) for k, v in stages.items()}
     dom = max(stage_ms, key=stage_ms.get)
     if dom == "update":
-        dom_bytes, kernel = ab["update"], "k_update"
+        dom_bytes = ab["update"]
     elif dom == "publish":
-        dom_bytes, kernel = ab["publish"], "k_pub_write"
+        dom_bytes = ab["publish"]
     else:
-        dom_bytes, kernel = ab["step"] * stage_ms[dom] / max(sum(stage_ms.values()), 1e-9), dom
+        dom_bytes = ab["step"] * stage_ms[dom] / max(sum(stage_ms.values()), 1e-9)
+    kernel = "+".join(STAGE_KERNELS[dom][0]) if dom in STAGE_KERNELS else dom
     achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
     step_gbs = ab["step"] / (r["ms_per_step"] / 1000.0) / 1e9
     line = {
@@ -433,7 +456,7 @@ def main():
         "e2e": r["e2e"], "plain": r["plain"],
         "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic_from_profiles(kernel),
+                     "traffic": stage_traffic(dom, args.workload, r["stats"]),
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / peak},
         "stage_ms_per_step": stage_ms,
         "per_step": {k: r["stats"][k] for k in ("n_points", "voxel_updates", "distinct_voxels", "blocks_touched",
