@@ -1388,6 +1388,10 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
   return make_float2(sdf, W);
 }
 
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // Hot chains (voxels of binned heavy segments with more than kHotChain
 // updates, listed by k_heavy_scan): one warp per chain, long chains dequeued
 // first.  The voxel is on no other update path this step.
@@ -1436,16 +1440,23 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
     run_hot_chains(c, tile, t & 31);
     __syncthreads();
   }
-  while (true) {
+  // The queue item after the current one is claimed when the current one
+  // starts; its segment bounds, block and records are fetched during the
+  // current segment's phases (prefetch only: no registers held), so the next
+  // iteration finds them in L1 instead of waiting on a chain of dependent
+  // global loads.
+  const long long nqueue = nheavy + nseg;
+  const long long nplanned = c.ctr->n_hplanned;
+  if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
+  __syncthreads();
+  long long q = s_seg;
+  __syncthreads();
+  for (; q < nqueue; __syncthreads(), q = s_seg, __syncthreads()) {
     if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
-    __syncthreads();
-    long long q = s_seg;
-    __syncthreads();
-    if (q >= nheavy + nseg) break;
     long long sj;
     bool heavy;
     if (q < nheavy) {
-      if (q < c.ctr->n_hplanned && c.hfit[q]) continue;  // k_heavy_update's
+      if (q < nplanned && c.hfit[q]) continue;  // k_heavy_update's
       sj = c.heavy[q];
       heavy = true;
     } else {
@@ -1466,6 +1477,14 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
     sv4[t + UPD_T] = gv[t + UPD_T];
     if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
     __syncthreads();  // the staged block and touch mask are shared by every path below
+    // next item: segment bounds now, its block and records further down
+    const long long qn = s_seg;
+    long long nb0 = -1, nb1 = 0;
+    if (qn < nqueue && !(qn < nplanned && c.hfit[qn])) {
+      const long long sjn = qn < nheavy ? (long long)c.heavy[qn] : qn - nheavy;
+      nb0 = c.seg_start[sjn];
+      nb1 = (sjn + 1 < nseg) ? c.seg_start[sjn + 1] : nrec;
+    }
     unsigned n_upd = 0;
     if (!heavy) {
       // ---- light path: the whole segment in one chunk
@@ -1494,6 +1513,11 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
       }
       n_upd += ne;
       __syncthreads();
+      unsigned nrk = 0u, nrv = 0u;
+      if (nb0 >= 0) {
+        nrk = rk[nb0];
+        if (nb0 + t < nb1 && t < UPD_T) nrv = rv[nb0 + t];
+      }
       {
         int a[4];
 #pragma unroll
@@ -1513,6 +1537,16 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
         if (t == 0) s_off[kVoxelsPerBlock] = tot;
       }
       __syncthreads();
+      if (nb0 >= 0) {
+        const float4* ngv = reinterpret_cast<const float4*>(c.voxels + (h.key_lo + nrk) * kVoxelsPerBlock);
+        prefetch_l1(ngv + t);
+        prefetch_l1(ngv + t + UPD_T);
+        if ((nrv & 31u) != 0u) {
+          const uint2* ne0 = c.entries + (nrv >> 5);
+          prefetch_l1(ne0);
+          prefetch_l1(ne0 + (nrv & 31u) - 1);
+        }
+      }
       for (int k = 0; k < ne; ++k) {
         const int l = s_l[t * kUpdEntries + k];
         int rank = __popc(s_mask[l][t >> 5] & lt_bits);
@@ -1649,7 +1683,6 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
       stat_add(c.item_stats, item, ST_DVOX, b);
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
     }
-    __syncthreads();
   }
 }
 
@@ -1681,7 +1714,6 @@ __global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c, int rec_sel) {
   const int np = (int)c.ctr->n_hplanned;
   const BatchHdr hd = *c.hdr;
   const unsigned* rk = c.rec_key[rec_sel];
-  const unsigned* rv = c.rec_val[rec_sel];
   for (int h = blockIdx.x; h < np; h += gridDim.x) {
     if (!c.hfit[h]) continue;  // k_update's fallback passes take it
     const int j = c.heavy[h];
@@ -2105,9 +2137,9 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
   k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c, sel);
   k_heavy_plan<<<1, 1024, 0, s>>>(c);
-  k_heavy_count<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
-  k_heavy_scan<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c, sel);
-  k_heavy_place<<<lc.sm_count * 4, UPD_T, 0, s>>>(c, sel);
+  k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c, sel);
+  k_heavy_scan<<<lc.sm_count * 4, kVoxelsPerBlock, 0, s>>>(c, sel);
+  k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
   *launches += 8;
 }
 
