@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--heap-blocks", type=int, default=1 << 16, help="per-map heap capacity (blocks)")
     ap.add_argument("--pub-cap", type=int, default=1 << 20)
     ap.add_argument("--json-out", default=None)
+    ap.add_argument("--bucket-size", type=int, default=1, choices=[1, 2, 4, 8, 16], help="hash bucket size (tuning)")
+    ap.add_argument("--ray-chunk", type=int, default=32, help="points per ray work-queue item (tuning)")
+    ap.add_argument("--ray-threads", type=int, default=256, choices=[64, 128, 256], help="ray kernel CTA size")
     return ap.parse_args()
 
 
@@ -190,7 +193,8 @@ def run_ours(args, rank, world, local, pg):
 
     def new_engine(**kw):
         return Engine(device=local, max_maps=max(64, len(specs)), pool_blocks=pool, max_batch_points=max_pts,
-                      max_publish=cap * len(specs), **kw)
+                      max_publish=cap * len(specs), bucket_size=args.bucket_size, ray_chunk=args.ray_chunk,
+                      ray_threads=args.ray_threads, **kw)
 
     # ---- value: device-resident inputs and outputs, CUDA-event device time
     eng = new_engine()

@@ -83,7 +83,7 @@ typedef struct tsdf_engine_cfg {
   int64_t pool_blocks;      /* voxel blocks shared by all maps, 4 KiB each    */
   int64_t max_batch_points; /* points per step over all maps (default 1<<20)  */
   int64_t max_publish;      /* published voxels per step, staging (default 8M)*/
-  int bucket_size;          /* hash entries per bucket: 4, 8 or 16 (def. 8)   */
+  int bucket_size;          /* hash entries per bucket: 1, 2, 4, 8, 16 (def. 1)*/
   int ray_threads;          /* threads per CTA of the ray kernels (def. 256)  */
   int ray_chunk;            /* points per work-queue item (default 32)        */
   int max_routes;           /* per-point block routes of the voxel pass (16)  */

@@ -728,8 +728,9 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   if (c.pool_blocks <= 0) c.pool_blocks = kDefaultPool;
   if (c.max_batch_points <= 0) c.max_batch_points = kDefaultBatchPoints;
   if (c.max_publish <= 0) c.max_publish = kDefaultPublish;
-  if (c.bucket_size <= 0) c.bucket_size = 8;
-  if (c.bucket_size != 4 && c.bucket_size != 8 && c.bucket_size != 16) return TSDF_ERR_INVALID_ARG;
+  if (c.bucket_size <= 0) c.bucket_size = 1;
+  if (c.bucket_size != 1 && c.bucket_size != 2 && c.bucket_size != 4 && c.bucket_size != 8 && c.bucket_size != 16)
+    return TSDF_ERR_INVALID_ARG;
   if (c.ray_threads <= 0) c.ray_threads = 256;
   if (c.ray_threads != 64 && c.ray_threads != 128 && c.ray_threads != 256) return TSDF_ERR_INVALID_ARG;
   if (c.ray_chunk <= 0) c.ray_chunk = 32;

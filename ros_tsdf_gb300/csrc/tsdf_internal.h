@@ -198,7 +198,7 @@ enum {
 // pipeline stage on `s`; every launch is counted in *launches.
 struct LaunchCfg {
   int sm_count;
-  int bucket_size;   // 4, 8 or 16
+  int bucket_size;   // 1, 2, 4, 8 or 16
   int ray_threads;
   int rank_passes;
   int rec_passes;

@@ -192,50 +192,25 @@ struct Dda {
       done = true;
       return true;
     }
-    if (tmx < tmy) {
-      if (tmx < tmz) {
-        cx = fadd(cx, stx);
-        tmx = fadd(tmx, tdx);
-      } else if (tmx > tmz) {
-        cz = fadd(cz, stz);
-        tmz = fadd(tmz, tdz);
-      } else {
-        cx = fadd(cx, stx);
-        cz = fadd(cz, stz);
-        tmx = fadd(tmx, tdx);
-        tmz = fadd(tmz, tdz);
-      }
-    } else if (tmx > tmy) {
-      if (tmy < tmz) {
-        cy = fadd(cy, sty);
-        tmy = fadd(tmy, tdy);
-      } else if (tmy > tmz) {
-        cz = fadd(cz, stz);
-        tmz = fadd(tmz, tdz);
-      } else {
-        cy = fadd(cy, sty);
-        cz = fadd(cz, stz);
-        tmy = fadd(tmy, tdy);
-        tmz = fadd(tmz, tdz);
-      }
-    } else {
-      if (tmz < tmx) {
-        cz = fadd(cz, stz);
-        tmz = fadd(tmz, tdz);
-      } else if (tmz > tmx) {
-        cx = fadd(cx, stx);
-        cy = fadd(cy, sty);
-        tmx = fadd(tmx, tdx);
-        tmy = fadd(tmy, tdy);
-      } else {
-        cx = fadd(cx, stx);
-        cy = fadd(cy, sty);
-        cz = fadd(cz, stz);
-        tmx = fadd(tmx, tdx);
-        tmy = fadd(tmy, tdy);
-        tmz = fadd(tmz, tdz);
-      }
-    }
+    // The reference's branch tree over the three crossing distances
+    // (tsdf_handler.cu:175-227), as per-axis step flags so that the lanes of
+    // a warp do not split over its seven outcomes.  Ties step several axes;
+    // a NaN distance (0/0 on an axis the ray does not move along) compares
+    // false everywhere, as in the tree.
+    const bool lt_xy = tmx < tmy, gt_xy = tmx > tmy;
+    const bool lt_xz = tmx < tmz, gt_xz = tmx > tmz;
+    const bool lt_yz = tmy < tmz, gt_yz = tmy > tmz;
+    const bool step_x = lt_xy ? !gt_xz : (!gt_xy && !gt_xz);
+    const bool step_y = !lt_xy && (gt_xy ? !gt_yz : !gt_xz);
+    const bool step_z = lt_xy ? !lt_xz : (gt_xy ? !lt_yz : !lt_xz);
+    const float ncx = fadd(cx, stx), ncy = fadd(cy, sty), ncz = fadd(cz, stz);
+    const float ntx = fadd(tmx, tdx), nty = fadd(tmy, tdy), ntz = fadd(tmz, tdz);
+    cx = step_x ? ncx : cx;
+    cy = step_y ? ncy : cy;
+    cz = step_z ? ncz : cz;
+    tmx = step_x ? ntx : tmx;
+    tmy = step_y ? nty : tmy;
+    tmz = step_z ? ntz : tmz;
     float px = ccx, py = ccy, pz = ccz;
     ccx = cell_center(cx, scale, ys, half, &fx);
     ccy = cell_center(cy, scale, ys, half, &fy);
@@ -832,7 +807,7 @@ __global__ void __launch_bounds__(1024) k_alloc_finalize(Ctx c) {
 // entries[g * vox_stride + j]; each run of voxels in one block yields one
 // routing record (block slot, entry range) at rec[g * rec_stride + run].
 template <int G>
-__global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
+__global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
   __shared__ long long s_pb[kMaxItems];
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
@@ -874,6 +849,11 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
       const HEntry* tab = c.hash + m.hash_base;
       const unsigned mask = m.hash_mask;
       const long long kbase = m.heap_base - h.key_lo;
+      // per-map constants and the origin in registers: the loop's stores
+      // could alias the map and item records as far as the compiler knows
+      const float scale_b = m.scale_b, rs_b = m.rs_b, half_bs = m.half_bs, vs = m.vs, r_vs = m.r_vs;
+      const int rmax = m.rmax;
+      const float ox = it.ox, oy = it.oy, oz = it.oz;
       const long long rbase = g * (long long)R;
       const long long ebase = g * (long long)VS;
       unsigned long long cur = kEmptyKey;
@@ -888,14 +868,14 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
         unsigned long long bkey = 0;
         float fbx = 0.f, fby = 0.f, fbz = 0.f;
         if (has) {
-          fbx = floorf(fmul(x, m.scale_b));
-          fby = floorf(fmul(y, m.scale_b));
-          fbz = floorf(fmul(z, m.scale_b));
+          fbx = floorf(fmul(x, scale_b));
+          fby = floorf(fmul(y, scale_b));
+          fbz = floorf(fmul(z, scale_b));
           bkey = pack_key((int)fbx, (int)fby, (int)fbz);
         }
         const bool newrun = has && bkey != cur;
         if (newrun) {
-          if (run >= 0 && run < m.rmax) {
+          if (run >= 0 && run < rmax) {
             rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
             rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
           }
@@ -905,13 +885,13 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
           run_start = j;
           run_cnt = 0;
           // block centre and bottom-left corner (tsdf_handler.cu:612-624)
-          blx = fsub(fadd(div_const(fbx, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
-          bly = fsub(fadd(div_const(fby, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
-          blz = fsub(fadd(div_const(fbz, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
+          blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
+          bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
+          blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
         }
-        const bool need = newrun && run < m.rmax;
+        const bool need = newrun && run < rmax;
         const unsigned nm = __ballot_sync(kFull, need);
-        for (int i = 0; i < G; ++i) {
+        for (int i = 0; i < G && (nm & gmask) != 0u; ++i) {
           const int src = gbase + i;
           if (!((nm >> src) & 1u)) continue;
           unsigned long long k2 = __shfl_sync(gmask, bkey, src);
@@ -922,7 +902,7 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
           if (lane == src) run_slot = res;
         }
         if (has) {
-          if (run >= m.rmax) {
+          if (run >= rmax) {
             ++route_ovf;
           } else if (run_slot < 0) {
             ++missing;
@@ -930,15 +910,15 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
             ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
           } else {
             // getLocalVoxelIndex (tsdf_handler.cu:507-512)
-            float ix = floorf(div_const(fsub(x, blx), m.vs, m.r_vs));
-            float iy = floorf(div_const(fsub(y, bly), m.vs, m.r_vs));
-            float iz = floorf(div_const(fsub(z, blz), m.vs, m.r_vs));
+            float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
+            float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
+            float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
             unsigned local = kBadLocal;
             if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
               local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
             else
               ++bad;
-            const float d = distance_update(x, y, z, px, py, pz, it.ox, it.oy, it.oz);
+            const float d = distance_update(x, y, z, px, py, pz, ox, oy, oz);
             ent[ebase + j] = make_uint2(__float_as_uint(d), local);
             ++run_cnt;
           }
@@ -946,11 +926,11 @@ __global__ void __launch_bounds__(256) k_ray_voxels(Ctx c) {
         }
       }
       if (active) {
-        if (run >= 0 && run < m.rmax) {
+        if (run >= 0 && run < rmax) {
           rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
           rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
         }
-        int first = valid ? min(run + 1, m.rmax) : 0;
+        int first = valid ? min(run + 1, rmax) : 0;
         for (int r = first; r < R; ++r) rk[rbase + r] = kRecSentinel;
       }
       stat_add_warp(c.item_stats, item, ST_VOVF, (valid && dda.ovf) ? 1u : 0u);
@@ -2093,6 +2073,8 @@ void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* la
 void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * (2048 / lc.ray_threads);
   switch (lc.bucket_size) {
+    case 1: k_ray_blocks<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 2: k_ray_blocks<2><<<grid, lc.ray_threads, 0, s>>>(c); break;
     case 4: k_ray_blocks<4><<<grid, lc.ray_threads, 0, s>>>(c); break;
     case 16: k_ray_blocks<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
     default: k_ray_blocks<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
@@ -2118,6 +2100,8 @@ void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* l
 void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * (2048 / lc.ray_threads);
   switch (lc.bucket_size) {
+    case 1: k_ray_voxels<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 2: k_ray_voxels<2><<<grid, lc.ray_threads, 0, s>>>(c); break;
     case 4: k_ray_voxels<4><<<grid, lc.ray_threads, 0, s>>>(c); break;
     case 16: k_ray_voxels<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
     default: k_ray_voxels<8><<<grid, lc.ray_threads, 0, s>>>(c); break;

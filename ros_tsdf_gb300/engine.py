@@ -55,7 +55,7 @@ def _as_points(xyz) -> tuple[np.ndarray, int]:
 
 class Engine:
     def __init__(self, device: int = 0, max_maps: int = 64, pool_blocks: int = 1 << 18,
-                 max_batch_points: int = 1 << 20, max_publish: int = 1 << 23, bucket_size: int = 8,
+                 max_batch_points: int = 1 << 20, max_publish: int = 1 << 23, bucket_size: int = 1,
                  ray_threads: int = 256, ray_chunk: int = 32, max_routes: int = 16, lanes: int = 1,
                  graphs: bool = True, hot_chains: int = 0):
         self.lib = L.load()

@@ -117,7 +117,8 @@ def test_batched_multimap_matches_oracle(built):
     assert heavy_seen
 
 
-@pytest.mark.parametrize("cfg", [dict(bucket_size=4), dict(bucket_size=16), dict(ray_threads=128, ray_chunk=256),
+@pytest.mark.parametrize("cfg", [dict(bucket_size=2), dict(bucket_size=4), dict(bucket_size=8), dict(bucket_size=16),
+                                 dict(ray_threads=128, ray_chunk=256),
                                  dict(graphs=False), dict(ray_chunk=64, bucket_size=4, graphs=False),
                                  dict(hot_chains=2)])
 def test_engine_configs_give_identical_results(built, cfg):
