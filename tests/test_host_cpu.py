@@ -86,3 +86,19 @@ def test_two_rank_gloo_map_parallel(built):
     assert out[0][1] != out[1][1]  # different maps per rank
     assert out[0][2] == out[1][2] == out[0][1] + out[1][1]
     assert out[0][3] == out[1][3] == 2.0
+
+
+def test_poisson_trace_is_seeded_and_sorted():
+    from ros_tsdf_gb300 import serving as S
+
+    a = S.poisson_trace(64, 10.0, 2.0, 6, seed=5)
+    b = S.poisson_trace(64, 10.0, 2.0, 6, seed=5)
+    assert [(r.client, r.scan, r.t_arrival) for r in a] == [(r.client, r.scan, r.t_arrival) for r in b]
+    assert all(x.t_arrival <= y.t_arrival for x, y in zip(a, a[1:]))
+    assert all(0.0 <= r.t_arrival < 2.0 and 0 <= r.scan < 6 for r in a)
+    # 64 clients x 10 Hz x 2 s = 1280 expected arrivals; Poisson spread is about 36
+    assert 1100 < len(a) < 1460
+    per = {}
+    for r in a:
+        per.setdefault(r.client, []).append(r.scan)
+    assert all(v == [k % 6 for k in range(len(v))] for v in per.values())
