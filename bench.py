@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--heap-blocks", type=int, default=1 << 16, help="per-map heap capacity (blocks)")
     ap.add_argument("--pub-cap", type=int, default=1 << 20)
     ap.add_argument("--json-out", default=None)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use --bucket-size/--ray-chunk/--ray-threads instead of the autotuner's choice")
     ap.add_argument("--bucket-size", type=int, default=1, choices=[1, 2, 4, 8, 16], help="hash bucket size (tuning)")
     ap.add_argument("--ray-chunk", type=int, default=32, help="points per ray work-queue item (tuning)")
     ap.add_argument("--ray-threads", type=int, default=256, choices=[64, 128, 256], help="ray kernel CTA size")
@@ -482,6 +484,15 @@ def main():
         if rank == 0:
             print(json.dumps({"serving": run_serving(args, local)}))
         return
+    tuned = None
+    if not args.no_autotune:
+        from ros_tsdf_gb300 import autotune
+
+        specs0 = make_workload(args.workload, rank, args.heap_blocks)
+        sample = gen_scans(specs0, 4)
+        best = autotune.tune(specs0, sample, steps=3, device=local)
+        args.bucket_size, args.ray_chunk, args.ray_threads = best["bucket_size"], best["ray_chunk"], best["ray_threads"]
+        tuned = dict(best, source="ros_tsdf_gb300.autotune on the first 4 scans of every map")
     r = run_ours(args, rank, world, local, pg)
     peak, peak_kind = load_peaks()
     ab = algorithmic_bytes(r["stats"])
@@ -504,7 +515,9 @@ def main():
         "dtype": "f32", "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
         "config": {"workload": args.workload, "maps": len(r["specs"]),
                    "points_per_step": r["timed_pts"] / n, "voxel_size": 0.5, "truncation_distance": 4.0,
-                   "l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step"},
+                   "l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step",
+                   "launch": tuned or {"bucket_size": args.bucket_size, "ray_chunk": args.ray_chunk,
+                                       "ray_threads": args.ray_threads, "source": "command line"}},
         "e2e": r["e2e"], "plain": r["plain"],
         "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,

@@ -1,0 +1,98 @@
+"""Autotuner for the engine's launch parameters: hash bucket size (lanes per
+cooperative probe), ray work-queue chunk (points per queue item) and ray CTA
+size (rays per CTA).  None of them changes a result bit: the engine's steps
+are deterministic for every choice (tests/test_parity_gpu.py checks this),
+so the tuner only times candidates on a sample of the caller's workload and
+keeps the fastest.  Results are cached per device and workload signature in
+a JSON file.
+
+    from ros_tsdf_gb300 import autotune
+    best = autotune.tune(specs, scans, steps=3)        # {'bucket_size': 1, 'ray_chunk': 32, 'ray_threads': 256}
+    eng = Engine(..., **best)
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+
+from .engine import Engine
+
+CANDIDATES = [dict(bucket_size=b, ray_chunk=ch, ray_threads=rt)
+              for b in (1, 2, 4, 8) for ch in (32, 64) for rt in (128, 256)]
+
+
+def default_cache() -> Path:
+    root = os.environ.get("XDG_CACHE_HOME") or os.path.join(os.path.expanduser("~"), ".cache")
+    return Path(root) / "ros_tsdf_gb300" / "autotune.json"
+
+
+def signature(specs, n_points: list[int]) -> str:
+    """Workload signature: map count, voxel sizes, truncation distances and a
+    coarse histogram of scan sizes (powers of two)."""
+    sizes = sorted(int(np.log2(max(n, 1))) for n in n_points)
+    items = sorted((round(s.params.voxel_size, 4), round(s.params.truncation_distance, 4)) for s in specs)
+    raw = json.dumps({"maps": len(specs), "params": items, "sizes": sizes})
+    return hashlib.sha1(raw.encode()).hexdigest()[:16]
+
+
+def device_key(eng: Engine) -> str:
+    return f"sm{eng.sm_count}"
+
+
+def time_candidate(cand: dict, specs, scans, steps: int, device: int = 0, **engine_kw) -> float:
+    """Mean device time (ms) of one batched step over `steps` steps after
+    one untimed step, on a fresh engine with the candidate's parameters."""
+    pool = sum(s.heap_blocks for s in specs) + 64
+    max_pts = max(sum(scans[m][k][0].shape[0] for m in range(len(specs))) for k in range(len(scans[0])))
+    with Engine(device=device, max_maps=max(len(specs), 1), pool_blocks=pool,
+                max_batch_points=max(max_pts, 1024), **cand, **engine_kw) as eng:
+        mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+        eng.set_stage_timing(True)
+        n = len(scans[0])
+        total = 0.0
+        timed = 0
+        for k in range(min(n, steps + 1)):
+            if k == 1:
+                eng.reset_stage_times()
+            eng.integrate_batch([(mids[m], *scans[m][k]) for m in range(len(specs))], pub_cap=0)
+            timed = k
+        st = eng.stage_times()
+        total = sum(v[0] for v in st.values())
+        return total / max(timed, 1)
+
+
+def tune(specs, scans, steps: int = 3, device: int = 0, cache: Path | None = None, candidates=None,
+         refresh: bool = False, **engine_kw) -> dict:
+    """Pick the fastest candidate for this workload (cached).  `scans[m][k]`
+    is scan k of map m as (points, origin); the first `steps + 1` are used."""
+    cache = Path(cache) if cache else default_cache()
+    candidates = candidates or CANDIDATES
+    with Engine(device=device, max_maps=1, pool_blocks=64, max_batch_points=1024) as probe:
+        dkey = device_key(probe)
+    sig = signature(specs, [scans[m][0][0].shape[0] for m in range(len(specs))])
+    table = {}
+    if cache.exists():
+        try:
+            table = json.loads(cache.read_text())
+        except ValueError:
+            table = {}
+    key = f"{dkey}/{sig}"
+    if not refresh and key in table:
+        return dict(table[key]["best"])
+    times = []
+    for cand in candidates:
+        times.append((time_candidate(cand, specs, scans, steps, device, **engine_kw), cand))
+    times.sort(key=lambda x: x[0])
+    best = dict(times[0][1])
+    table[key] = {"best": best, "ms_per_step": times[0][0],
+                  "tried": [{"ms_per_step": t, **c} for t, c in times]}
+    try:
+        cache.parent.mkdir(parents=True, exist_ok=True)
+        cache.write_text(json.dumps(table, indent=1))
+    except OSError:
+        pass
+    return best

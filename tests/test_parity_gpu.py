@@ -390,3 +390,27 @@ def test_update_division_matches_cuda_fdiv(built):
         first = (C.c_float * 2)()
         eng._check(eng.lib.tsdf_check_division(eng.h, 12345, 1 << 28, C.byref(mism), first), "check_division")
         assert mism.value == 0, f"first mismatch a={first[0]!r} b={first[1]!r}"
+
+
+def test_autotune_choice_keeps_parity(built, tmp_path):
+    """The autotuner times candidates, caches its choice, and the chosen
+    launch parameters reproduce the oracle on configs[0] run map by map."""
+    from ros_tsdf_gb300 import Engine, autotune, workloads as W
+
+    specs = [W.plain_small(seed=s, heap_blocks=1 << 14) for s in (0, 1)]
+    srcs = [W.ScanSource(s) for s in specs]
+    scans = [[src.scan(k) for k in range(4)] for src in srcs]
+    cands = [dict(bucket_size=1, ray_chunk=32, ray_threads=256), dict(bucket_size=4, ray_chunk=64, ray_threads=128)]
+    cache = tmp_path / "tune.json"
+    best = autotune.tune(specs, scans, steps=2, cache=cache, candidates=cands)
+    assert best in cands and cache.exists()
+    assert autotune.tune(specs, scans, steps=2, cache=cache, candidates=cands[::-1]) == best  # cached
+    for m, spec in enumerate(specs):
+        orc = _oracle(spec.params, spec.heap_blocks)
+        with Engine(max_maps=1, pool_blocks=spec.heap_blocks, max_batch_points=1 << 16, **best) as eng:
+            mid = eng.create_map(spec.params, spec.heap_blocks)
+            for k in range(4):
+                r = eng.integrate(mid, *scans[m][k], pub_cap=1 << 18)
+                assert_scan_equal(r, orc.integrate(*scans[m][k], pub_cap=1 << 18), spec.params.truncation_distance,
+                                  f"map {m} scan {k}")
+            assert_state_equal(eng, mid, orc, spec.heap_blocks)
