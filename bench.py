@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="multimap32", choices=["multimap32", "plain_small", "large_stream"])
+    ap.add_argument("--workload", default="multimap32", choices=["multimap32", "plain_small", "large_stream", "stress8"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -164,6 +164,8 @@ def make_workload(name: str, rank: int, heap_blocks: int = 1 << 16):
         specs = W.multimap32(32, base_seed=1000 + 100 * rank, heap_blocks=heap_blocks)
     elif name == "plain_small":
         specs = [W.plain_small(seed=rank, heap_blocks=heap_blocks)]
+    elif name == "stress8":
+        specs = W.stress8(8, base_seed=4000 + 100 * rank, heap_blocks=max(heap_blocks, 1 << 22))
     else:
         specs = [W.large_stream(seed=2000 + rank, heap_blocks=max(heap_blocks, 1 << 21))]
     return specs
@@ -199,7 +201,7 @@ def run_ours(args, rank, world, local, pg):
     def new_engine(**kw):
         return Engine(device=local, max_maps=max(64, len(specs)), pool_blocks=pool, max_batch_points=max_pts,
                       max_publish=cap * len(specs), bucket_size=args.bucket_size, ray_chunk=args.ray_chunk,
-                      ray_threads=args.ray_threads, **kw)
+                      ray_threads=args.ray_threads, max_routes=max(8, max(s.params.routes() for s in specs)), **kw)
 
     # ---- value: device-resident inputs and outputs, CUDA-event device time
     eng = new_engine()
@@ -436,7 +438,7 @@ def run_serving(args, local: int) -> dict:
     for mode in ("served", "plain"):
         eng = Engine(device=local, max_maps=64, pool_blocks=heap * len(specs) + 64, max_batch_points=1 << 20,
                      max_publish=1 << 20, lanes=2, bucket_size=args.bucket_size, ray_chunk=args.ray_chunk,
-                     ray_threads=args.ray_threads)
+                     ray_threads=args.ray_threads, max_routes=max(8, max(s.params.routes() for s in specs)))
         rig = S.ServingRig(eng, specs, n_scans, pub_cap=400000)
         out["clients_admitted"] = rig.admitted
         if mode == "served":
@@ -514,7 +516,9 @@ def main():
         "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
         "config": {"workload": args.workload, "maps": len(r["specs"]),
-                   "points_per_step": r["timed_pts"] / n, "voxel_size": 0.5, "truncation_distance": 4.0,
+                   "points_per_step": r["timed_pts"] / n,
+                   "voxel_size": sorted({s.params.voxel_size for s in r["specs"]}),
+                   "truncation_distance": sorted({s.params.truncation_distance for s in r["specs"]}),
                    "l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step",
                    "launch": tuned or {"bucket_size": args.bucket_size, "ray_chunk": args.ray_chunk,
                                        "ray_threads": args.ray_threads, "source": "command line"}},

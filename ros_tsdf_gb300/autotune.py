@@ -48,8 +48,10 @@ def time_candidate(cand: dict, specs, scans, steps: int, device: int = 0, **engi
     one untimed step, on a fresh engine with the candidate's parameters."""
     pool = sum(s.heap_blocks for s in specs) + 64
     max_pts = max(sum(scans[m][k][0].shape[0] for m in range(len(specs))) for k in range(len(scans[0])))
+    kw = dict(engine_kw)
+    kw.setdefault("max_routes", max(8, max(s.params.routes() for s in specs)))
     with Engine(device=device, max_maps=max(len(specs), 1), pool_blocks=pool,
-                max_batch_points=max(max_pts, 1024), **cand, **engine_kw) as eng:
+                max_batch_points=max(max_pts, 1024), **cand, **kw) as eng:
         mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
         eng.set_stage_timing(True)
         n = len(scans[0])

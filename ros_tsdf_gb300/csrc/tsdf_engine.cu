@@ -121,6 +121,8 @@ struct Request {
 
 struct Lane {
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   Ctx ctx{};
   // device scratch
   BatchHdr* d_hdr = nullptr;
@@ -224,19 +226,25 @@ tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>*
     if (_s != TSDF_OK) return _s;       \
   } while (0)
 
-LaunchCfg launch_cfg(tsdf_engine* eng, int rank_passes, int rec_passes) {
+LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes) {
   LaunchCfg lc;
   lc.sm_count = eng->sm_count;
   lc.bucket_size = eng->cfg.bucket_size;
   lc.ray_threads = eng->cfg.ray_threads;
   lc.rank_passes = rank_passes;
   lc.rec_passes = rec_passes;
+  lc.side = L.side;
+  lc.ev_fork = L.ev_fork;
+  lc.ev_join = L.ev_join;
   return lc;
 }
 
 tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   const tsdf_engine_cfg& c = eng->cfg;
   CK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&L.ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&L.ev_join, cudaEventDisableTiming));
   for (int i = 0; i <= STAGE_COUNT; ++i) CK(cudaEventCreate(&L.ev_stage[i]));
   CK(cudaEventCreateWithFlags(&L.ev_done, cudaEventDisableTiming));
   const long long npts = c.max_batch_points;
@@ -274,13 +282,15 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.entries, entry_cap, tr));
   TRY(dalloc(eng, &x.bin_d, entry_cap, tr));
   TRY(dalloc(eng, &x.heavy, rec_cap, tr));
-  x.hchunk_cap = (int)std::min<long long>(rec_cap / 128 + 64, 1 << 15);
+  // heavy-block counting sort: every routing record can sit in a planned
+  // heavy segment (dense scans at small voxel sizes put most blocks there)
+  x.hchunk_cap = (int)std::min<long long>(rec_cap / 128 + 64, 1 << 30);
   TRY(dalloc(eng, &x.hchunk_base, x.hchunk_cap, tr));
   TRY(dalloc(eng, &x.hcnt, (long long)x.hchunk_cap * kVoxelsPerBlock, tr));
   TRY(dalloc(eng, &x.hvoff, (long long)(x.hchunk_cap / 2 + 1) * (kVoxelsPerBlock + 1), tr));
   TRY(dalloc(eng, &x.hbin_base, x.hchunk_cap / 2 + 1, tr));
   TRY(dalloc(eng, &x.hfit, x.hchunk_cap / 2 + 1, tr));
-  x.hbin_cap = std::min<long long>(entry_cap, 1ll << 23);
+  x.hbin_cap = std::min<long long>(entry_cap, std::max<long long>(1ll << 23, npts * 32));
   TRY(dalloc(eng, &x.hbin, x.hbin_cap, tr));
   x.hot_cap = c.hot_chains;
   TRY(dalloc(eng, &x.hot, x.hot_cap, tr));
@@ -324,6 +334,9 @@ void lane_free(Lane& L) {
   for (int i = 0; i <= STAGE_COUNT; ++i)
     if (L.ev_stage[i]) cudaEventDestroy(L.ev_stage[i]);
   if (L.ev_done) cudaEventDestroy(L.ev_done);
+  if (L.ev_fork) cudaEventDestroy(L.ev_fork);
+  if (L.ev_join) cudaEventDestroy(L.ev_join);
+  if (L.side) cudaStreamDestroy(L.side);
   if (L.stream) cudaStreamDestroy(L.stream);
   L = Lane();
 }
@@ -331,7 +344,7 @@ void lane_free(Lane& L) {
 // Enqueue the pipeline of one step on the lane's stream (used directly or
 // inside a graph capture).  Returns the number of kernel launches.
 long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool timed) {
-  LaunchCfg lc = launch_cfg(eng, rank_passes, rec_passes);
+  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes);
   long long n = 0;
   using Fn = void (*)(const Ctx&, const LaunchCfg&, cudaStream_t, long long*);
   const Fn stages[STAGE_COUNT] = {stage_init,       stage_ray_blocks,  stage_alloc_order,

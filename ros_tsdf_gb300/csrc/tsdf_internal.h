@@ -202,6 +202,9 @@ struct LaunchCfg {
   int ray_threads;
   int rank_passes;
   int rec_passes;
+  cudaStream_t side;     // second stream of the lane: a stage may fork work onto it
+  cudaEvent_t ev_fork;   // and join it back (timing disabled; usable in graph capture)
+  cudaEvent_t ev_join;
 };
 
 cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice

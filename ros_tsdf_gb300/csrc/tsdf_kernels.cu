@@ -2128,9 +2128,17 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  // k_update (hot chains first, then the light blocks) and k_heavy_update
+  // (binned heavy blocks) touch disjoint voxels: fork the latter onto the
+  // lane's side stream so it fills the SMs the light blocks leave while the
+  // longest chains still run, and join before the publish stage
   const int sel = lc.rec_passes & 1;
-  k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, s>>>(c, sel);
+  cudaEventRecord(lc.ev_fork, s);
+  cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel, lc.sm_count);
+  k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
+  cudaEventRecord(lc.ev_join, lc.side);
+  cudaStreamWaitEvent(s, lc.ev_join, 0);
   *launches += 2;
 }
 

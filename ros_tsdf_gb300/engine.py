@@ -36,6 +36,15 @@ class TsdfParams:
         return L.Params(self.voxel_size, self.truncation_distance, self.max_weight,
                         self.publish_distance_squared, self.garbage_collect_distance_squared)
 
+    def routes(self) -> int:
+        """Block routes per point the engine reserves for this map: the
+        block DDA cap ceil(2T / 8vs) * 4 plus 4, in float arithmetic as the
+        engine derives it (an engine's max_routes must be at least this)."""
+        f = np.float32
+        t2 = f(self.truncation_distance) * f(2.0)
+        bs = f(self.voxel_size) * f(8.0)
+        return int(np.ceil(t2 / bs) * f(4.0)) + 4
+
 
 @dataclass
 class ScanResult:
