@@ -1392,21 +1392,40 @@ __device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32],
   }
 }
 
+// A light segment's update entries, compacted (bounds the shared memory, so
+// more CTAs fit on an SM); a segment with more goes to the pass-based path.
+constexpr int kLightEntries = 1024;
+
+// Load the up to 31 entries of one routing record, eight in flight at a time,
+// and call f(k, entry) for each.
+template <typename F>
+__device__ __forceinline__ void for_record_entries(const uint2* e, int cnt, F f) {
+  for (int k0 = 0; k0 < cnt; k0 += 8) {
+    uint2 xs[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) xs[k] = k0 + k < cnt ? __ldg(e + k0 + k) : make_uint2(0u, kBadLocal);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k0 + k < cnt) f(k0 + k, xs[k]);
+  }
+}
+
 // The first hot_ctas CTAs (one per SM: blocks are dispatched in index order)
 // start with the hot chains, so the longest serial chains run from the start
 // of the kernel, beside the segment work of the other CTAs.
-__global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ctas) {
+__global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot_ctas) {
   __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
-  __shared__ __align__(16) float s_d[UPD_T * kUpdEntries];
-  __shared__ unsigned short s_l[UPD_T * kUpdEntries];
-  __shared__ unsigned short s_bin[UPD_T * kUpdEntries];
-  __shared__ unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];
+  __shared__ __align__(16) unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];  // hot-chain tiles before the loop
+  __shared__ float s_d[kLightEntries];
+  __shared__ unsigned short s_l[kLightEntries];
+  __shared__ int s_bin_run[kVoxelsPerBlock];  // light path: bins (ushort); pass-based path: per-voxel cursors
   __shared__ int s_off[kVoxelsPerBlock + 1];
-  __shared__ int s_run[kVoxelsPerBlock];
   __shared__ unsigned s_touch[kVoxelsPerBlock / 32];
   __shared__ int s_warp[32];
   __shared__ long long s_seg;
   __shared__ unsigned long long s_base;
+  unsigned short* s_bin = reinterpret_cast<unsigned short*>(s_bin_run);
+  int* s_run = s_bin_run;
   const BatchHdr h = *c.hdr;
   const int t = threadIdx.x;
   const long long nseg = c.ctr->n_seg;
@@ -1416,7 +1435,7 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned lt_bits = (1u << (t & 31)) - 1u;
   if ((int)blockIdx.x < hot_ctas) {
-    float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(s_d) + 2 * (t >> 5);
+    float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(&s_mask[0][0]) + 2 * (t >> 5);
     run_hot_chains(c, tile, t & 31);
     __syncthreads();
   }
@@ -1466,99 +1485,100 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
       nb1 = (sjn + 1 < nseg) ? c.seg_start[sjn + 1] : nrec;
     }
     unsigned n_upd = 0;
+    bool passes = heavy;
     if (!heavy) {
-      // ---- light path: the whole segment in one chunk
+      // ---- light path: the whole segment in one chunk, its entries
+      // compacted in shared memory at this record's offset
       for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
 #pragma unroll
         for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
       }
-      __syncthreads();
-      int ne = 0;
+      int cnt = 0;
+      unsigned ebase = 0;
       if (b0 + t < b1) {
         const unsigned v = rv[b0 + t];
-        const int cnt = (int)(v & 31u);
-        const uint2* e = c.entries + (v >> 5);
-        uint2 xs[kUpdEntries];
-#pragma unroll
-        for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
-#pragma unroll
-        for (int k = 0; k < kUpdEntries; ++k) {
-          const uint2 x = xs[k];
-          if (x.y == kBadLocal) continue;
-          s_d[t * kUpdEntries + ne] = __uint_as_float(x.x);
-          s_l[t * kUpdEntries + ne] = (unsigned short)x.y;
-          atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
-          ++ne;
+        cnt = (int)(v & 31u);
+        ebase = v >> 5;
+      }
+      int etot;
+      const int eoff = block_excl_scan(cnt, s_warp, &etot);  // its barriers also close the mask zeroing
+      if (etot > kLightEntries) {
+        passes = true;
+      } else {
+        for_record_entries(c.entries + ebase, cnt, [&](int k, uint2 x) {
+          s_d[eoff + k] = __uint_as_float(x.x);
+          s_l[eoff + k] = (unsigned short)x.y;
+          if (x.y != kBadLocal) {
+            atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
+            ++n_upd;
+          }
+        });
+        __syncthreads();
+        unsigned nrk = 0u, nrv = 0u;
+        if (nb0 >= 0) {
+          nrk = rk[nb0];
+          if (nb0 + t < nb1) nrv = rv[nb0 + t];
         }
-      }
-      n_upd += ne;
-      __syncthreads();
-      unsigned nrk = 0u, nrv = 0u;
-      if (nb0 >= 0) {
-        nrk = rk[nb0];
-        if (nb0 + t < nb1 && t < UPD_T) nrv = rv[nb0 + t];
-      }
-      {
-        int a[4];
+        {
+          int a[4];
 #pragma unroll
-        for (int qq = 0; qq < 4; ++qq) {
-          const int l = 4 * t + qq;
-          int cnt = 0;
+          for (int qq = 0; qq < 4; ++qq) {
+            const int l = 4 * t + qq;
+            int vc = 0;
 #pragma unroll
-          for (int w = 0; w < UPD_T / 32; ++w) cnt += __popc(s_mask[l][w]);
-          a[qq] = cnt;
+            for (int w = 0; w < UPD_T / 32; ++w) vc += __popc(s_mask[l][w]);
+            a[qq] = vc;
+          }
+          int tot;
+          int ex = block_excl_scan(a[0] + a[1] + a[2] + a[3], s_warp, &tot);
+          s_off[4 * t] = ex;
+          s_off[4 * t + 1] = ex + a[0];
+          s_off[4 * t + 2] = ex + a[0] + a[1];
+          s_off[4 * t + 3] = ex + a[0] + a[1] + a[2];
+          if (t == 0) s_off[kVoxelsPerBlock] = tot;
         }
-        int tot;
-        int ex = block_excl_scan(a[0] + a[1] + a[2] + a[3], s_warp, &tot);
-        s_off[4 * t] = ex;
-        s_off[4 * t + 1] = ex + a[0];
-        s_off[4 * t + 2] = ex + a[0] + a[1];
-        s_off[4 * t + 3] = ex + a[0] + a[1] + a[2];
-        if (t == 0) s_off[kVoxelsPerBlock] = tot;
-      }
-      __syncthreads();
-      if (nb0 >= 0) {
-        const float4* ngv = reinterpret_cast<const float4*>(c.voxels + (h.key_lo + nrk) * kVoxelsPerBlock);
-        prefetch_l1(ngv + t);
-        prefetch_l1(ngv + t + UPD_T);
-        if ((nrv & 31u) != 0u) {
-          const uint2* ne0 = c.entries + (nrv >> 5);
-          prefetch_l1(ne0);
-          prefetch_l1(ne0 + (nrv & 31u) - 1);
+        __syncthreads();
+        if (nb0 >= 0) {
+          const float4* ngv = reinterpret_cast<const float4*>(c.voxels + (h.key_lo + nrk) * kVoxelsPerBlock);
+          prefetch_l1(ngv + t);
+          prefetch_l1(ngv + t + UPD_T);
+          if ((nrv & 31u) != 0u) {
+            const uint2* ne0 = c.entries + (nrv >> 5);
+            prefetch_l1(ne0);
+            prefetch_l1(ne0 + (nrv & 31u) - 1);
+          }
         }
+        for (int k = 0; k < cnt; ++k) {
+          const int l = s_l[eoff + k];
+          if (l == (int)kBadLocal) continue;
+          int rank = __popc(s_mask[l][t >> 5] & lt_bits);
+          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+          s_bin[s_off[l] + rank] = (unsigned short)(eoff + k);
+        }
+        __syncthreads();
+        for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+          const int b = s_off[l], e = s_off[l + 1];
+          if (e == b) continue;
+          float sdf = s_vox[l].x, w = s_vox[l].y;
+          for (int a = b; a < e; ++a) update_voxel(&sdf, &w, s_d[s_bin[a]], maxw);
+          s_vox[l] = make_float2(sdf, w);
+          atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+        }
+        __syncthreads();
       }
-      for (int k = 0; k < ne; ++k) {
-        const int l = s_l[t * kUpdEntries + k];
-        int rank = __popc(s_mask[l][t >> 5] & lt_bits);
-        for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
-        s_bin[s_off[l] + rank] = (unsigned short)(t * kUpdEntries + k);
-      }
-      __syncthreads();
-      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-        const int b = s_off[l], e = s_off[l + 1];
-        if (e == b) continue;
-        float sdf = s_vox[l].x, w = s_vox[l].y;
-        for (int a = b; a < e; ++a) update_voxel(&sdf, &w, s_d[s_bin[a]], maxw);
-        s_vox[l] = make_float2(sdf, w);
-        atomicOr(&s_touch[l >> 5], 1u << (l & 31));
-      }
-      __syncthreads();
-    } else {
-      // ---- heavy segment beyond the planning capacity, pass 0: per-voxel
-      // update counts over all records
+    }
+    if (passes) {
+      // ---- a heavy segment beyond the counting sort's capacity, or a light
+      // one with more entries than the compacted arrays hold.  Pass 0:
+      // per-voxel update counts over all records
       for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_run[l] = 0;
       __syncthreads();
       for (long long cb = b0; cb < b1; cb += UPD_T) {
         if (cb + t < b1) {
           const unsigned v = rv[cb + t];
-          const int cnt = (int)(v & 31u);
-          const uint2* e = c.entries + (v >> 5);
-          uint2 xs[kUpdEntries];
-#pragma unroll
-          for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
-#pragma unroll
-          for (int k = 0; k < kUpdEntries; ++k)
-            if (xs[k].y != kBadLocal) atomicAdd(&s_run[xs[k].y], 1);
+          for_record_entries(c.entries + (v >> 5), (int)(v & 31u), [&](int, uint2 x) {
+            if (x.y != kBadLocal) atomicAdd(&s_run[x.y], 1);
+          });
         }
       }
       __syncthreads();
@@ -1580,45 +1600,37 @@ __global__ void __launch_bounds__(UPD_T) k_update(Ctx c, int rec_sel, int hot_ct
       const unsigned long long base = s_base;
       const bool fits = base + (unsigned long long)s_off[kVoxelsPerBlock] <= (unsigned long long)c.entry_cap;
       if (!fits && t == 0) set_error(c.ctr, ERR_CAPACITY);
-      // pass 1: ordered placement into the bins
+      // pass 1: ordered placement into the bins, one 128-record chunk at a
+      // time (masks give each entry's rank among the chunk's updates of its
+      // voxel; s_run carries the earlier chunks' counts)
       for (long long cb = b0; cb < b1 && fits; cb += UPD_T) {
         for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
 #pragma unroll
           for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
         }
         __syncthreads();
-        int ne = 0;
-        if (cb + t < b1) {
-          const unsigned v = rv[cb + t];
-          const int cnt = (int)(v & 31u);
-          const uint2* e = c.entries + (v >> 5);
-          uint2 xs[kUpdEntries];
-#pragma unroll
-          for (int k = 0; k < kUpdEntries; ++k) xs[k] = k < cnt ? __ldg(e + k) : make_uint2(0u, kBadLocal);
-#pragma unroll
-          for (int k = 0; k < kUpdEntries; ++k) {
-            const uint2 x = xs[k];
-            if (x.y == kBadLocal) continue;
-            s_d[t * kUpdEntries + ne] = __uint_as_float(x.x);
-            s_l[t * kUpdEntries + ne] = (unsigned short)x.y;
+        const unsigned v = cb + t < b1 ? rv[cb + t] : 0u;
+        const int cnt = cb + t < b1 ? (int)(v & 31u) : 0;
+        for_record_entries(c.entries + (v >> 5), cnt, [&](int, uint2 x) {
+          if (x.y != kBadLocal) {
             atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
-            ++ne;
+            ++n_upd;
           }
-        }
-        n_upd += ne;
+        });
         __syncthreads();
-        for (int k = 0; k < ne; ++k) {
-          const int l = s_l[t * kUpdEntries + k];
+        for_record_entries(c.entries + (v >> 5), cnt, [&](int, uint2 x) {
+          if (x.y == kBadLocal) return;
+          const int l = (int)x.y;
           int rank = __popc(s_mask[l][t >> 5] & lt_bits);
           for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
-          c.bin_d[base + s_off[l] + s_run[l] + rank] = s_d[t * kUpdEntries + k];
-        }
+          c.bin_d[base + s_off[l] + s_run[l] + rank] = __uint_as_float(x.x);
+        });
         __syncthreads();
         for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-          int cnt = 0;
+          int vc = 0;
 #pragma unroll
-          for (int w = 0; w < UPD_T / 32; ++w) cnt += __popc(s_mask[l][w]);
-          s_run[l] += cnt;
+          for (int w = 0; w < UPD_T / 32; ++w) vc += __popc(s_mask[l][w]);
+          s_run[l] += vc;
         }
         __syncthreads();
       }
