@@ -958,6 +958,28 @@ constexpr int UPD_T = 128;
 constexpr int kHotChain = 128;    // longer voxel chains of a heavy segment run as a warp each
 constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
+// Zero the 4 x 512 record masks (word-major), 16 bytes per store.
+__device__ __forceinline__ void zero_masks(unsigned* m, int t) {
+  uint4* v = reinterpret_cast<uint4*>(m);
+#pragma unroll
+  for (int i = 0; i < (UPD_T / 32) * kVoxelsPerBlock / 4 / UPD_T; ++i) v[t + i * UPD_T] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Update counts of voxels 4t..4t+3: popcounts of their four mask words, read
+// as one 16-byte load per word.
+__device__ __forceinline__ void mask_counts(const unsigned* m, int t, int a[4]) {
+  a[0] = a[1] = a[2] = a[3] = 0;
+#pragma unroll
+  for (int w = 0; w < UPD_T / 32; ++w) {
+    const uint4 x = reinterpret_cast<const uint4*>(m + w * kVoxelsPerBlock)[t];
+    a[0] += __popc(x.x);
+    a[1] += __popc(x.y);
+    a[2] += __popc(x.z);
+    a[3] += __popc(x.w);
+  }
+}
+
+
 // Per segment: its batch item (the scan of the entry of its first record) and,
 // for segments longer than one update chunk, a place on the heavy list.
 __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
@@ -1159,7 +1181,7 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c, int rec_s
 __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
   __shared__ float s_d[UPD_T * kUpdEntries];
   __shared__ unsigned short s_l[UPD_T * kUpdEntries];
-  __shared__ unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];
+  __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];  // word-major, as in k_update
   const int t = threadIdx.x;
   const unsigned lt_bits = (1u << (t & 31)) - 1u;
   const long long nch = c.ctr->n_hchunks;
@@ -1173,13 +1195,10 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
     const long long b0 = c.seg_start[j];
     const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
     const long long r0 = b0 + (gc - c.hchunk_base[h]) * UPD_T;
-    for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-#pragma unroll
-      for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
-    }
+    zero_masks(&s_mask[0][0], t);
     __syncthreads();
     const int ne = load_chunk_entries(c, rv, r0 + t, b1, s_d, s_l, t);
-    for (int k = 0; k < ne; ++k) atomicOr(&s_mask[s_l[t * kUpdEntries + k]][t >> 5], 1u << (t & 31));
+    for (int k = 0; k < ne; ++k) atomicOr(&s_mask[t >> 5][s_l[t * kUpdEntries + k]], 1u << (t & 31));
     __syncthreads();
     const int* hc = c.hcnt + gc * kVoxelsPerBlock;
     const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
@@ -1189,8 +1208,8 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
     const float maxw = c.maps[c.items[item].map].maxw;
     for (int k = 0; k < ne && fits; ++k) {
       const int l = s_l[t * kUpdEntries + k];
-      int rank = __popc(s_mask[l][t >> 5] & lt_bits);
-      for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+      int rank = __popc(s_mask[t >> 5][l] & lt_bits);
+      for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[w][l]);
       // getWeightUpdate (tsdf_handler.cu:579-581): w = 1/(|d|+1), and w d.
       // A voxel already at max_weight stays there (min(RN(max + w), max) =
       // max for w > 0), so its W' = RN(max + w) and 1/W' are known now.
@@ -1415,7 +1434,10 @@ __device__ __forceinline__ void for_record_entries(const uint2* e, int cnt, F f)
 // of the kernel, beside the segment work of the other CTAs.
 __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot_ctas) {
   __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
-  __shared__ __align__(16) unsigned s_mask[kVoxelsPerBlock][UPD_T / 32];  // hot-chain tiles before the loop
+  // record bit masks per voxel, word-major (word w covers records 32w..32w+31)
+  // so that 16-byte accesses of four consecutive voxels hit distinct banks;
+  // the hot-chain tiles live here before the segment loop
+  __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];
   __shared__ float s_d[kLightEntries];
   __shared__ unsigned short s_l[kLightEntries];
   __shared__ int s_bin_run[kVoxelsPerBlock];  // light path: bins (ushort); pass-based path: per-voxel cursors
@@ -1489,10 +1511,7 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
     if (!heavy) {
       // ---- light path: the whole segment in one chunk, its entries
       // compacted in shared memory at this record's offset
-      for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-#pragma unroll
-        for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
-      }
+      zero_masks(&s_mask[0][0], t);
       int cnt = 0;
       unsigned ebase = 0;
       if (b0 + t < b1) {
@@ -1509,7 +1528,7 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
           s_d[eoff + k] = __uint_as_float(x.x);
           s_l[eoff + k] = (unsigned short)x.y;
           if (x.y != kBadLocal) {
-            atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
+            atomicOr(&s_mask[t >> 5][x.y], 1u << (t & 31));
             ++n_upd;
           }
         });
@@ -1521,14 +1540,7 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
         }
         {
           int a[4];
-#pragma unroll
-          for (int qq = 0; qq < 4; ++qq) {
-            const int l = 4 * t + qq;
-            int vc = 0;
-#pragma unroll
-            for (int w = 0; w < UPD_T / 32; ++w) vc += __popc(s_mask[l][w]);
-            a[qq] = vc;
-          }
+          mask_counts(&s_mask[0][0], t, a);
           int tot;
           int ex = block_excl_scan(a[0] + a[1] + a[2] + a[3], s_warp, &tot);
           s_off[4 * t] = ex;
@@ -1551,8 +1563,8 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
         for (int k = 0; k < cnt; ++k) {
           const int l = s_l[eoff + k];
           if (l == (int)kBadLocal) continue;
-          int rank = __popc(s_mask[l][t >> 5] & lt_bits);
-          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+          int rank = __popc(s_mask[t >> 5][l] & lt_bits);
+          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[w][l]);
           s_bin[s_off[l] + rank] = (unsigned short)(eoff + k);
         }
         __syncthreads();
@@ -1604,16 +1616,13 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
       // time (masks give each entry's rank among the chunk's updates of its
       // voxel; s_run carries the earlier chunks' counts)
       for (long long cb = b0; cb < b1 && fits; cb += UPD_T) {
-        for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
-#pragma unroll
-          for (int w = 0; w < UPD_T / 32; ++w) s_mask[l][w] = 0;
-        }
+        zero_masks(&s_mask[0][0], t);
         __syncthreads();
         const unsigned v = cb + t < b1 ? rv[cb + t] : 0u;
         const int cnt = cb + t < b1 ? (int)(v & 31u) : 0;
         for_record_entries(c.entries + (v >> 5), cnt, [&](int, uint2 x) {
           if (x.y != kBadLocal) {
-            atomicOr(&s_mask[x.y][t >> 5], 1u << (t & 31));
+            atomicOr(&s_mask[t >> 5][x.y], 1u << (t & 31));
             ++n_upd;
           }
         });
@@ -1621,15 +1630,15 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
         for_record_entries(c.entries + (v >> 5), cnt, [&](int, uint2 x) {
           if (x.y == kBadLocal) return;
           const int l = (int)x.y;
-          int rank = __popc(s_mask[l][t >> 5] & lt_bits);
-          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[l][w]);
+          int rank = __popc(s_mask[t >> 5][l] & lt_bits);
+          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[w][l]);
           c.bin_d[base + s_off[l] + s_run[l] + rank] = __uint_as_float(x.x);
         });
         __syncthreads();
         for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
           int vc = 0;
 #pragma unroll
-          for (int w = 0; w < UPD_T / 32; ++w) vc += __popc(s_mask[l][w]);
+          for (int w = 0; w < UPD_T / 32; ++w) vc += __popc(s_mask[w][l]);
           s_run[l] += vc;
         }
         __syncthreads();
