@@ -126,16 +126,28 @@ typedef struct tsdf_scan {
   float origin[3];     /* sensor position in the same frame                  */
 } tsdf_scan;
 
+/* Output formats of the published voxels (tsdf_scan_result.pub_format). */
+#define TSDF_PUB_ARRAYS 0   /* pub_pos: 3 floats per voxel, pub_data: {sdf, weight} */
+#define TSDF_PUB_TSDF_MSG 1 /* pub_pos: a serialized tsdf_package_msgs/Tsdf message */
+/* Bytes of a serialized Tsdf message holding up to cap voxels: the 4-byte CDR
+ * encapsulation (little endian), uint32 size, uint32 sequence length, cap
+ * Voxel records {sdf, weight, x, y, z} (float32 each), float32
+ * truncation_distance, float32 voxel_size (Tsdf.msg, Voxel.msg). */
+#define TSDF_MSG_BYTES(cap) (20 + 20 * (int64_t)(cap))
+
 /* Where one scan's published voxels go.  Pointers may be host (pinned or
  * pageable) or device memory; pinned and device buffers are written by the
- * publish kernel directly. */
+ * publish kernel directly.  With pub_format TSDF_PUB_TSDF_MSG, pub_pos is a
+ * pinned or device buffer of TSDF_MSG_BYTES(pub_cap) bytes that receives the
+ * message (pub_data is unused): the publish kernel writes the voxel records,
+ * the engine the header and trailer, min(count, pub_cap) voxels in all. */
 typedef struct tsdf_scan_result {
-  float* pub_pos;          /* 3 floats per voxel (Vector3f)                  */
+  float* pub_pos;          /* 3 floats per voxel (Vector3f), or the message  */
   tsdf_voxel* pub_data;    /* sdf, weight per voxel                          */
   int64_t pub_cap;         /* capacity of both arrays, in voxels             */
   int64_t pub_count;       /* out: full count                                */
   int status;              /* out: tsdf_status of this scan                  */
-  int reserved;
+  int pub_format;          /* TSDF_PUB_ARRAYS (0) or TSDF_PUB_TSDF_MSG       */
   tsdf_scan_stats stats;   /* out                                            */
 } tsdf_scan_result;
 
@@ -230,6 +242,33 @@ tsdf_status tsdf_dump_blocks(tsdf_engine* eng, int map_id, int32_t* kxyz, int32_
 tsdf_status tsdf_dump_free_list(tsdf_engine* eng, int map_id, int32_t* out, int64_t cap, int64_t* block_count);
 /* The 512 voxels of one heap slot. */
 tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, tsdf_voxel* out512);
+
+/* Map snapshot and restore.  The reference has neither (its one map lives and
+ * dies with the process); they let a serving loop evict a map and admit it
+ * again later.  A snapshot is a little-endian byte image: a 64-byte header
+ * (tsdf_snapshot_header), the free-block stack (heap_blocks int32), then for
+ * the heap slots below the high-water mark their block keys (uint64, packed
+ * 21-bit coordinates, all ones when free), non-zero voxel counts (int32) and
+ * voxels (512 tsdf_voxel each).  The map must be idle (no scan in flight or
+ * queued).  out may be host or device memory; with out == NULL or cap too
+ * small *bytes receives the size needed (TSDF_ERR_CAPACITY when cap is too
+ * small). */
+typedef struct tsdf_snapshot_header {
+  char magic[8];              /* "TSDFSNP1" */
+  uint32_t version;           /* 1 */
+  uint32_t header_bytes;      /* 64 */
+  tsdf_params params;
+  int32_t block_count;        /* allocated blocks */
+  int64_t heap_blocks;        /* heap slots of the map */
+  int32_t high_water;         /* slots [0, high_water) follow */
+  int32_t reserved[3];
+} tsdf_snapshot_header;
+tsdf_status tsdf_map_snapshot(tsdf_engine* eng, int map_id, void* out, int64_t cap, int64_t* bytes);
+/* Restore a snapshot into a new map (admitted like tsdf_map_create; heap_blocks
+ * 0 = the snapshot's, otherwise at least the snapshot's).  The new map gives
+ * the same results as the original on every later scan. */
+tsdf_status tsdf_map_restore(tsdf_engine* eng, const void* snapshot, int64_t bytes, int64_t heap_blocks,
+                             int* map_id);
 
 /* Device self-check of the voxel-update arithmetic: n seeded operand pairs,
  * the engine's division (correction step from a correctly rounded

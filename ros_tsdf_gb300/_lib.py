@@ -19,6 +19,14 @@ ERR_BUSY = 8
 ERR_NOT_READY = 9
 ERR_BAD_POINTS = 10
 
+PUB_ARRAYS = 0
+PUB_TSDF_MSG = 1
+
+
+def tsdf_msg_bytes(cap: int) -> int:
+    """TSDF_MSG_BYTES: size of a serialized Tsdf message of up to cap voxels."""
+    return 20 + 20 * int(cap)
+
 STATUS_NAMES = {
     0: "OK", 1: "INVALID_ARG", 2: "HEAP_FULL", 3: "PUBLISH_OVERFLOW", 4: "CUDA", 5: "CAPACITY",
     6: "SPIN_LIMIT", 7: "HASH_FULL", 8: "BUSY", 9: "NOT_READY", 10: "BAD_POINTS",
@@ -57,7 +65,13 @@ class Scan(C.Structure):
 
 class ScanResult(C.Structure):
     _fields_ = [("pub_pos", C.c_void_p), ("pub_data", C.c_void_p), ("pub_cap", C.c_int64),
-                ("pub_count", C.c_int64), ("status", C.c_int), ("reserved", C.c_int), ("stats", ScanStats)]
+                ("pub_count", C.c_int64), ("status", C.c_int), ("pub_format", C.c_int), ("stats", ScanStats)]
+
+
+class SnapshotHeader(C.Structure):
+    _fields_ = [("magic", C.c_char * 8), ("version", C.c_uint32), ("header_bytes", C.c_uint32), ("params", Params),
+                ("block_count", C.c_int32), ("heap_blocks", C.c_int64), ("high_water", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
 
 
 class MapInfo(C.Structure):
@@ -91,6 +105,8 @@ SIGNATURES = [
     ("tsdf_dump_blocks", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_free_list", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_block_voxels", C.c_int, [C.c_void_p, C.c_int, C.c_int32, C.c_void_p]),
+    ("tsdf_map_snapshot", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    ("tsdf_map_restore", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(C.c_int)]),
     ("tsdf_check_division", C.c_int, [C.c_void_p, C.c_uint64, C.c_int64, C.POINTER(C.c_int64),
                                       C.POINTER(C.c_float)]),
     ("tsdf_set_stage_timing", C.c_int, [C.c_void_p, C.c_int]),

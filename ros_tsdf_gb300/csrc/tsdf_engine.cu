@@ -438,7 +438,8 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
       return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id " + std::to_string(s.map_id));
     if (s.n_points < 0 || (s.n_points > 0 && !s.xyz)) return fail(eng, TSDF_ERR_INVALID_ARG, "bad point array");
     if (s.stride_bytes < 12 || (s.stride_bytes & 3)) return fail(eng, TSDF_ERR_INVALID_ARG, "stride must be >= 12, multiple of 4");
-    if (!res[i].pub_pos || !res[i].pub_data) {
+    const bool msg_out = res[i].pub_format == TSDF_PUB_TSDF_MSG;
+    if (!res[i].pub_pos || (!msg_out && !res[i].pub_data)) {
       if (res[i].pub_cap > 0) return fail(eng, TSDF_ERR_INVALID_ARG, "null publish arrays");
     }
     for (int j = 0; j < i; ++j)
@@ -471,7 +472,9 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     } else if (device_resident(s.xyz, &dp)) {
       it.pts = (const char*)dp;
     } else {
-      long long nb = s.n_points * (long long)s.stride_bytes;
+      // the bytes the points span: a strided view into wider records (a
+      // PointCloud2 buffer) ends 12 bytes into its last record
+      long long nb = (s.n_points - 1) * (long long)s.stride_bytes + 12;
       if (bytes + nb > c.max_batch_points * 16) return fail(eng, TSDF_ERR_CAPACITY, "point staging full");
       CK(cudaMemcpyAsync(L.d_points + bytes, s.xyz, nb, cudaMemcpyHostToDevice, L.stream));
       it.pts = L.d_points + bytes;
@@ -481,7 +484,15 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     const void* pp = nullptr;
     const void* pd = nullptr;
     it.out_cap = std::max<long long>(res[i].pub_cap, 0);
-    if (it.out_cap > 0 && device_accessible(res[i].pub_pos, &pp) && device_accessible(res[i].pub_data, &pd)) {
+    it.out_fmt = res[i].pub_format;
+    if (it.out_fmt == TSDF_PUB_TSDF_MSG) {
+      if (it.out_cap > 0 && !device_accessible(res[i].pub_pos, &pp))
+        return fail(eng, TSDF_ERR_INVALID_ARG, "a Tsdf message output needs a pinned or device buffer");
+      it.out_pos = (float*)pp;
+      it.out_data = nullptr;
+    } else if (it.out_fmt != TSDF_PUB_ARRAYS) {
+      return fail(eng, TSDF_ERR_INVALID_ARG, "unknown pub_format");
+    } else if (it.out_cap > 0 && device_accessible(res[i].pub_pos, &pp) && device_accessible(res[i].pub_data, &pd)) {
       it.out_pos = (float*)pp;
       it.out_data = (float2*)pd;
     } else {
@@ -566,6 +577,20 @@ tsdf_status finish_batch(tsdf_engine* eng, Lane& L, int n, tsdf_scan_result* res
     else if (st[ST_BAD] > 0)
       s = TSDF_ERR_BAD_POINTS;
     res[i].status = s;
+  }
+  // Tsdf messages: header (encapsulation, size, sequence length) and
+  // trailer (truncation_distance, voxel_size) around the kernel's records
+  for (int i = 0; i < n; ++i) {
+    if (res[i].pub_format != TSDF_PUB_TSDF_MSG || res[i].pub_cap <= 0) continue;
+    const uint32_t k = (uint32_t)std::min<long long>(counts[i], res[i].pub_cap);
+    unsigned char head[12] = {0x00, 0x01, 0x00, 0x00};
+    std::memcpy(head + 4, &k, 4);
+    std::memcpy(head + 8, &k, 4);
+    const tsdf_params& pr = eng->maps[L.maps[i]].params;
+    float tail[2] = {pr.truncation_distance, pr.voxel_size};
+    char* msg = reinterpret_cast<char*>(res[i].pub_pos);
+    CK(cudaMemcpy(msg, head, sizeof(head), cudaMemcpyDefault));
+    CK(cudaMemcpy(msg + 12 + 20ll * k, tail, sizeof(tail), cudaMemcpyDefault));
   }
   for (const auto& sg : L.staged) {
     long long k = std::min<long long>(counts[sg.item], res[sg.item].pub_cap);
@@ -929,6 +954,123 @@ tsdf_status tsdf_map_destroy(tsdf_engine* eng, int map_id) {
   eng->heap_ranges.release(m.dev.heap_base, m.dev.heap_cap);
   eng->hash_ranges.release(m.dev.hash_base, m.hash_entries);
   m = MapHost();
+  return TSDF_OK;
+}
+
+static_assert(sizeof(tsdf_snapshot_header) == 64, "snapshot header layout");
+static_assert(kPubTsdfMsg == TSDF_PUB_TSDF_MSG, "output format ids");
+
+namespace {
+
+bool map_idle(tsdf_engine* eng, int map_id) {
+  if (eng->maps[map_id].in_flight) return false;
+  for (auto& r : eng->queue)
+    if (r->scan.map_id == map_id) return false;
+  return true;
+}
+
+// byte offsets of the snapshot sections
+struct SnapLayout {
+  long long free_off, key_off, nnz_off, vox_off, total;
+};
+
+SnapLayout snap_layout(long long heap_blocks, long long hw) {
+  SnapLayout l;
+  l.free_off = sizeof(tsdf_snapshot_header);
+  l.key_off = l.free_off + ((heap_blocks * 4 + 7) & ~7ll);
+  l.nnz_off = l.key_off + hw * 8;
+  l.vox_off = l.nnz_off + ((hw * 4 + 15) & ~15ll);
+  l.total = l.vox_off + hw * (long long)kVoxelsPerBlock * 8;
+  return l;
+}
+
+}  // namespace
+
+tsdf_status tsdf_map_snapshot(tsdf_engine* eng, int map_id, void* out, int64_t cap, int64_t* bytes) {
+  if (!eng || !bytes) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  if (!map_idle(eng, map_id)) return fail(eng, TSDF_ERR_BUSY, "map has a scan in flight or queued");
+  CK(cudaSetDevice(eng->device));
+  const MapHost& m = eng->maps[map_id];
+  MapCounters mc;
+  CK(cudaMemcpy(&mc, eng->d_mctr + map_id, sizeof(mc), cudaMemcpyDeviceToHost));
+  const SnapLayout lay = snap_layout(m.dev.heap_cap, mc.hw);
+  *bytes = lay.total;
+  if (!out) return TSDF_OK;
+  if (cap < lay.total) return fail(eng, TSDF_ERR_CAPACITY, "snapshot buffer too small");
+  tsdf_snapshot_header hd;
+  std::memset(&hd, 0, sizeof(hd));
+  std::memcpy(hd.magic, "TSDFSNP1", 8);
+  hd.version = 1;
+  hd.header_bytes = sizeof(hd);
+  hd.params = m.params;
+  hd.block_count = mc.block_count;
+  hd.heap_blocks = m.dev.heap_cap;
+  hd.high_water = mc.hw;
+  char* o = static_cast<char*>(out);
+  CK(cudaMemcpy(o, &hd, sizeof(hd), cudaMemcpyDefault));
+  CK(cudaMemcpy(o + lay.free_off, eng->free_list + m.dev.heap_base, sizeof(int) * m.dev.heap_cap, cudaMemcpyDefault));
+  if (mc.hw > 0) {
+    CK(cudaMemcpy(o + lay.key_off, eng->slot_key + m.dev.heap_base, 8ll * mc.hw, cudaMemcpyDefault));
+    CK(cudaMemcpy(o + lay.nnz_off, eng->nnz + m.dev.heap_base, 4ll * mc.hw, cudaMemcpyDefault));
+    CK(cudaMemcpy(o + lay.vox_off, eng->voxels + m.dev.heap_base * kVoxelsPerBlock,
+                  8ll * kVoxelsPerBlock * mc.hw, cudaMemcpyDefault));
+  }
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_map_restore(tsdf_engine* eng, const void* snapshot, int64_t bytes, int64_t heap_blocks,
+                             int* map_id) {
+  if (!eng || !snapshot || !map_id) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  CK(cudaSetDevice(eng->device));
+  if (bytes < (int64_t)sizeof(tsdf_snapshot_header)) return fail(eng, TSDF_ERR_INVALID_ARG, "snapshot too short");
+  tsdf_snapshot_header hd;
+  CK(cudaMemcpy(&hd, snapshot, sizeof(hd), cudaMemcpyDefault));
+  if (std::memcmp(hd.magic, "TSDFSNP1", 8) != 0 || hd.version != 1 || hd.header_bytes != sizeof(hd))
+    return fail(eng, TSDF_ERR_INVALID_ARG, "not a version-1 map snapshot");
+  if (hd.heap_blocks <= 0 || hd.high_water < 0 || hd.high_water > hd.heap_blocks || hd.block_count < 0 ||
+      hd.block_count > hd.high_water)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "snapshot header out of range");
+  const SnapLayout lay = snap_layout(hd.heap_blocks, hd.high_water);
+  if (bytes < lay.total) return fail(eng, TSDF_ERR_INVALID_ARG, "snapshot truncated");
+  if (heap_blocks == 0) heap_blocks = hd.heap_blocks;
+  if (heap_blocks < hd.heap_blocks) return fail(eng, TSDF_ERR_INVALID_ARG, "heap_blocks below the snapshot's");
+  int id = -1;
+  TRY(tsdf_map_create(eng, &hd.params, heap_blocks, &id));
+  MapHost& m = eng->maps[id];
+  const char* in = static_cast<const char*>(snapshot);
+  Lane& L = eng->lanes[0];
+  // slots past the snapshot's heap keep the fresh map's identity free list
+  CK(cudaMemcpyAsync(eng->free_list + m.dev.heap_base, in + lay.free_off, 4ll * hd.heap_blocks, cudaMemcpyDefault,
+                     L.stream));
+  const long long hw = hd.high_water;
+  if (hw > 0) {
+    CK(cudaMemcpyAsync(eng->slot_key + m.dev.heap_base, in + lay.key_off, 8ll * hw, cudaMemcpyDefault, L.stream));
+    CK(cudaMemcpyAsync(eng->nnz + m.dev.heap_base, in + lay.nnz_off, 4ll * hw, cudaMemcpyDefault, L.stream));
+    CK(cudaMemcpyAsync(eng->voxels + m.dev.heap_base * kVoxelsPerBlock, in + lay.vox_off,
+                       8ll * kVoxelsPerBlock * hw, cudaMemcpyDefault, L.stream));
+  }
+  // hash table from the live keys (the same kernel that rebuilds a table
+  // crowded with tombstones)
+  CK(cudaMemsetAsync(eng->d_tmp + 1, 0, sizeof(int), L.stream));
+  launch_map_rehash(L.ctx, id, eng->cfg.bucket_size, m.dev.heap_base, hw, m.dev.hash_base, m.hash_entries,
+                    m.dev.hash_mask, eng->d_tmp, eng->d_tmp + 1, L.stream);
+  MapCounters mc{};
+  mc.block_count = hd.block_count;
+  mc.hw = (int)hw;
+  CK(cudaMemcpyAsync(eng->d_mctr + id, &mc, sizeof(mc), cudaMemcpyHostToDevice, L.stream));
+  CK(cudaMemcpyAsync(&eng->d_mctr[id].hash_used, eng->d_tmp, sizeof(int), cudaMemcpyDeviceToDevice, L.stream));
+  int host[2] = {0, 0};
+  CK(cudaMemcpyAsync(host, eng->d_tmp, sizeof(int) * 2, cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  if (host[1]) {
+    tsdf_map_destroy(eng, id);
+    return fail(eng, TSDF_ERR_HASH_FULL, "restore: hash table full");
+  }
+  *map_id = id;
   return TSDF_OK;
 }
 

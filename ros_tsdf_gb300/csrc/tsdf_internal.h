@@ -18,6 +18,7 @@ constexpr unsigned kRecSentinel = 0xFFFFFFFFu;
 constexpr int kRadixBits = 8;
 constexpr int kMaxRadixPasses = 4;
 constexpr int kUpdEntries = 24;        // voxel updates of one point inside one block (<= 3*7+1 = 22)
+constexpr int kPubTsdfMsg = 1;            // ItemDev::out_fmt of a serialized Tsdf message (TSDF_PUB_TSDF_MSG)
 constexpr unsigned kBadLocal = 0xFFFFu;  // entry whose local voxel index fell outside its block
 
 // One hash entry: packed block key, logical heap slot, first-touch rank.
@@ -60,7 +61,7 @@ struct ItemDev {
   float ox, oy, oz;
   int stride;
   int map;
-  int pad;
+  int out_fmt;            // TSDF_PUB_ARRAYS, or TSDF_PUB_TSDF_MSG: out_pos holds the message bytes
   float* out_pos;         // published positions (device-accessible) or null
   float2* out_data;       // published voxels (device-accessible)
   long long out_cap;

@@ -1897,7 +1897,7 @@ __global__ void __launch_bounds__(1024) k_item_bases(Ctx c, const int* prefix, c
 // (getVoxelCoordinatesFromLocalVoxelIndex, tsdf_handler.cu:520-534)
 __global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
   __shared__ int s_sb[kMaxItems];
-  __shared__ float s_pos[256 / 32][96];  // a warp's compacted positions of one round
+  __shared__ float s_pos[256 / 32][160];  // a warp's compacted output words of one round
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
@@ -1922,6 +1922,7 @@ __global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
     const float blz = fsub(fadd(div_const((float)kz, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
     long long out = (long long)c.pub_prefix[e] - c.item_i[item * II_COUNT + II_PUB_BASE];
     float* sp = s_pos[threadIdx.x >> 5];
+    const bool msg = it.out_fmt == kPubTsdfMsg;
 #pragma unroll
     for (int r = 0; r < kVoxelsPerBlock / 32; ++r) {
       const int l = r * 32 + lane;
@@ -1932,17 +1933,35 @@ __global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
       if (nzv) {
         const int rank = __popc(bm & lt_mask);
         const float x = (float)(l & 7), y = (float)((l >> 3) & 7), z = (float)(l >> 6);
-        sp[3 * rank + 0] = fadd(fadd(fmul(x, m.vs), m.half_vs), blx);
-        sp[3 * rank + 1] = fadd(fadd(fmul(y, m.vs), m.half_vs), bly);
-        sp[3 * rank + 2] = fadd(fadd(fmul(z, m.vs), m.half_vs), blz);
-        if (out + rank < it.out_cap) it.out_data[out + rank] = v[r];
+        const float px = fadd(fadd(fmul(x, m.vs), m.half_vs), blx);
+        const float py = fadd(fadd(fmul(y, m.vs), m.half_vs), bly);
+        const float pz = fadd(fadd(fmul(z, m.vs), m.half_vs), blz);
+        if (msg) {
+          // Voxel.msg record: sdf, weight, x, y, z
+          sp[5 * rank + 0] = v[r].x;
+          sp[5 * rank + 1] = v[r].y;
+          sp[5 * rank + 2] = px;
+          sp[5 * rank + 3] = py;
+          sp[5 * rank + 4] = pz;
+        } else {
+          sp[3 * rank + 0] = px;
+          sp[3 * rank + 1] = py;
+          sp[3 * rank + 2] = pz;
+          if (out + rank < it.out_cap) it.out_data[out + rank] = v[r];
+        }
       }
       __syncwarp();
-      // positions leave as consecutive words: every store instruction of the
+      // outputs leave as consecutive words: every store instruction of the
       // warp covers one contiguous range (host memory over the C2C link
       // takes strided 12-byte records at a third of the rate)
-      for (int j = lane; j < 3 * cnt; j += 32)
-        if (out + j / 3 < it.out_cap) it.out_pos[3 * out + j] = sp[j];
+      if (msg) {
+        float* rec = it.out_pos + 3;  // after the 12-byte message header
+        for (int j = lane; j < 5 * cnt; j += 32)
+          if (out + j / 5 < it.out_cap) rec[5 * out + j] = sp[j];
+      } else {
+        for (int j = lane; j < 3 * cnt; j += 32)
+          if (out + j / 3 < it.out_cap) it.out_pos[3 * out + j] = sp[j];
+      }
       __syncwarp();
       out += cnt;
     }

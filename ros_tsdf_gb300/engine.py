@@ -56,6 +56,13 @@ class ScanResult:
 
 
 def _as_points(xyz) -> tuple[np.ndarray, int]:
+    """Points as (array, stride in bytes).  A float32 (N, 3) view whose rows
+    are strided through wider records (pointcloud2.xyz_view of a PointCloud2
+    buffer) passes as it is: the engine copies the raw records and reads x,
+    y, z at the stride on the device."""
+    if (isinstance(xyz, np.ndarray) and xyz.dtype == np.float32 and xyz.ndim == 2 and xyz.shape[1] == 3
+            and xyz.strides[1] == 4 and xyz.strides[0] >= 12 and xyz.strides[0] % 4 == 0):
+        return xyz, xyz.strides[0]
     a = np.ascontiguousarray(xyz, dtype=np.float32)
     if a.ndim != 2 or a.shape[1] not in (3, 4):
         raise ValueError("points must be (N, 3) or (N, 4) float32")
@@ -114,6 +121,23 @@ class Engine:
     def destroy_map(self, map_id: int):
         self._check(self.lib.tsdf_map_destroy(self.h, int(map_id)), "tsdf_map_destroy")
 
+    def snapshot(self, map_id: int) -> np.ndarray:
+        """The map's state as a byte image (tsdf_map_snapshot)."""
+        n = C.c_int64()
+        self._check(self.lib.tsdf_map_snapshot(self.h, int(map_id), None, 0, C.byref(n)), "tsdf_map_snapshot")
+        buf = np.empty(n.value, np.uint8)
+        self._check(self.lib.tsdf_map_snapshot(self.h, int(map_id), buf.ctypes.data, buf.size, C.byref(n)),
+                    "tsdf_map_snapshot")
+        return buf
+
+    def restore(self, snapshot: np.ndarray, heap_blocks: int = 0) -> int:
+        """A new map from a snapshot (tsdf_map_restore); returns its id."""
+        a = np.ascontiguousarray(snapshot, np.uint8)
+        mid = C.c_int()
+        self._check(self.lib.tsdf_map_restore(self.h, a.ctypes.data, a.size, int(heap_blocks), C.byref(mid)),
+                    "tsdf_map_restore")
+        return mid.value
+
     def map_info(self, map_id: int) -> dict:
         mi = L.MapInfo()
         self._check(self.lib.tsdf_map_info_get(self.h, int(map_id), C.byref(mi)), "tsdf_map_info_get")
@@ -122,6 +146,30 @@ class Engine:
     # -- integration --------------------------------------------------------
     def integrate(self, map_id: int, xyz, origin, pub_cap: int = 400000) -> ScanResult:
         return self.integrate_batch([(map_id, xyz, origin)], pub_cap=pub_cap)[0]
+
+    def integrate_msg(self, map_id: int, xyz, origin, pub_cap: int = 400000) -> tuple[np.ndarray, ScanResult]:
+        """One scan whose published voxels come back as a serialized
+        tsdf_package_msgs/Tsdf message (TSDF_PUB_TSDF_MSG), written into a
+        pinned buffer by the publish kernel; returns (message bytes, result
+        with the counts and stats)."""
+        a, stride = _as_points(xyz)
+        sc = L.Scan()
+        sc.map_id = int(map_id)
+        sc.stride_bytes = stride
+        sc.n_points = a.shape[0]
+        sc.xyz = a.ctypes.data if a.shape[0] else None
+        sc.origin[:] = [float(v) for v in origin]
+        buf = self.pinned_empty((L.tsdf_msg_bytes(pub_cap),), np.uint8)
+        rs = L.ScanResult()
+        rs.pub_pos = buf.ctypes.data
+        rs.pub_data = None
+        rs.pub_cap = int(pub_cap)
+        rs.pub_format = L.PUB_TSDF_MSG
+        st = self.lib.tsdf_integrate_batch(self.h, 1, C.byref(sc), C.byref(rs))
+        self._check(st, "tsdf_integrate_batch", soft=True)
+        k = min(rs.pub_count, rs.pub_cap)
+        return buf[:L.tsdf_msg_bytes(k)], ScanResult(None, None, int(rs.pub_count), int(rs.status),
+                                                     rs.stats.to_dict())
 
     def integrate_batch(self, scans, pub_cap=400000, outputs=None) -> list[ScanResult]:
         """scans: list of (map_id, points (N,3|4) float32, origin (3,)).

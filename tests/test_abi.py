@@ -43,7 +43,8 @@ def test_struct_layouts_match_header(tmp_path):
     from ros_tsdf_gb300 import _lib as L
 
     structs = {"tsdf_params": L.Params, "tsdf_engine_cfg": L.EngineCfg, "tsdf_scan_stats": L.ScanStats,
-               "tsdf_scan": L.Scan, "tsdf_scan_result": L.ScanResult, "tsdf_map_info": L.MapInfo}
+               "tsdf_scan": L.Scan, "tsdf_scan_result": L.ScanResult, "tsdf_map_info": L.MapInfo,
+               "tsdf_snapshot_header": L.SnapshotHeader}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tsdf_c.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -102,3 +102,35 @@ def test_poisson_trace_is_seeded_and_sorted():
     for r in a:
         per.setdefault(r.client, []).append(r.scan)
     assert all(v == [k % 6 for k in range(len(v))] for v in per.values())
+
+
+def test_pointcloud2_view_and_tsdf_message_layout():
+    import struct
+
+    from ros_tsdf_gb300 import pointcloud2 as P
+    from ros_tsdf_gb300.engine import _as_points
+
+    n = 7
+    rec = np.zeros((n, 6), np.float32)  # point_step 24: x at byte 4
+    rec[:, 1:4] = np.arange(3 * n, dtype=np.float32).reshape(n, 3)
+    f = [P.PointField("x", 4, P.FLOAT32), P.PointField("y", 8, P.FLOAT32), P.PointField("z", 12, P.FLOAT32)]
+    v = P.xyz_view(rec.tobytes(), f, 24, n)
+    assert v.shape == (n, 3) and np.array_equal(v, rec[:, 1:4])
+    arr, stride = _as_points(v)
+    assert stride == 24 and arr.ctypes.data == v.ctypes.data  # no copy
+    # padded rows fall back to a packed copy
+    rows = np.zeros((2, 4 * 24 + 8), np.uint8)
+    for r in range(2):
+        part = rec[:4] if r == 0 else np.concatenate([rec[4:], rec[:1]])
+        rows[r, :96] = np.frombuffer(part.tobytes(), np.uint8)
+    w = P.xyz_view(rows.tobytes(), f, 24, 4, height=2, row_step=104)
+    assert w.shape == (8, 3) and np.array_equal(w[:4], rec[:4, 1:4])
+    with pytest.raises(ValueError):
+        P.xyz_view(rec.tobytes(), [P.PointField("x", 4, P.FLOAT64)] + f[1:], 24, n)
+    pos = np.arange(6, dtype=np.float32).reshape(2, 3)
+    dat = np.array([[0.5, 3.0], [-0.25, 1.0]], np.float32)
+    m = P.encode_tsdf_msg(pos, dat, 0.4, 0.1)
+    assert len(m) == 20 + 40 and m[:4] == b"\x00\x01\x00\x00" and struct.unpack_from("<II", m, 4) == (2, 2)
+    assert struct.unpack_from("<5f", m, 12) == (0.5, 3.0, 0.0, 1.0, 2.0)
+    d = P.decode_tsdf_msg(m)
+    assert np.array_equal(d["pos"], pos) and np.array_equal(d["data"], dat)

@@ -414,3 +414,77 @@ def test_autotune_choice_keeps_parity(built, tmp_path):
                 assert_scan_equal(r, orc.integrate(*scans[m][k], pub_cap=1 << 18), spec.params.truncation_distance,
                                   f"map {m} scan {k}")
             assert_state_equal(eng, mid, orc, spec.heap_blocks)
+
+
+def test_snapshot_restore_continues_identically(built):
+    """A map restored from its snapshot (same engine, and a fresh engine with
+    a larger heap) gives the same results as the original on later scans,
+    and both match the oracle that never stopped."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = _mixed_specs()[0]
+    src = W.ScanSource(spec)
+    scans = [src.scan(k) for k in range(6)]
+    orc = _oracle(spec.params, spec.heap_blocks)
+    T = spec.params.truncation_distance
+    with Engine(max_maps=4, pool_blocks=3 * spec.heap_blocks, max_batch_points=1 << 18) as eng, \
+            Engine(max_maps=2, pool_blocks=2 * spec.heap_blocks + 64, max_batch_points=1 << 18, bucket_size=4) as eng2:
+        a = eng.create_map(spec.params, spec.heap_blocks)
+        for k in range(3):
+            assert_scan_equal(eng.integrate(a, *scans[k], pub_cap=1 << 20), orc.integrate(*scans[k], pub_cap=1 << 20),
+                              T, f"scan {k}")
+        snap = eng.snapshot(a)
+        b = eng.restore(snap)
+        c = eng2.restore(snap, heap_blocks=spec.heap_blocks + 64)
+        assert_state_equal(eng, b, orc, spec.heap_blocks)
+        for k in range(3, 6):
+            want = orc.integrate(*scans[k], pub_cap=1 << 20)
+            for e, mid in ((eng, a), (eng, b), (eng2, c)):
+                assert_scan_equal(e.integrate(mid, *scans[k], pub_cap=1 << 20), want, T, f"scan {k} map {mid}")
+        assert_state_equal(eng, a, orc, spec.heap_blocks)
+        assert_state_equal(eng, b, orc, spec.heap_blocks)
+        # a corrupted snapshot is refused, not restored
+        bad = snap.copy()
+        bad[:8] = 0
+        with pytest.raises(Exception):
+            eng.restore(bad)
+
+
+def test_pointcloud2_records_and_tsdf_message(built):
+    """PointCloud2-style records (x, y, z at byte 8 of 32-byte points, NaN
+    rows for rays without a return) integrate exactly like the packed points;
+    the Tsdf message written by the publish kernel holds the same voxels as
+    the array output, with its header and trailer."""
+    from ros_tsdf_gb300 import Engine, pointcloud2 as P, workloads as W
+
+    spec = W.plain_small(seed=3, heap_blocks=1 << 13)
+    src = W.ScanSource(spec)
+    fields = [P.PointField("t", 0, P.FLOAT64), P.PointField("x", 8, P.FLOAT32), P.PointField("y", 12, P.FLOAT32),
+              P.PointField("z", 16, P.FLOAT32), P.PointField("intensity", 20, P.FLOAT32)]
+    with Engine(max_maps=4, pool_blocks=4 << 13, max_batch_points=1 << 16) as eng:
+        a = eng.create_map(spec.params, spec.heap_blocks)
+        b = eng.create_map(spec.params, spec.heap_blocks)
+        c = eng.create_map(spec.params, spec.heap_blocks)
+        for k in range(4):
+            xyz, org = src.scan(k)
+            rec = np.zeros((xyz.shape[0] + 5, 8), np.float32)
+            rec[:-5, 2:5] = xyz
+            rec[-5:, 2:5] = np.nan
+            view = P.xyz_view(rec.tobytes(), fields, 32, rec.shape[0])
+            ra = eng.integrate(a, xyz, org, pub_cap=1 << 16)
+            rb = eng.integrate(b, view, org, pub_cap=1 << 16)
+            assert rb.stats["bad_points"] == 5
+            assert ra.count == rb.count and np.array_equal(ra.pos, rb.pos) and np.array_equal(ra.data, rb.data)
+            cap = (1 << 16) if k < 3 else max(ra.count // 2, 1)
+            msg, rc = eng.integrate_msg(c, xyz, org, pub_cap=cap)
+            d = P.decode_tsdf_msg(msg)
+            kk = min(ra.count, cap)
+            assert rc.count == ra.count and d["size"] == kk and msg.size == P_bytes(kk)
+            assert np.array_equal(d["pos"], ra.pos[:kk]) and np.array_equal(d["data"], ra.data[:kk])
+            assert d["truncation_distance"] == np.float32(spec.params.truncation_distance)
+            assert d["voxel_size"] == np.float32(spec.params.voxel_size)
+        assert np.array_equal(eng.dump_blocks(a)[0], eng.dump_blocks(b)[0])
+
+
+def P_bytes(k):
+    return 20 + 20 * k
