@@ -42,7 +42,7 @@ constexpr int kMaxLanes = 4;
 constexpr long long kFlushBytes = 512ll << 20;
 
 const char* kStageNames[STAGE_COUNT] = {"init",        "ray_blocks", "alloc_order", "alloc", "ray_voxels",
-                                        "route_sort", "update",      "publish",     "gc"};
+                                        "route_sort", "heavy_bins",  "update",      "publish",     "gc"};
 
 int64_t now_ns() {
   timespec ts;
@@ -348,7 +348,7 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
   long long n = 0;
   using Fn = void (*)(const Ctx&, const LaunchCfg&, cudaStream_t, long long*);
   const Fn stages[STAGE_COUNT] = {stage_init,       stage_ray_blocks,  stage_alloc_order,
-                                  stage_alloc,      stage_ray_voxels,  stage_route_sort,
+                                  stage_alloc,      stage_ray_voxels,  stage_route_sort,  stage_heavy_bins,
                                   stage_update,     stage_publish,     stage_gc};
   for (int i = 0; i < STAGE_COUNT; ++i) {
     if (timed) cudaEventRecordWithFlags(L.ev_stage[i], L.stream, cudaEventRecordExternal);

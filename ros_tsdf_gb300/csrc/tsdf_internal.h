@@ -192,7 +192,7 @@ struct Ctx {
 // Stage ids for timing.
 enum {
   STAGE_INIT = 0, STAGE_RAY_BLOCKS, STAGE_ALLOC_ORDER, STAGE_ALLOC, STAGE_RAY_VOXELS, STAGE_ROUTE_SORT,
-  STAGE_UPDATE, STAGE_PUBLISH, STAGE_GC, STAGE_COUNT
+  STAGE_HEAVY_BINS, STAGE_UPDATE, STAGE_PUBLISH, STAGE_GC, STAGE_COUNT
 };
 
 // Launch entry points implemented in tsdf_kernels.cu.  Each enqueues one
@@ -215,6 +215,7 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
+void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);

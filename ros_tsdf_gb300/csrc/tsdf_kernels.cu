@@ -629,13 +629,19 @@ __global__ void __launch_bounds__(1024) k_rs_scan_digits(int* hist, const long l
   if (threadIdx.x == 0) digit_tot[blockIdx.x] = (int)carry;
 }
 
+// Stable scatter of one pass.  A tile's 2048 keys (8 rounds of 256, index
+// order round-major) are ranked in three barrier-separated phases instead of
+// per round: (1) per round and warp, match_any gives every key its rank among
+// the warp's keys of the same digit and the group leader records the group
+// size; (2) one thread per digit turns the 8 x 8 (round, warp) counts into
+// offsets within the tile, in index order; (3) every key goes to its digit's
+// base + tile offset + group offset + rank.
 __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* kin, const unsigned* vin, unsigned* kout,
                                                      unsigned* vout, const long long* n_ptr, long long cap,
                                                      int shift, unsigned key_limit, const int* hist,
                                                      int max_tiles, const int* digit_tot, long long* n_out) {
   __shared__ int s_base[256];
-  __shared__ int s_run[256];
-  __shared__ int s_wc[RS_T / 32][256];
+  __shared__ __align__(16) unsigned short s_cell[RS_IPT][RS_T / 32][256];
   __shared__ int s_warp[32];
   const long long n = min(*n_ptr, cap);
   const long long ntiles = (n + RS_TILE - 1) / RS_TILE;
@@ -650,43 +656,55 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* kin, const 
   __syncthreads();
   const unsigned lt_mask = (1u << lane) - 1u;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    s_run[t] = hist[t * max_tiles + tile];
-    __syncthreads();
-    for (int r = 0; r < RS_IPT; ++r) {
-      long long i = tile * RS_TILE + r * RS_T + t;
-      unsigned k = 0, v = 0;
-      bool valid = false;
-      if (i < n) {
-        k = kin[i];
-        valid = k < key_limit;
-        if (valid) v = vin[i];
-      }
-      int d = valid ? (int)((k >> shift) & 255u) : 256;
+    unsigned k[RS_IPT], v[RS_IPT];
+    int d[RS_IPT], lt[RS_IPT];
 #pragma unroll
-      for (int w = 0; w < RS_T / 32; ++w) s_wc[w][t] = 0;
-      __syncthreads();
-      unsigned peers = __match_any_sync(kFull, d);
-      int lt = __popc(peers & lt_mask);
-      if (valid && lt == 0) s_wc[warp][d] = __popc(peers);
-      __syncthreads();
-      {
-        int acc = s_run[t];
+    for (int r = 0; r < RS_IPT; ++r) {
+      const long long i = tile * RS_TILE + r * RS_T + t;
+      k[r] = i < n ? kin[i] : key_limit;
+      const bool valid = k[r] < key_limit;
+      v[r] = valid ? vin[i] : 0u;
+      d[r] = valid ? (int)((k[r] >> shift) & 255u) : 256;
+    }
+    {
+      uint4* z = reinterpret_cast<uint4*>(&s_cell[0][0][0]);
+      constexpr int kWords = RS_IPT * (RS_T / 32) * 256 * 2 / 16;
+#pragma unroll
+      for (int j = 0; j < kWords / RS_T; ++j) z[t + j * RS_T] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    const int tile_run = hist[t * max_tiles + tile];  // this tile's offset within digit t
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_IPT; ++r) {
+      const unsigned peers = __match_any_sync(kFull, d[r]);
+      lt[r] = __popc(peers & lt_mask);
+      if (d[r] < 256 && lt[r] == 0) s_cell[r][warp][d[r]] = (unsigned short)__popc(peers);
+    }
+    __syncthreads();
+    {
+      int acc = 0;
+#pragma unroll
+      for (int r = 0; r < RS_IPT; ++r) {
 #pragma unroll
         for (int w = 0; w < RS_T / 32; ++w) {
-          int cnt = s_wc[w][t];
-          s_wc[w][t] = acc;
+          const int cnt = s_cell[r][w][t];
+          s_cell[r][w][t] = (unsigned short)acc;
           acc += cnt;
         }
-        s_run[t] = acc;
       }
-      __syncthreads();
-      if (valid) {
-        long long pos = (long long)s_base[d] + s_wc[warp][d] + lt;
-        kout[pos] = k;
-        vout[pos] = v;
-      }
-      __syncthreads();
+      s_base[t] += tile_run;  // digit t's base for this tile (restored below)
     }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_IPT; ++r) {
+      if (d[r] < 256) {
+        const long long pos = (long long)s_base[d[r]] + s_cell[r][warp][d[r]] + lt[r];
+        kout[pos] = k[r];
+        vout[pos] = v[r];
+      }
+    }
+    __syncthreads();
+    s_base[t] -= tile_run;
   }
 }
 
@@ -2160,11 +2178,16 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_rec_live, &c.ctr->n_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
   k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c, sel);
+  *launches += 4;
+}
+
+void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  const int sel = lc.rec_passes & 1;
   k_heavy_plan<<<1, 1024, 0, s>>>(c);
   k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c, sel);
   k_heavy_scan<<<lc.sm_count * 4, kVoxelsPerBlock, 0, s>>>(c, sel);
   k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
-  *launches += 8;
+  *launches += 4;
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
