@@ -1124,12 +1124,104 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_count(Ctx c, int rec_sel) {
   }
 }
 
-// One CTA of 512 threads per planned heavy segment: per voxel, exclusive scan
-// of its counts over the segment's chunks; per-voxel bin offsets; bin base.
-// A voxel with more than kHotChain updates goes on the grid-wide hot list
-// (long chains in the first half) and is marked in the segment's hot mask;
-// when its half of the list is full, k_heavy_update runs it instead.
-__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c, int rec_sel) {
+// One warp per planned heavy segment (no block barriers; eight segments per
+// CTA): per voxel, exclusive scan of its counts over the segment's chunks,
+// then the exclusive scan over the 512 voxels (lane j owns voxels 16j ..
+// 16j+15) gives the bin offsets; one atomic reserves the segment's bins.  A
+// voxel with more than kHotChain updates goes on the grid-wide hot list (long
+// chains in the first half) and is marked in the segment's hot mask; when its
+// half of the list is full, k_heavy_update runs it instead.
+constexpr int HS_T = 256;
+constexpr int kScanWarpChunks = 16;  // longer segments: k_heavy_scan_large
+
+__global__ void __launch_bounds__(HS_T) k_heavy_scan(Ctx c, int rec_sel) {
+  const int lane = threadIdx.x & 31;
+  const int np = (int)c.ctr->n_hplanned;
+  const long long nch = c.ctr->n_hchunks;
+  const long long half = c.hot_cap / 2;
+  const int nwarps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
+  constexpr int V = kVoxelsPerBlock / 32;  // voxels per lane
+  for (int h = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); h < np; h += nwarps) {
+    const long long c0 = c.hchunk_base[h];
+    const long long c1 = (h + 1 < np) ? c.hchunk_base[h + 1] : nch;
+    if (c1 - c0 > kScanWarpChunks) continue;  // k_heavy_scan_large's
+    int run[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) run[i] = 0;
+    for (long long gc = c0; gc < c1; ++gc) {
+      int4* row = reinterpret_cast<int4*>(c.hcnt + gc * kVoxelsPerBlock + V * lane);
+      int4 q[V / 4];
+#pragma unroll
+      for (int i = 0; i < V / 4; ++i) q[i] = row[i];
+#pragma unroll
+      for (int i = 0; i < V / 4; ++i) {
+        int4 o;
+        o.x = run[4 * i + 0];
+        o.y = run[4 * i + 1];
+        o.z = run[4 * i + 2];
+        o.w = run[4 * i + 3];
+        run[4 * i + 0] += q[i].x;
+        run[4 * i + 1] += q[i].y;
+        run[4 * i + 2] += q[i].z;
+        run[4 * i + 3] += q[i].w;
+        row[i] = o;
+      }
+    }
+    int lsum = 0;
+#pragma unroll
+    for (int i = 0; i < V; ++i) lsum += run[i];
+    int incl = lsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int tot = __shfl_sync(kFull, incl, 31);
+    unsigned long long base = 0;
+    int fit = 0;
+    if (lane == 0) {
+      base = atomicAdd(&c.ctr->hbin_cursor, (unsigned long long)tot);
+      fit = base + (unsigned long long)tot <= (unsigned long long)c.hbin_cap ? 1 : 0;
+      c.hbin_base[h] = base;
+      c.hfit[h] = fit;
+    }
+    base = __shfl_sync(kFull, base, 0);
+    fit = __shfl_sync(kFull, fit, 0);
+    int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
+    int ex = incl - lsum;
+    unsigned hot_bits = 0;  // bit i: voxel V*lane+i went on the hot list
+    long long b0 = -1;
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      vo[V * lane + i] = ex;
+      if (fit && run[i] > kHotChain) {
+        const bool lng = run[i] >= kLongChain;
+        const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
+        if (idx < half) {
+          if (b0 < 0) b0 = c.seg_start[c.heavy[h]];
+          const int item = c.seg_item[c.heavy[h]];
+          HotChain hc;
+          hc.bin = base + (unsigned long long)ex;
+          hc.n = run[i];
+          hc.phys = (int)(c.hdr->key_lo + c.rec_key[rec_sel][b0]);
+          hc.local = V * lane + i;
+          hc.maxw = c.maps[c.items[item].map].maxw;
+          c.hot[(lng ? 0 : half) + idx] = hc;
+          hot_bits |= 1u << i;
+        }
+      }
+      ex += run[i];
+    }
+    if (lane == 31) vo[kVoxelsPerBlock] = tot;
+    // hot mask word w covers voxels 32w..32w+31 = lanes 2w, 2w+1 (V = 16)
+    const unsigned lo = __shfl_down_sync(kFull, hot_bits, 1);
+    if ((lane & 1) == 0) c.hmask[(long long)h * (kVoxelsPerBlock / 32) + (lane >> 1)] = hot_bits | (lo << 16);
+  }
+}
+
+// The same for segments of more than kScanWarpChunks chunks: one CTA of 512
+// threads per segment, one thread per voxel, eight chunk counts in flight.
+__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan_large(Ctx c, int rec_sel) {
   __shared__ int s_warp[32];
   __shared__ unsigned long long s_base;
   __shared__ int s_fit;
@@ -1141,6 +1233,7 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan(Ctx c, int rec_s
   for (int h = blockIdx.x; h < np; h += gridDim.x) {
     const long long c0 = c.hchunk_base[h];
     const long long c1 = (h + 1 < np) ? c.hchunk_base[h + 1] : nch;
+    if (c1 - c0 <= kScanWarpChunks) continue;  // k_heavy_scan's
     int run = 0;
     long long gc = c0;
     for (; gc + 8 <= c1; gc += 8) {  // eight chunk counts in flight
@@ -2185,9 +2278,10 @@ void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   const int sel = lc.rec_passes & 1;
   k_heavy_plan<<<1, 1024, 0, s>>>(c);
   k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c, sel);
-  k_heavy_scan<<<lc.sm_count * 4, kVoxelsPerBlock, 0, s>>>(c, sel);
+  k_heavy_scan<<<lc.sm_count * 8, HS_T, 0, s>>>(c, sel);
+  k_heavy_scan_large<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c, sel);
   k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
-  *launches += 4;
+  *launches += 5;
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
