@@ -4,24 +4,32 @@
 // Stages (each a handful of grid-fixed kernels, so a step captures as one
 // CUDA graph and replays for any batch composition):
 //   ray_blocks   persistent work queue over (scan, point chunk): truncation
-//                segment + block DDA per point; warp-cooperative lookup /
-//                lock-free CAS insertion of every block into the map's hash
-//                table; unallocated blocks enter as "pending" with the
-//                smallest first-touch rank seen.
+//                segment + block DDA per point; lookup / lock-free CAS
+//                insertion of every block into the map's hash table
+//                (G-lane cooperative probes, G = bucket size); unallocated
+//                blocks enter as "pending" with the smallest first-touch rank.
 //                (tsdf_handler.cu:112-272, :282-500)
 //   alloc_order  pending entries sorted by first-touch rank (LSD radix sort)
 //   alloc        heap slot = free_list[block_count + rank within the map]
 //                (device free-list stack), block zeroed, entry resolved
 //   ray_voxels   voxel DDA per point; its voxels grouped into runs of one
-//                block; one routing record (block slot, point) per run
+//                block; per voxel an entry {d, local index}, per run one
+//                routing record (block slot, entry range)
 //   route_sort   stable radix sort of the records by block slot; segment
-//                heads -> one work item per block touched
-//   update       one CTA per block: 4 KiB of voxels staged in shared memory
-//                with 16-byte loads/stores; each point's voxels in the block
-//                recomputed and applied per voxel in ascending point order
-//                (tsdf_handler.cu:604-665)
+//                heads -> one segment per block touched; segment items and
+//                the list of heavy segments (more than 128 records)
+//   heavy_bins   heavy segments: counting sort of their updates into
+//                per-voxel bins in point order (plan, count, scan, place);
+//                voxels with more than 128 updates go on the hot list
+//   update       k_update: its first CTAs run the hot chains (one warp per
+//                voxel), the rest take the light segments (one CTA per
+//                block, voxels staged in shared memory, per-voxel record
+//                masks give each update its place in point order);
+//                k_heavy_update, on a second stream: binned heavy segments,
+//                one lane per voxel.  (tsdf_handler.cu:604-665)
 //   publish      in-radius blocks counted, prefix-summed, compacted to the
-//                output (tsdf_handler.cu:767-825)
+//                output arrays or a serialized Tsdf message
+//                (tsdf_handler.cu:767-825, publisher.cpp:9-31)
 //   gc           out-of-radius blocks compacted, pushed to the free list in
 //                ascending slot order, hash entries tombstoned
 //                (tsdf_handler.cu:836-952)
@@ -1341,7 +1349,9 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
 // a time; every voxel gets a 128-bit mask of the records that update it, an
 // entry's rank in its voxel's bin is a popcount of the mask below it, so each
 // bin lists its updates in ascending point order and its owner thread applies
-// them sequentially: the reference's update rule, in a fixed order.
+// them sequentially: the reference's update rule, in a fixed order.  The
+// apply_chain helper below is that rule over a bin in global memory (the
+// pass-based path).
 //
 // Segments longer than one chunk (a block that many points update, e.g. the
 // blocks around a sensor standing inside an object) are binned per voxel by
