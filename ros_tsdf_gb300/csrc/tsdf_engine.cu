@@ -121,8 +121,8 @@ struct Request {
 
 struct Lane {
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t side = nullptr, side2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
   Ctx ctx{};
   // device scratch
   BatchHdr* d_hdr = nullptr;
@@ -234,8 +234,10 @@ LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_p
   lc.rank_passes = rank_passes;
   lc.rec_passes = rec_passes;
   lc.side = L.side;
+  lc.side2 = L.side2;
   lc.ev_fork = L.ev_fork;
   lc.ev_join = L.ev_join;
+  lc.ev_join2 = L.ev_join2;
   return lc;
 }
 
@@ -243,8 +245,10 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   const tsdf_engine_cfg& c = eng->cfg;
   CK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&L.side2, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&L.ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&L.ev_join, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&L.ev_join2, cudaEventDisableTiming));
   for (int i = 0; i <= STAGE_COUNT; ++i) CK(cudaEventCreate(&L.ev_stage[i]));
   CK(cudaEventCreateWithFlags(&L.ev_done, cudaEventDisableTiming));
   const long long npts = c.max_batch_points;
@@ -336,7 +340,9 @@ void lane_free(Lane& L) {
   if (L.ev_done) cudaEventDestroy(L.ev_done);
   if (L.ev_fork) cudaEventDestroy(L.ev_fork);
   if (L.ev_join) cudaEventDestroy(L.ev_join);
+  if (L.ev_join2) cudaEventDestroy(L.ev_join2);
   if (L.side) cudaStreamDestroy(L.side);
+  if (L.side2) cudaStreamDestroy(L.side2);
   if (L.stream) cudaStreamDestroy(L.stream);
   L = Lane();
 }

@@ -203,9 +203,11 @@ struct LaunchCfg {
   int ray_threads;
   int rank_passes;
   int rec_passes;
-  cudaStream_t side;     // second stream of the lane: a stage may fork work onto it
+  cudaStream_t side;     // second and third streams of the lane: a stage may fork
+  cudaStream_t side2;    // work onto them
   cudaEvent_t ev_fork;   // and join it back (timing disabled; usable in graph capture)
   cudaEvent_t ev_join;
+  cudaEvent_t ev_join2;
 };
 
 cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice

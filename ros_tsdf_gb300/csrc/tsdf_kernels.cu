@@ -1550,6 +1550,20 @@ __device__ __forceinline__ void for_record_entries(const uint2* e, int cnt, F f)
   }
 }
 
+// The hot chains on their own, on a third stream of the update stage: one
+// CTA of four warps per SM, launched first so each SM gets one; its shared
+// memory request thins out the light-block CTAs beside a long chain (less
+// issue contention on its sub-partition).  Each warp takes chains until the
+// list is empty; a CTA that finds it empty exits and frees its SM.
+constexpr int kHotSmem = 64 * 1024;
+
+__global__ void __launch_bounds__(128) k_hot_chains(Ctx c) {
+  extern __shared__ __align__(16) float4 s_hot_tile[];
+  const int t = threadIdx.x;
+  float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(s_hot_tile) + 2 * (t >> 5);
+  run_hot_chains(c, tile, t & 31);
+}
+
 // The first hot_ctas CTAs (one per SM: blocks are dispatched in index order)
 // start with the hot chains, so the longest serial chains run from the start
 // of the kernel, beside the segment work of the other CTAs.
@@ -2223,7 +2237,9 @@ void launch_check_div(unsigned long long seed, long long n, unsigned long long* 
 // ----------------------------------------------------------------------------
 // stage launchers
 cudaError_t kernels_init() {
-  return cudaFuncSetAttribute(k_heavy_update, cudaFuncAttributeMaxDynamicSharedMemorySize, kHuSmem);
+  cudaError_t e = cudaFuncSetAttribute(k_heavy_update, cudaFuncAttributeMaxDynamicSharedMemorySize, kHuSmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_hot_chains, cudaFuncAttributeMaxDynamicSharedMemorySize, kHotSmem);
 }
 
 void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
@@ -2295,18 +2311,23 @@ void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  // k_update (hot chains first, then the light blocks) and k_heavy_update
-  // (binned heavy blocks) touch disjoint voxels: fork the latter onto the
-  // lane's side stream so it fills the SMs the light blocks leave while the
-  // longest chains still run, and join before the publish stage
+  // k_hot_chains (the listed long chains), k_heavy_update (binned heavy
+  // blocks) and k_update (light blocks, heavy blocks past the counting
+  // sort's capacity) touch disjoint voxels: the first two are forked onto
+  // the lane's side streams, launched before k_update so the chains start at
+  // once, and all three join before the publish stage
   const int sel = lc.rec_passes & 1;
   cudaEventRecord(lc.ev_fork, s);
+  cudaStreamWaitEvent(lc.side2, lc.ev_fork, 0);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
-  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel, lc.sm_count);
+  k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
   k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
+  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel, 0);
+  cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);
+  cudaStreamWaitEvent(s, lc.ev_join2, 0);
   cudaStreamWaitEvent(s, lc.ev_join, 0);
-  *launches += 2;
+  *launches += 3;
 }
 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
