@@ -21,12 +21,12 @@
 //   heavy_bins   heavy segments: counting sort of their updates into
 //                per-voxel bins in point order (plan, count, scan, place);
 //                voxels with more than 128 updates go on the hot list
-//   update       k_update: its first CTAs run the hot chains (one warp per
-//                voxel), the rest take the light segments (one CTA per
-//                block, voxels staged in shared memory, per-voxel record
-//                masks give each update its place in point order);
-//                k_heavy_update, on a second stream: binned heavy segments,
-//                one lane per voxel.  (tsdf_handler.cu:604-665)
+//   update       three streams: k_hot_chains (one warp per voxel with more
+//                than 128 updates), k_heavy_update (binned heavy segments,
+//                one lane per voxel) and k_update (light segments: one CTA
+//                per block, voxels staged in shared memory, per-voxel record
+//                masks give each update its place in point order).
+//                (tsdf_handler.cu:604-665)
 //   publish      in-radius blocks counted, prefix-summed, compacted to the
 //                output arrays or a serialized Tsdf message
 //                (tsdf_handler.cu:767-825, publisher.cpp:9-31)
@@ -1356,7 +1356,7 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
 // Segments longer than one chunk (a block that many points update, e.g. the
 // blocks around a sensor standing inside an object) are binned per voxel by
 // the multi-CTA counting sort of the routing stage and updated by
-// k_heavy_update and the hot-chain warps.  Only heavy segments beyond that sort's
+// k_heavy_update and k_hot_chains.  Only heavy segments beyond that sort's
 // capacity stay here, in three passes: per-voxel counts over all records,
 // ordered placement of every update into per-voxel bins in global scratch
 // (mask popcount + running per-voxel cursor), then one chain per voxel.
@@ -1564,14 +1564,10 @@ __global__ void __launch_bounds__(128) k_hot_chains(Ctx c) {
   run_hot_chains(c, tile, t & 31);
 }
 
-// The first hot_ctas CTAs (one per SM: blocks are dispatched in index order)
-// start with the hot chains, so the longest serial chains run from the start
-// of the kernel, beside the segment work of the other CTAs.
-__global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot_ctas) {
+__global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
   __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
   // record bit masks per voxel, word-major (word w covers records 32w..32w+31)
-  // so that 16-byte accesses of four consecutive voxels hit distinct banks;
-  // the hot-chain tiles live here before the segment loop
+  // so that 16-byte accesses of four consecutive voxels hit distinct banks
   __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];
   __shared__ float s_d[kLightEntries];
   __shared__ unsigned short s_l[kLightEntries];
@@ -1591,11 +1587,6 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
   const unsigned* rk = c.rec_key[rec_sel];
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned lt_bits = (1u << (t & 31)) - 1u;
-  if ((int)blockIdx.x < hot_ctas) {
-    float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(&s_mask[0][0]) + 2 * (t >> 5);
-    run_hot_chains(c, tile, t & 31);
-    __syncthreads();
-  }
   // The queue item after the current one is claimed when the current one
   // starts; its segment bounds, block and records are fetched during the
   // current segment's phases (prefetch only: no registers held), so the next
@@ -1833,7 +1824,7 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel, int hot
 // Markstein steps (sat_step); otherwise each step runs the weight chain and
 // one reciprocal RN(1/W') in the lane, then the same Markstein step.  A range
 // flag or NaN makes the lane redo its chain exactly.  Voxels on the hot list
-// are left to the hot-chain warps of k_update; longer chains that did not fit
+// are left to k_hot_chains; longer chains that did not fit
 // on the list run here, a
 // warp each (warp_chain), after the lanes.
 constexpr int HU_T = kVoxelsPerBlock;
@@ -2322,7 +2313,7 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
   k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
-  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel, 0);
+  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
   cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);
   cudaStreamWaitEvent(s, lc.ev_join2, 0);
