@@ -226,8 +226,9 @@ tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>*
     if (_s != TSDF_OK) return _s;       \
   } while (0)
 
-LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes) {
+LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes, bool staged) {
   LaunchCfg lc;
+  lc.staged = staged ? 1 : 0;
   lc.sm_count = eng->sm_count;
   lc.bucket_size = eng->cfg.bucket_size;
   lc.ray_threads = eng->cfg.ray_threads;
@@ -349,8 +350,8 @@ void lane_free(Lane& L) {
 
 // Enqueue the pipeline of one step on the lane's stream (used directly or
 // inside a graph capture).  Returns the number of kernel launches.
-long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool timed) {
-  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes);
+long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool timed) {
+  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged);
   long long n = 0;
   using Fn = void (*)(const Ctx&, const LaunchCfg&, cudaStream_t, long long*);
   const Fn stages[STAGE_COUNT] = {stage_init,       stage_ray_blocks,  stage_alloc_order,
@@ -364,20 +365,20 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
   return n;
 }
 
-tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes) {
+tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged) {
   const bool timed = eng->stage_timing;
   L.timed = timed;
   if (eng->cfg.no_graphs) {
-    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, timed);
+    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, timed);
     CK(cudaGetLastError());
     return TSDF_OK;
   }
-  const int key = rank_passes * 100 + rec_passes * 10 + (timed ? 1 : 0);
+  const int key = (staged ? 1000 : 0) + rank_passes * 100 + rec_passes * 10 + (timed ? 1 : 0);
   auto it = L.graphs.find(key);
   if (it == L.graphs.end()) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
-    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, timed);
+    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, timed);
     cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     cudaGraphExec_t ex = nullptr;
@@ -409,9 +410,10 @@ bool device_accessible(const void* p, const void** dev_ptr) {
   return false;
 }
 
-// Device or managed memory, which kernels read in place.  Host memory, pinned
-// or not, is copied in by the DMA engine instead: kernels reading it over the
-// host link would see its latency on every point load.
+// Device or managed memory, which kernels read in place.  Host memory is
+// staged into HBM first (kernels reading it over the host link would see its
+// latency on every point load): pinned memory by k_stage_points, one launch
+// for the batch; pageable memory by the DMA engine, one copy per scan.
 bool device_resident(const void* p, const void** dev_ptr) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -469,10 +471,12 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     return fail(eng, TSDF_ERR_CAPACITY, "batch has " + std::to_string(total) + " points; capacity " +
                                             std::to_string(c.max_batch_points));
   // inputs
+  long long chunks = 0;
   for (int i = 0; i < n; ++i) {
     const tsdf_scan& s = scans[i];
     ItemDev& it = items[i];
     const void* dp = nullptr;
+    it.chunk_base = chunks;
     if (s.n_points == 0) {
       it.pts = L.d_points;
     } else if (device_resident(s.xyz, &dp)) {
@@ -482,7 +486,15 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
       // PointCloud2 buffer) ends 12 bytes into its last record
       long long nb = (s.n_points - 1) * (long long)s.stride_bytes + 12;
       if (bytes + nb > c.max_batch_points * 16) return fail(eng, TSDF_ERR_CAPACITY, "point staging full");
-      CK(cudaMemcpyAsync(L.d_points + bytes, s.xyz, nb, cudaMemcpyHostToDevice, L.stream));
+      const void* mp = nullptr;
+      if ((reinterpret_cast<uintptr_t>(s.xyz) & 3) == 0 && device_accessible(s.xyz, &mp)) {
+        // pinned: copied in by k_stage_points, one launch for the batch
+        it.src = (const char*)mp;
+        it.src_bytes = nb;
+        chunks += (nb + kStageChunk - 1) / kStageChunk;
+      } else {
+        CK(cudaMemcpyAsync(L.d_points + bytes, s.xyz, nb, cudaMemcpyHostToDevice, L.stream));
+      }
       it.pts = L.d_points + bytes;
       bytes += (nb + 15) & ~15ll;
     }
@@ -521,13 +533,14 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   hdr->rec_total = total * rec_stride;
   hdr->key_lo = lo;
   hdr->rec_key_limit = kRecSentinel;
+  hdr->stage_chunks = chunks;
   const unsigned long long rank_range = (unsigned long long)std::max<long long>(total, 1) * rank_stride;
   if (rank_range >= 0xFFFFFFFFull) return fail(eng, TSDF_ERR_CAPACITY, "rank range exceeds 32 bits");
   const int rank_passes = std::max(1, (bits_for(rank_range) + kRadixBits - 1) / kRadixBits);
   const int rec_passes = std::max(1, (bits_for((unsigned long long)(hi - lo)) + kRadixBits - 1) / kRadixBits);
   CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr), cudaMemcpyHostToDevice, L.stream));
   CK(cudaMemcpyAsync(L.d_items, items, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
-  TRY(launch_pipeline(eng, L, rank_passes, rec_passes));
+  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0));
   CK(cudaMemcpyAsync(L.h_stats, L.ctx.item_stats, sizeof(long long) * ST_COUNT * n, cudaMemcpyDeviceToHost, L.stream));
   CK(cudaMemcpyAsync(L.h_ctr, L.ctx.ctr, sizeof(LaneCounters), cudaMemcpyDeviceToHost, L.stream));
   CK(cudaMemcpyAsync(L.h_mctr, eng->d_mctr, sizeof(MapCounters) * eng->maps.size(), cudaMemcpyDeviceToHost,

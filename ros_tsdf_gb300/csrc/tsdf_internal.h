@@ -9,6 +9,7 @@ namespace tsdfg {
 
 constexpr int kVoxelsPerSide = 8;      // tsdf_container.cuh:19
 constexpr int kVoxelsPerBlock = 512;   // tsdf_container.cuh:21
+constexpr int kStageChunk = 4096;       // bytes of pinned host input per staging CTA iteration
 constexpr int kKeyBias = 1 << 20;      // 21-bit signed block coordinates
 constexpr unsigned long long kEmptyKey = ~0ull;
 constexpr unsigned long long kTombKey = ~0ull - 1ull;
@@ -65,6 +66,9 @@ struct ItemDev {
   float* out_pos;         // published positions (device-accessible) or null
   float2* out_data;       // published voxels (device-accessible)
   long long out_cap;
+  const char* src;        // pinned host points (device-mapped) that k_stage_points copies to pts, or null
+  long long src_bytes;    // bytes the points span at src
+  long long chunk_base;   // first staging chunk of this item (non-decreasing over items)
 };
 
 // Per-item stats slots (match tsdf_scan_stats field order).
@@ -96,6 +100,7 @@ struct BatchHdr {
   long long key_lo;           // record key = physical slot - key_lo
   unsigned rec_key_limit;     // record keys >= this are empty routes
   int pad1;
+  long long stage_chunks;     // staging chunks of pinned host inputs (k_stage_points)
 };
 
 // Device-side counters of one step (zeroed by the first kernel).
@@ -203,6 +208,7 @@ struct LaunchCfg {
   int ray_threads;
   int rank_passes;
   int rec_passes;
+  int staged;            // pinned host inputs are copied in by k_stage_points
   cudaStream_t side;     // second and third streams of the lane: a stage may fork
   cudaStream_t side2;    // work onto them
   cudaEvent_t ev_fork;   // and join it back (timing disabled; usable in graph capture)
