@@ -191,9 +191,13 @@ def run_ours(args, rank, world, local, pg):
 
     specs = make_workload(args.workload, rank, args.heap_blocks)
     n_steps = args.warmup + args.steps
-    scans = gen_scans(specs, n_steps)
-    pts_per_step = [sum(scans[m][k][0].shape[0] for m in range(len(specs))) for k in range(n_steps)]
-    timed_pts = float(sum(pts_per_step[args.warmup:]))
+    # the timed steps carry no events inside their graphs (device time from two
+    # events around each step); the per-stage breakdown comes from a few extra
+    # steps after them, with events around every stage
+    n_stage = min(args.steps, 5)
+    scans = gen_scans(specs, n_steps + n_stage)
+    pts_per_step = [sum(scans[m][k][0].shape[0] for m in range(len(specs))) for k in range(n_steps + n_stage)]
+    timed_pts = float(sum(pts_per_step[args.warmup:n_steps]))
     pool = sum(s.heap_blocks for s in specs) + 1024
     max_pts = max(pts_per_step) + 1024
     cap = args.pub_cap
@@ -206,7 +210,7 @@ def run_ours(args, rank, world, local, pg):
     # ---- value: device-resident inputs and outputs, CUDA-event device time
     eng = new_engine()
     mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
-    dev_in = [[eng.device_array(scans[m][k][0]) for k in range(n_steps)] for m in range(len(specs))]
+    dev_in = [[eng.device_array(scans[m][k][0]) for k in range(n_steps + n_stage)] for m in range(len(specs))]
     dev_pos = [eng.device_array(np.zeros((cap, 3), np.float32)) for _ in specs]
     dev_dat = [eng.device_array(np.zeros((cap, 2), np.float32)) for _ in specs]
     import ctypes as C
@@ -241,7 +245,7 @@ def run_ours(args, rank, world, local, pg):
     stats_steps = []
     dev_ms = []
     wall_ms = []
-    eng.set_stage_timing(True)
+    eng.set_stage_timing(2)
     stage_acc = {}
     launches0 = 0
     barrier(pg)
@@ -253,19 +257,26 @@ def run_ours(args, rank, world, local, pg):
             a3 = batch_args(eng, k, lambda m, kk: dev_in[m][kk].ptr, lambda m: dev_pos[m].ptr,
                             lambda m: dev_dat[m].ptr, cap)
             eng.flush_l2()
-            before = eng.stage_times()
+            before = eng.step_times()[0]
             t0 = time.perf_counter()
             st, stat = batch_run(eng, a3)
             wall = time.perf_counter() - t0
-            after = eng.stage_times()
-            step_ms = sum(after[s][0] - before[s][0] for s in after)
+            step_ms = eng.step_times()[0] - before
             if k >= args.warmup:
                 dev_ms.append(step_ms)
                 wall_ms.append(wall * 1000.0)
                 stats_steps.append(st)
     gpu_launches = eng.kernel_launches() - launches0
-    stage_acc = eng.stage_times()
     clocks = clk.summary()
+    eng.set_stage_timing(1)
+    eng.reset_stage_times()
+    for k in range(n_steps, n_steps + n_stage):
+        a3 = batch_args(eng, k, lambda m, kk: dev_in[m][kk].ptr, lambda m: dev_pos[m].ptr,
+                        lambda m: dev_dat[m].ptr, cap)
+        eng.flush_l2()
+        batch_run(eng, a3)
+    stage_acc = eng.stage_times()
+    eng.set_stage_timing(0)
     t_dev = sum(dev_ms) / 1000.0
     t_dev = max_over_ranks(pg, t_dev)
     total_pts = sum_over_ranks(pg, timed_pts)
@@ -520,6 +531,9 @@ def main():
                    "voxel_size": sorted({s.params.voxel_size for s in r["specs"]}),
                    "truncation_distance": sorted({s.params.truncation_distance for s in r["specs"]}),
                    "l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step",
+                   "timing": ("device time of each timed step from two CUDA events on the engine's stream around "
+                              "it (its graph carries no events); stage_ms_per_step from "
+                              f"{min(args.steps, 5)} further steps with events around every stage"),
                    "launch": tuned or {"bucket_size": args.bucket_size, "ray_chunk": args.ray_chunk,
                                        "ray_threads": args.ray_threads, "source": "command line"}},
         "e2e": r["e2e"], "plain": r["plain"],

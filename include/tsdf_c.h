@@ -277,8 +277,15 @@ tsdf_status tsdf_map_restore(tsdf_engine* eng, const void* snapshot, int64_t byt
 tsdf_status tsdf_check_division(tsdf_engine* eng, uint64_t seed, int64_t n, int64_t* mismatches, float* first_ab);
 
 /* ---- measurement helpers --------------------------------------------- */
-/* Record CUDA events around every pipeline stage of later steps. */
+/* Device timing of later steps with CUDA events on the lane's stream.
+ * on = 1: events around every pipeline stage (recorded inside the step's
+ * graph; each adds a few microseconds) and around the step; on = 2: around
+ * the step only, outside the graph (the graph carries no events); 0: off. */
 tsdf_status tsdf_set_stage_timing(tsdf_engine* eng, int on);
+/* Accumulated device milliseconds of timed steps (from the batch header
+ * upload to the end of the step's graph) and their count since the last
+ * reset. */
+tsdf_status tsdf_step_times(tsdf_engine* eng, double* ms, int64_t* steps);
 /* Stage names and accumulated milliseconds / launch counts since the last
  * reset.  names may be NULL.  *n in: capacity, out: number of stages. */
 tsdf_status tsdf_stage_times(tsdf_engine* eng, const char** names, double* ms, int64_t* launches, int* n);

@@ -113,6 +113,7 @@ SIGNATURES = [
     ("tsdf_stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
     ("tsdf_reset_stage_times", C.c_int, [C.c_void_p]),
+    ("tsdf_step_times", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("tsdf_flush_l2", C.c_int, [C.c_void_p]),
     ("tsdf_kernel_launches", C.c_int64, [C.c_void_p]),
     ("tsdf_host_alloc", C.c_int, [C.POINTER(C.c_void_p), C.c_int64]),

@@ -140,10 +140,12 @@ struct Lane {
   std::map<int, cudaGraphExec_t> graphs;
   std::map<int, long long> graph_launches;
   cudaEvent_t ev_stage[STAGE_COUNT + 1] = {};
+  cudaEvent_t ev_step[2] = {};  // around the whole step, outside the graph
   cudaEvent_t ev_done = nullptr;
   // the batch currently in flight (served mode)
   bool busy = false;
   bool timed = false;
+  bool step_timed = false;
   std::vector<std::shared_ptr<Request>> reqs;
   struct Staged {
     int item;
@@ -179,10 +181,14 @@ struct tsdf_engine {
   std::vector<MapHost> maps;
   Lane lanes[kMaxLanes];
   int n_lanes = 1;
-  // measurement
+  // measurement: 1 = events around every stage (inside the graph) and the
+  // step; 2 = events around the step only (the graph carries none)
+  int timing = 0;
   bool stage_timing = false;
   double stage_ms[STAGE_COUNT] = {};
   long long stage_launches[STAGE_COUNT] = {};
+  double step_ms = 0;
+  long long step_count = 0;
   std::atomic<long long> launches{0};
   // served mode
   std::thread sched;
@@ -251,6 +257,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   CK(cudaEventCreateWithFlags(&L.ev_join, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&L.ev_join2, cudaEventDisableTiming));
   for (int i = 0; i <= STAGE_COUNT; ++i) CK(cudaEventCreate(&L.ev_stage[i]));
+  for (int i = 0; i < 2; ++i) CK(cudaEventCreate(&L.ev_step[i]));
   CK(cudaEventCreateWithFlags(&L.ev_done, cudaEventDisableTiming));
   const long long npts = c.max_batch_points;
   const long long rank_cap = npts * c.max_routes;
@@ -338,6 +345,8 @@ void lane_free(Lane& L) {
   if (L.h_mctr) cudaFreeHost(L.h_mctr);
   for (int i = 0; i <= STAGE_COUNT; ++i)
     if (L.ev_stage[i]) cudaEventDestroy(L.ev_stage[i]);
+  for (int i = 0; i < 2; ++i)
+    if (L.ev_step[i]) cudaEventDestroy(L.ev_step[i]);
   if (L.ev_done) cudaEventDestroy(L.ev_done);
   if (L.ev_fork) cudaEventDestroy(L.ev_fork);
   if (L.ev_join) cudaEventDestroy(L.ev_join);
@@ -538,9 +547,12 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   if (rank_range >= 0xFFFFFFFFull) return fail(eng, TSDF_ERR_CAPACITY, "rank range exceeds 32 bits");
   const int rank_passes = std::max(1, (bits_for(rank_range) + kRadixBits - 1) / kRadixBits);
   const int rec_passes = std::max(1, (bits_for((unsigned long long)(hi - lo)) + kRadixBits - 1) / kRadixBits);
+  L.step_timed = eng->timing != 0;
+  if (L.step_timed) CK(cudaEventRecord(L.ev_step[0], L.stream));
   CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr), cudaMemcpyHostToDevice, L.stream));
   CK(cudaMemcpyAsync(L.d_items, items, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
   TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0));
+  if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   CK(cudaMemcpyAsync(L.h_stats, L.ctx.item_stats, sizeof(long long) * ST_COUNT * n, cudaMemcpyDeviceToHost, L.stream));
   CK(cudaMemcpyAsync(L.h_ctr, L.ctx.ctr, sizeof(LaneCounters), cudaMemcpyDeviceToHost, L.stream));
   CK(cudaMemcpyAsync(L.h_mctr, eng->d_mctr, sizeof(MapCounters) * eng->maps.size(), cudaMemcpyDeviceToHost,
@@ -559,6 +571,14 @@ tsdf_status maybe_rehash(tsdf_engine* eng, int map_id, Lane& L);
 // Wait for lane L's batch and deliver its results.
 tsdf_status finish_batch(tsdf_engine* eng, Lane& L, int n, tsdf_scan_result* res) {
   CK(cudaEventSynchronize(L.ev_done));
+  if (L.step_timed) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, L.ev_step[0], L.ev_step[1]) == cudaSuccess) {
+      eng->step_ms += ms;
+      eng->step_count += 1;
+    }
+    cudaGetLastError();
+  }
   if (L.timed) {
     for (int i = 0; i < STAGE_COUNT; ++i) {
       float ms = 0;
@@ -1352,7 +1372,17 @@ tsdf_status tsdf_check_division(tsdf_engine* eng, uint64_t seed, int64_t n, int6
 tsdf_status tsdf_set_stage_timing(tsdf_engine* eng, int on) {
   if (!eng) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
-  eng->stage_timing = on != 0;
+  if (on < 0 || on > 2) return TSDF_ERR_INVALID_ARG;
+  eng->timing = on;
+  eng->stage_timing = on == 1;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_step_times(tsdf_engine* eng, double* ms, int64_t* steps) {
+  if (!eng || !ms || !steps) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  *ms = eng->step_ms;
+  *steps = eng->step_count;
   return TSDF_OK;
 }
 
@@ -1373,6 +1403,8 @@ tsdf_status tsdf_reset_stage_times(tsdf_engine* eng) {
   if (!eng) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   for (int i = 0; i < STAGE_COUNT; ++i) eng->stage_ms[i] = 0, eng->stage_launches[i] = 0;
+  eng->step_ms = 0;
+  eng->step_count = 0;
   return TSDF_OK;
 }
 

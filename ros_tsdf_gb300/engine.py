@@ -295,8 +295,17 @@ class Engine:
         return out
 
     # -- measurement ----------------------------------------------------------
-    def set_stage_timing(self, on: bool):
-        self._check(self.lib.tsdf_set_stage_timing(self.h, 1 if on else 0), "tsdf_set_stage_timing")
+    def set_stage_timing(self, on):
+        """True / 1: events around every stage and the step; 2: around the
+        step only (no events inside the graph); False / 0: off."""
+        self._check(self.lib.tsdf_set_stage_timing(self.h, int(on)), "tsdf_set_stage_timing")
+
+    def step_times(self) -> tuple[float, int]:
+        """(device milliseconds, steps) accumulated since the last reset."""
+        ms = C.c_double()
+        n = C.c_int64()
+        self._check(self.lib.tsdf_step_times(self.h, C.byref(ms), C.byref(n)), "tsdf_step_times")
+        return ms.value, int(n.value)
 
     def stage_times(self) -> dict:
         n = C.c_int(16)

@@ -530,3 +530,31 @@ def test_pinned_inputs_staged_by_kernel_match_oracle(built):
                                   specs[i].params.truncation_distance, f"step {k} map {i}")
         for i in range(len(specs)):
             assert_state_equal(eng, mids[i], orcs[i], specs[i].heap_blocks, voxels=(i < 2))
+
+
+def test_step_timing_modes(built):
+    """Timing mode 2 records one device interval per step (no events inside
+    the graph); mode 1 also fills the per-stage times; results are the same."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = W.plain_small(seed=5, heap_blocks=1 << 12)
+    src = W.ScanSource(spec)
+    scans = [src.scan(k) for k in range(4)]
+    outs = []
+    for mode in (2, 1):
+        with Engine(max_maps=2, pool_blocks=1 << 12, max_batch_points=1 << 14) as eng:
+            mid = eng.create_map(spec.params, spec.heap_blocks)
+            eng.set_stage_timing(mode)
+            res = [eng.integrate(mid, *sc, pub_cap=1 << 16) for sc in scans]
+            ms, steps = eng.step_times()
+            assert steps == 4 and ms > 0
+            st = eng.stage_times()
+            if mode == 2:
+                assert all(v == (0.0, 0) for v in st.values())
+            else:
+                assert all(v[1] == 4 for v in st.values()) and sum(v[0] for v in st.values()) > 0
+            eng.reset_stage_times()
+            assert eng.step_times() == (0.0, 0)
+            outs.append([(r.count, r.pos.copy(), r.data.copy()) for r in res])
+    for (ca, pa, da), (cb, pb, db) in zip(*outs):
+        assert ca == cb and np.array_equal(pa, pb) and np.array_equal(da, db)
