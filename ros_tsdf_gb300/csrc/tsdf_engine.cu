@@ -232,9 +232,11 @@ tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>*
     if (_s != TSDF_OK) return _s;       \
   } while (0)
 
-LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes, bool staged) {
+LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes, bool staged,
+                     bool copyout) {
   LaunchCfg lc;
   lc.staged = staged ? 1 : 0;
+  lc.copyout = copyout ? 1 : 0;
   lc.sm_count = eng->sm_count;
   lc.bucket_size = eng->cfg.bucket_size;
   lc.ray_threads = eng->cfg.ray_threads;
@@ -359,8 +361,9 @@ void lane_free(Lane& L) {
 
 // Enqueue the pipeline of one step on the lane's stream (used directly or
 // inside a graph capture).  Returns the number of kernel launches.
-long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool timed) {
-  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged);
+long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
+                           bool timed) {
+  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout);
   long long n = 0;
   using Fn = void (*)(const Ctx&, const LaunchCfg&, cudaStream_t, long long*);
   const Fn stages[STAGE_COUNT] = {stage_init,       stage_ray_blocks,  stage_alloc_order,
@@ -374,20 +377,21 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
   return n;
 }
 
-tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged) {
+tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout) {
   const bool timed = eng->stage_timing;
   L.timed = timed;
   if (eng->cfg.no_graphs) {
-    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, timed);
+    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed);
     CK(cudaGetLastError());
     return TSDF_OK;
   }
-  const int key = (staged ? 1000 : 0) + rank_passes * 100 + rec_passes * 10 + (timed ? 1 : 0);
+  const int key =
+      (copyout ? 2000 : 0) + (staged ? 1000 : 0) + rank_passes * 100 + rec_passes * 10 + (timed ? 1 : 0);
   auto it = L.graphs.find(key);
   if (it == L.graphs.end()) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
-    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, timed);
+    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed);
     cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     cudaGraphExec_t ex = nullptr;
@@ -481,6 +485,15 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
                                             std::to_string(c.max_batch_points));
   // inputs
   long long chunks = 0;
+  bool copyout = false;
+  // staging that pageable outputs need (pinned outputs use what is left)
+  long long pageable_need = 0;
+  for (int i = 0; i < n; ++i) {
+    const void* q = nullptr;
+    if (res[i].pub_format == TSDF_PUB_ARRAYS && res[i].pub_cap > 0 &&
+        !(device_accessible(res[i].pub_pos, &q) && device_accessible(res[i].pub_data, &q)))
+      pageable_need += res[i].pub_cap;
+  }
   for (int i = 0; i < n; ++i) {
     const tsdf_scan& s = scans[i];
     ItemDev& it = items[i];
@@ -520,8 +533,21 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     } else if (it.out_fmt != TSDF_PUB_ARRAYS) {
       return fail(eng, TSDF_ERR_INVALID_ARG, "unknown pub_format");
     } else if (it.out_cap > 0 && device_accessible(res[i].pub_pos, &pp) && device_accessible(res[i].pub_data, &pd)) {
-      it.out_pos = (float*)pp;
-      it.out_data = (float2*)pd;
+      const void* q = nullptr;
+      const bool in_hbm = device_resident(res[i].pub_pos, &q) && device_resident(res[i].pub_data, &q);
+      if (!in_hbm && pub_staged + it.out_cap + pageable_need <= c.max_publish) {
+        // pinned host arrays: published into device staging, then streamed
+        // out by k_pub_copyout in whole 16-byte stores
+        it.out_pos = L.d_pub_pos + 3 * pub_staged;
+        it.out_data = L.d_pub_data + pub_staged;
+        it.host_pos = (float*)pp;
+        it.host_data = (float2*)pd;
+        pub_staged += it.out_cap;
+        copyout = true;
+      } else {
+        it.out_pos = (float*)pp;
+        it.out_data = (float2*)pd;
+      }
     } else {
       long long cap = it.out_cap;
       if (pub_staged + cap > c.max_publish)
@@ -551,7 +577,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[0], L.stream));
   CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr), cudaMemcpyHostToDevice, L.stream));
   CK(cudaMemcpyAsync(L.d_items, items, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
-  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0));
+  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   CK(cudaMemcpyAsync(L.h_stats, L.ctx.item_stats, sizeof(long long) * ST_COUNT * n, cudaMemcpyDeviceToHost, L.stream));
   CK(cudaMemcpyAsync(L.h_ctr, L.ctx.ctr, sizeof(LaneCounters), cudaMemcpyDeviceToHost, L.stream));

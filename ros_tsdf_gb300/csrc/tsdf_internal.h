@@ -66,6 +66,8 @@ struct ItemDev {
   float* out_pos;         // published positions (device-accessible) or null
   float2* out_data;       // published voxels (device-accessible)
   long long out_cap;
+  float* host_pos;        // pinned host outputs (device-mapped) that k_pub_copyout fills from out_pos /
+  float2* host_data;      // out_data (device staging), or null
   const char* src;        // pinned host points (device-mapped) that k_stage_points copies to pts, or null
   long long src_bytes;    // bytes the points span at src
   long long chunk_base;   // first staging chunk of this item (non-decreasing over items)
@@ -86,6 +88,8 @@ enum {
   II_PUB_BASE,     // publish prefix at the item's first slot
   II_GC_BASE,      // gc prefix at the item's first slot
   II_GC_N,         // blocks collected
+  II_CO_BASE,      // first copy-out chunk of the item's positions (k_pub_copyout)
+  II_CO_MID,       // first copy-out chunk of its voxel data
   II_COUNT
 };
 
@@ -115,6 +119,7 @@ struct LaneCounters {
   long long n_rec_live;   // live routing records after the first sort pass
   long long n_seg;        // segments (distinct blocks updated)
   long long n_enum;       // enumerated slots for publish / gc
+  long long n_co_chunks;  // copy-out chunks of the published outputs (k_pub_copyout)
   long long scan_total;   // scratch for scans
   long long n_heavy;      // segments with more records than one update chunk
   unsigned long long bin_cursor;  // bump allocator of the heavy-segment bins
@@ -209,6 +214,7 @@ struct LaunchCfg {
   int rank_passes;
   int rec_passes;
   int staged;            // pinned host inputs are copied in by k_stage_points
+  int copyout;           // published voxels for pinned host outputs leave through k_pub_copyout
   cudaStream_t side;     // second and third streams of the lane: a stage may fork
   cudaStream_t side2;    // work onto them
   cudaEvent_t ev_fork;   // and join it back (timing disabled; usable in graph capture)

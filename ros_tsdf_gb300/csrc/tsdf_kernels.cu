@@ -2318,6 +2318,98 @@ __global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
   }
 }
 
+// Published voxels for pinned host outputs are written to device staging by
+// k_pub_write and then streamed to the host arrays here: every 16-byte
+// aligned 16 bytes of an array leave as one store, so the host link carries
+// whole lines rather than the publish kernel's short per-block runs.  An
+// array of N bytes at host address D: head h = (16 - D mod 16) mod 16 bytes
+// (at most N), body = (N - h) rounded down to 16, tail the rest; chunk j of
+// the array covers body bytes [h + 4096 j, h + 4096 (j + 1)), one 16-byte
+// store per thread; chunk 0 also copies the head and tail words.
+struct CopyArray {
+  const char* src;
+  char* dst;
+  long long n;
+};
+
+__device__ __forceinline__ long long copy_chunks(const char* dst, long long n) {
+  if (n <= 0) return 0;
+  const long long h = min((long long)((16 - (reinterpret_cast<unsigned long long>(dst) & 15ull)) & 15ull), n);
+  const long long body = (n - h) & ~15ll;
+  return max(1ll, (body + kStageChunk - 1) / kStageChunk);
+}
+
+__device__ __forceinline__ CopyArray copy_array(const Ctx& c, int item, bool data) {
+  const ItemDev& it = c.items[item];
+  const long long k = min(c.item_stats[(long long)item * ST_COUNT + ST_PUB], it.out_cap);
+  CopyArray a;
+  a.src = data ? reinterpret_cast<const char*>(it.out_data) : reinterpret_cast<const char*>(it.out_pos);
+  a.dst = data ? reinterpret_cast<char*>(it.host_data) : reinterpret_cast<char*>(it.host_pos);
+  a.n = (a.dst == nullptr || k <= 0) ? 0 : k * (data ? 8 : 12);
+  return a;
+}
+
+// Chunk bases of every item's two arrays (one CTA; items <= kMaxItems).
+__global__ void __launch_bounds__(1024) k_copyout_plan(Ctx c) {
+  __shared__ int s_warp[32];
+  const int ni = c.hdr->n_items;
+  long long carry = 0;
+  for (int b = 0; b < ni; b += blockDim.x) {
+    const int i = b + threadIdx.x;
+    long long np = 0, nd = 0;
+    if (i < ni) {
+      const CopyArray p = copy_array(c, i, false), d = copy_array(c, i, true);
+      np = copy_chunks(p.dst, p.n);
+      nd = copy_chunks(d.dst, d.n);
+    }
+    int tot;
+    const int ex = block_excl_scan((int)(np + nd), s_warp, &tot);
+    if (i < ni) {
+      c.item_i[i * II_COUNT + II_CO_BASE] = (int)(carry + ex);
+      c.item_i[i * II_COUNT + II_CO_MID] = (int)(carry + ex + np);
+    }
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) c.ctr->n_co_chunks = carry;
+}
+
+__global__ void __launch_bounds__(256) k_pub_copyout(Ctx c) {
+  __shared__ int s_cb[kMaxItems];
+  const int ni = c.hdr->n_items;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) s_cb[i] = c.item_i[i * II_COUNT + II_CO_BASE];
+  __syncthreads();
+  const long long nch = c.ctr->n_co_chunks;
+  const int t = threadIdx.x;
+  for (long long ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+    int lo = 0, hi = ni - 1;  // the last item whose first chunk is <= ch
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_cb[mid] <= ch)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int cm = c.item_i[lo * II_COUNT + II_CO_MID];
+    const bool data = ch >= cm;
+    const long long j = ch - (data ? cm : s_cb[lo]);
+    const CopyArray a = copy_array(c, lo, data);
+    const long long h = min((long long)((16 - (reinterpret_cast<unsigned long long>(a.dst) & 15ull)) & 15ull), a.n);
+    const long long end = h + ((a.n - h) & ~15ll);
+    const long long off = h + j * kStageChunk + 16ll * t;
+    if (off + 16 <= end) {
+      const unsigned* s = reinterpret_cast<const unsigned*>(a.src + off);
+      *reinterpret_cast<uint4*>(a.dst + off) = make_uint4(s[0], s[1], s[2], s[3]);
+    }
+    if (j == 0 && t < 3) {
+      if (4 * t < h)
+        *reinterpret_cast<unsigned*>(a.dst + 4 * t) = *reinterpret_cast<const unsigned*>(a.src + 4 * t);
+      if (end + 4 * t < a.n)
+        *reinterpret_cast<unsigned*>(a.dst + end + 4 * t) = *reinterpret_cast<const unsigned*>(a.src + end + 4 * t);
+    }
+  }
+}
+
 // gc apply: free_list push in ascending slot order, entry tombstoned
 __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
   __shared__ int s_sb[kMaxItems];
@@ -2560,6 +2652,11 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
   k_item_bases<<<1, 1024, 0, s>>>(c, c.pub_prefix, &c.ctr->scan_total, II_PUB_BASE, -1, ST_PUB);
   k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c);
   *launches += 6;
+  if (lc.copyout) {
+    k_copyout_plan<<<1, 1024, 0, s>>>(c);
+    k_pub_copyout<<<lc.sm_count * 4, 256, 0, s>>>(c);
+    *launches += 2;
+  }
 }
 
 void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {

@@ -558,3 +558,41 @@ def test_step_timing_modes(built):
             outs.append([(r.count, r.pos.copy(), r.data.copy()) for r in res])
     for (ca, pa, da), (cb, pb, db) in zip(*outs):
         assert ca == cb and np.array_equal(pa, pb) and np.array_equal(da, db)
+
+
+def test_pinned_outputs_copied_out_match_oracle(built):
+    """Pinned host output arrays (page-aligned, and 4- and 8-byte offset views
+    that need the head/tail words) are filled by the copy-out kernel from
+    device staging; pageable ones by the DMA engine; with a publish cap
+    below the count (truncation), and with staging too small for the pinned
+    arrays (the publish kernel then writes them directly).  All bit-exact
+    with the oracle."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    specs = _mixed_specs()[:6]
+    srcs = [W.ScanSource(s) for s in specs]
+    scans = [[src.scan(k) for src in srcs] for k in range(3)]
+    pool = sum(s.heap_blocks for s in specs)
+    for max_publish in (1 << 23, 1 << 12):
+        orcs = [_oracle(s.params, s.heap_blocks) for s in specs]
+        with Engine(max_maps=8, pool_blocks=pool, max_batch_points=1 << 18, max_publish=max_publish) as eng:
+            mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+            for k in range(3):
+                outs, caps = [], []
+                for i in range(len(specs)):
+                    cap = 777 if (i == 0 and k == 1) else (1 << 18)
+                    form = (i + k) % (3 if max_publish > (1 << 20) else 2)  # pageable needs staging
+                    if form == 0:
+                        pos, dat = eng.pinned_empty((cap, 3), np.float32), eng.pinned_empty((cap, 2), np.float32)
+                    elif form == 1:
+                        bp = eng.pinned_empty((cap * 3 + 1,), np.float32)
+                        bd = eng.pinned_empty((cap * 2 + 2,), np.float32)
+                        pos, dat = bp[1:].reshape(cap, 3), bd[2:].reshape(cap, 2)
+                    else:
+                        pos, dat = np.empty((cap, 3), np.float32), np.empty((cap, 2), np.float32)
+                    outs.append((pos, dat))
+                    caps.append(cap)
+                rs = eng.integrate_batch([(mids[i], *scans[k][i]) for i in range(len(specs))], outputs=outs)
+                for i, r in enumerate(rs):
+                    assert_scan_equal(r, orcs[i].integrate(*scans[k][i], pub_cap=caps[i]),
+                                      specs[i].params.truncation_distance, f"max_publish {max_publish} step {k} map {i}")
