@@ -1554,170 +1554,6 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
   return make_float2(sdf, W);
 }
 
-// A hot chain run by a pair of warps.  The chain warp (lane 0) runs the
-// updates from shared memory and stores each update's a = RN(W sdf) + w d;
-// the loader warp stages the bins 64 at a time (two slots, two batches
-// ahead in registers) and checks the stored a values of every finished batch
-// against the Markstein range, so the chain's own instruction stream holds
-// only the shared loads, the five floating-point operations and one store
-// per update.  The warps hand the slots over with named barriers (bar.sync /
-// bar.arrive, 64 threads): FULL[s] = id + s, EMPTY[s] = id + 2 + s, DONE =
-// id + 4.  Per chain the loader arrives on FULL once per batch and waits on
-// EMPTY once per batch, the chain warp the other way round, and DONE closes
-// the chain; a chain of n = 0 sent on FULL[0] stops both.
-constexpr int kPairBatch = 64;
-constexpr int kPairBarriers = 5;
-
-struct PairSlots {
-  float4 tile[2][kPairBatch];
-  float a[2][kPairBatch];
-  HotChain hc;
-  int bad;
-};
-
-__device__ __forceinline__ void named_sync(int id) {
-  asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
-}
-__device__ __forceinline__ void named_arrive(int id) {
-  asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory");
-}
-
-// The loader warp: takes chains off the queue (long list first), stages
-// their bins and checks the chain warp's a values.
-__device__ void pair_loader(const HotChain* hot, long long nl, long long ns, long long half,
-                            unsigned long long* queue, const float4* hbin, PairSlots& ps, int lane, int bar) {
-  const float4 pad = make_float4(0.f, 1.f, 1.f, 0.f);
-  while (true) {
-    long long q = 0;
-    if (lane == 0) q = (long long)atomicAdd(queue, 1ull);
-    q = __shfl_sync(kFull, q, 0);
-    HotChain hc;
-    hc.n = 0;
-    if (q < nl + ns) hc = q < nl ? hot[q] : hot[half + (q - nl)];
-    if (lane == 0) ps.hc = hc;
-    const int n = hc.n;
-    if (n <= 0) {
-      __syncwarp();
-      named_arrive(bar);
-      return;
-    }
-    const float4* bins = hbin + hc.bin;
-    const int nb = (n + kPairBatch - 1) / kPairBatch;
-    float4 r0 = lane < n ? bins[lane] : pad;
-    float4 r1 = lane + 32 < n ? bins[lane + 32] : pad;
-    float4 r2 = lane + 64 < n ? bins[lane + 64] : pad;
-    float4 r3 = lane + 96 < n ? bins[lane + 96] : pad;
-    bool bad = false;
-    for (int b = 0; b < nb + 2; ++b) {
-      const int s = b & 1;
-      if (b >= 2) {
-        named_sync(bar + 2 + s);  // the chain warp is done with batch b - 2
-        const int m = min(kPairBatch, n - (b - 2) * kPairBatch);
-        bad |= (lane < m && !markstein_range(ps.a[s][lane])) | (lane + 32 < m && !markstein_range(ps.a[s][lane + 32]));
-      }
-      if (b < nb) {
-        ps.tile[s][lane] = r0;
-        ps.tile[s][lane + 32] = r1;
-        __syncwarp();
-        named_arrive(bar + s);
-        r0 = r2;
-        r1 = r3;
-        const int i = (b + 2) * kPairBatch + lane;
-        r2 = i < n ? bins[i] : pad;
-        r3 = i + 32 < n ? bins[i + 32] : pad;
-      }
-    }
-    bad = __any_sync(kFull, bad);
-    if (lane == 0) ps.bad = bad ? 1 : 0;
-    __syncwarp();
-    named_arrive(bar + 4);
-  }
-}
-
-// The chain warp: the update rule over the staged batches (below max_weight:
-// weight chain by lane 0, reciprocals by all lanes, sdf chain by lane 0, as
-// in warp_chain; at max_weight: the precomputed saturated bins), then the
-// exact redo when the loader flagged an a or the result is NaN.
-__device__ void pair_chain(float2* voxels, const float4* hbin, PairSlots& ps, int lane, int bar) {
-  while (true) {
-    named_sync(bar);  // FULL[0]: the first batch, or the stop
-    const HotChain hc = ps.hc;
-    if (hc.n <= 0) return;
-    const int n = hc.n;
-    const float maxw = hc.maxw;
-    float2* v = voxels + (long long)hc.phys * kVoxelsPerBlock + hc.local;
-    const float2 v0 = *v;
-    float sdf = v0.x, W = v0.y;
-    const int nb = (n + kPairBatch - 1) / kPairBatch;
-    for (int b = 0; b < nb; ++b) {
-      const int s = b & 1;
-      if (b > 0) named_sync(bar + s);
-      float4* tl = ps.tile[s];
-      float* ab = ps.a[s];
-      const int m = min(kPairBatch, n - b * kPairBatch);
-      if (__shfl_sync(kFull, W, 0) != maxw) {
-        if (lane == 0) {
-          for (int k = 0; k < m; ++k) {
-            const float nw = fadd(W, tl[k].w);
-            tl[k].y = nw;
-            tl[k].w = W;
-            W = fminf(nw, maxw);
-          }
-        }
-        __syncwarp();
-        for (int k = lane; k < m; k += 32) {
-          const float nw = tl[k].y;
-          tl[k].z = markstein_range(nw) ? __frcp_rn(nw) : __uint_as_float(0x7FC00000u);
-        }
-        __syncwarp();
-        if (lane == 0) {
-          for (int k = 0; k < m; ++k) {
-            const float4 x = tl[k];
-            const float a = fadd(fmul(x.w, sdf), x.x);
-            ab[k] = a;
-            const float qq = __fmul_rn(a, x.z);
-            const float rr = __fmaf_rn(-x.y, qq, a);
-            sdf = __fmaf_rn(rr, x.z, qq);
-          }
-        }
-      } else if (lane == 0) {
-        if (m == kPairBatch) {
-#pragma unroll
-          for (int k = 0; k < kPairBatch; ++k) {
-            const float4 x = tl[k];
-            const float a = fadd(fmul(maxw, sdf), x.x);
-            ab[k] = a;
-            const float qq = __fmul_rn(a, x.z);
-            const float rr = __fmaf_rn(-x.y, qq, a);
-            sdf = __fmaf_rn(rr, x.z, qq);
-          }
-        } else {
-          for (int k = 0; k < m; ++k) {
-            const float4 x = tl[k];
-            const float a = fadd(fmul(maxw, sdf), x.x);
-            ab[k] = a;
-            const float qq = __fmul_rn(a, x.z);
-            const float rr = __fmaf_rn(-x.y, qq, a);
-            sdf = __fmaf_rn(rr, x.z, qq);
-          }
-        }
-      }
-      __syncwarp();
-      named_arrive(bar + 2 + s);
-    }
-    named_sync(bar + 4);  // DONE: the loader has checked every batch
-    if (lane == 0) {
-      float2 r = make_float2(sdf, W);
-      if (ps.bad != 0 || sdf != sdf) {
-        r = v0;
-        chain_redo(&r.x, &r.y, hbin + hc.bin, n, maxw);
-      }
-      *v = r;
-    }
-    __syncwarp();
-  }
-}
-
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
@@ -2653,8 +2489,14 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
   k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c);
   *launches += 6;
   if (lc.copyout) {
-    k_copyout_plan<<<1, 1024, 0, s>>>(c);
-    k_pub_copyout<<<lc.sm_count * 4, 256, 0, s>>>(c);
+    // the copy to the host arrays runs on a side stream beside the gc stage
+    // (which touches neither the staging nor the publish counts); the gc
+    // stage joins it
+    cudaEventRecord(lc.ev_fork, s);
+    cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
+    k_copyout_plan<<<1, 1024, 0, lc.side>>>(c);
+    k_pub_copyout<<<lc.sm_count * 4, 256, 0, lc.side>>>(c);
+    cudaEventRecord(lc.ev_join, lc.side);
     *launches += 2;
   }
 }
@@ -2670,6 +2512,7 @@ void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* laun
   k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
   k_gc_finalize<<<1, 1024, 0, s>>>(c);
   *launches += 6;
+  if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
 }
 
 void launch_map_init(float2* voxels, unsigned long long* slot_key, int* nnz, int* free_list, HEntry* hash,
