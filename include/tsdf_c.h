@@ -136,8 +136,14 @@ typedef struct tsdf_scan {
 #define TSDF_MSG_BYTES(cap) (20 + 20 * (int64_t)(cap))
 
 /* Where one scan's published voxels go.  Pointers may be host (pinned or
- * pageable) or device memory; pinned and device buffers are written by the
- * publish kernel directly.  With pub_format TSDF_PUB_TSDF_MSG, pub_pos is a
+ * pageable) or device memory.  Device buffers are written by the publish
+ * kernel directly; pinned host arrays through the engine's publish staging
+ * (max_publish voxels per step) and a copy-out kernel that streams them over
+ * the host link in whole 16-byte stores, or directly when the staging has no
+ * room left; pageable arrays through the staging and one DMA copy each.
+ * Input points: device memory is read in place; pinned host points are
+ * copied in by one kernel for the whole batch, pageable ones by one DMA copy
+ * per scan.  With pub_format TSDF_PUB_TSDF_MSG, pub_pos is a
  * pinned or device buffer of TSDF_MSG_BYTES(pub_cap) bytes that receives the
  * message (pub_data is unused): the publish kernel writes the voxel records,
  * the engine the header and trailer, min(count, pub_cap) voxels in all. */
