@@ -313,6 +313,8 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.hist, 256ll * std::max(max_tiles_rank, max_tiles_rec), tr));
   TRY(dalloc(eng, &x.digit_tot, 256, tr));
   TRY(dalloc(eng, &x.tile_sums, max_tiles_scan + 1, tr));
+  TRY(dalloc(eng, &x.tile_sums2, max_tiles_scan + 1, tr));
+  TRY(dalloc(eng, &x.tile_sums3, max_tiles_scan + 1, tr));
   TRY(dalloc(eng, &x.seg_start, rec_cap, tr));
   TRY(dalloc(eng, &x.seg_item, rec_cap, tr));
   TRY(dalloc(eng, &x.enum_cnt, enum_cap, tr));

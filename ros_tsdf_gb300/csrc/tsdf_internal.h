@@ -128,6 +128,11 @@ struct LaneCounters {
   unsigned long long hbin_cursor;  // bump allocator of hbin
   unsigned long long n_hot_long;   // hot chains pushed (may exceed the list's half capacity)
   unsigned long long n_hot_short;
+  long long scan_total2;  // gc flag total (k_enum_flags)
+  unsigned done_seg;      // CTA tickets of the scans whose last CTA finishes the scan
+  unsigned done_enum;
+  unsigned done_pub;
+  unsigned done_gc;
   int error;              // bit flags, see ERR_*
   int pad;
 };
@@ -170,6 +175,8 @@ struct Ctx {
   int* hist;                     // [256][max_tiles]
   int* digit_tot;                // [256]
   int* tile_sums;                // scan tiles
+  int* tile_sums2;               // publish-flag tile sums (accumulated; zeroed by k_step_init)
+  int* tile_sums3;               // gc-flag tile sums (likewise)
   int* seg_start;
   int* seg_item;                 // batch item (map scan) of each segment
   int* enum_cnt;                 // publish counts per enumerated slot

@@ -424,6 +424,7 @@ __global__ void k_step_init(Ctx c) {
     c.item_stats[i] = v;
   }
   for (int i = t; i < h.n_items * II_COUNT; i += gridDim.x * blockDim.x) c.item_i[i] = 0;
+  for (int i = t; i <= c.max_tiles_scan; i += gridDim.x * blockDim.x) c.tile_sums2[i] = 0, c.tile_sums3[i] = 0;
 }
 
 // ----------------------------------------------------------------------------
@@ -587,8 +588,37 @@ __device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total) {
   return warp_off + x - v;
 }
 
+// True in the CTA that finishes last.  Every thread fences its own writes
+// before its CTA takes a ticket, so the last CTA sees all of them through L2
+// (it reads them with __ldcg).  All threads of every CTA must call it.
+__device__ __forceinline__ bool last_cta(unsigned* done) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return s_last;
+}
+
+// Exclusive scan of the tile sums in place by one CTA; returns the total.
+__device__ __forceinline__ long long scan_tile_sums(int* tile_sums, long long ntiles, int* s_warp) {
+  long long carry = 0;
+  for (long long b = 0; b < ntiles; b += blockDim.x) {
+    const long long i = b + threadIdx.x;
+    const int v = i < ntiles ? __ldcg(tile_sums + i) : 0;
+    int tot;
+    const int ex = block_excl_scan(v, s_warp, &tot);
+    if (i < ntiles) tile_sums[i] = (int)(carry + ex);
+    carry += tot;
+  }
+  return carry;
+}
+
+// Tile sums, then (in the CTA that finishes last) their exclusive scan and
+// the total: the reduce and top levels of the scan in one launch.
 template <class F>
-__global__ void __launch_bounds__(SC_T) k_scan_reduce(F f, const long long* n_ptr, int* tile_sums) {
+__global__ void __launch_bounds__(SC_T) k_scan_reduce(F f, const long long* n_ptr, int* tile_sums,
+                                                      long long* total_out, unsigned* done) {
   __shared__ int s_warp[32];
   const long long n = *n_ptr;
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
@@ -602,22 +632,10 @@ __global__ void __launch_bounds__(SC_T) k_scan_reduce(F f, const long long* n_pt
     block_excl_scan(sum, s_warp, &tot);
     if (threadIdx.x == 0) tile_sums[tile] = tot;
   }
-}
-
-__global__ void __launch_bounds__(1024) k_scan_top(int* tile_sums, const long long* n_ptr, long long* total_out) {
-  __shared__ int s_warp[32];
-  const long long n = *n_ptr;
-  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
-  long long carry = 0;
-  for (long long b = 0; b < ntiles; b += blockDim.x) {
-    long long i = b + threadIdx.x;
-    int v = i < ntiles ? tile_sums[i] : 0;
-    int tot;
-    int ex = block_excl_scan(v, s_warp, &tot);
-    if (i < ntiles) tile_sums[i] = (int)(carry + ex);
-    carry += tot;
+  if (last_cta(done)) {
+    const long long tot = scan_tile_sums(tile_sums, ntiles, s_warp);
+    if (threadIdx.x == 0) *total_out = tot;
   }
-  if (threadIdx.x == 0 && total_out) *total_out = carry;
 }
 
 template <class F, class O>
@@ -2022,60 +2040,94 @@ __device__ __forceinline__ int find_item_i(const int* base, int n, long long e) 
   return lo;
 }
 
+// Publish and gc flags of every enumerated slot, one slot per thread; each
+// warp adds its 32 slots' flags to their scan tile's sums (tile_sums2:
+// voxels to publish, tile_sums3: blocks to collect; zeroed at step start),
+// and the CTA that finishes last scans both: the reduce and top levels of the
+// publish and gc scans in this one launch.
 __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
   __shared__ int s_sb[kMaxItems];
+  __shared__ int s_warp[32];
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
+  const int lane = threadIdx.x & 31;
   const long long n = c.ctr->n_enum;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    int item = find_item_i(s_sb, h.n_items, e);
-    const ItemDev& it = c.items[item];
-    const MapDev& m = c.maps[it.map];
-    long long phys = m.heap_base + (e - s_sb[item]);
-    unsigned long long key = c.slot_key[phys];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long w0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += stride) {
+    const long long e = w0 + lane;
     int cnt = 0, gc = 0;
-    if (key != kEmptyKey) {
-      int kx, ky, kz;
-      unpack_key(key, &kx, &ky, &kz);
-      float cx = fadd(div_const((float)kx, m.scale_b, m.rs_b), m.half_bs);
-      float cy = fadd(div_const((float)ky, m.scale_b, m.rs_b), m.half_bs);
-      float cz = fadd(div_const((float)kz, m.scale_b, m.rs_b), m.half_bs);
-      // withinDistanceSquared (tsdf_handler.cu:749-757): diff = lidar - block
-      float d2 = sq3(fsub(it.ox, cx), fsub(it.oy, cy), fsub(it.oz, cz));
-      if (d2 <= m.pub_d2) cnt = c.nnz[phys];
-      gc = (d2 <= m.gc_d2) ? 0 : 1;
-      if (cnt > 0) stat_add(c.item_stats, item, ST_PUBBLK, 1);
+    if (e < n) {
+      int item = find_item_i(s_sb, h.n_items, e);
+      const ItemDev& it = c.items[item];
+      const MapDev& m = c.maps[it.map];
+      long long phys = m.heap_base + (e - s_sb[item]);
+      unsigned long long key = c.slot_key[phys];
+      if (key != kEmptyKey) {
+        int kx, ky, kz;
+        unpack_key(key, &kx, &ky, &kz);
+        float cx = fadd(div_const((float)kx, m.scale_b, m.rs_b), m.half_bs);
+        float cy = fadd(div_const((float)ky, m.scale_b, m.rs_b), m.half_bs);
+        float cz = fadd(div_const((float)kz, m.scale_b, m.rs_b), m.half_bs);
+        // withinDistanceSquared (tsdf_handler.cu:749-757): diff = lidar - block
+        float d2 = sq3(fsub(it.ox, cx), fsub(it.oy, cy), fsub(it.oz, cz));
+        if (d2 <= m.pub_d2) cnt = c.nnz[phys];
+        gc = (d2 <= m.gc_d2) ? 0 : 1;
+        if (cnt > 0) stat_add(c.item_stats, item, ST_PUBBLK, 1);
+      }
+      c.enum_cnt[e] = cnt;
+      c.enum_gc[e] = gc;
     }
-    c.enum_cnt[e] = cnt;
-    c.enum_gc[e] = gc;
+    // a warp's 32 slots lie in one tile (tiles are multiples of 32 slots)
+    const int sp = __reduce_add_sync(kFull, cnt);
+    const int sg = __reduce_add_sync(kFull, gc);
+    if (lane == 0) {
+      if (sp) atomicAdd(&c.tile_sums2[w0 / SC_TILE], sp);
+      if (sg) atomicAdd(&c.tile_sums3[w0 / SC_TILE], sg);
+    }
+  }
+  if (last_cta(&c.ctr->done_enum)) {
+    const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
+    const long long tp = scan_tile_sums(c.tile_sums2, ntiles, s_warp);
+    const long long tg = scan_tile_sums(c.tile_sums3, ntiles, s_warp);
+    if (threadIdx.x == 0) {
+      c.ctr->scan_total = tp;
+      c.ctr->scan_total2 = tg;
+    }
   }
 }
 
-struct ArrIn {
-  const int* a;
-  __device__ int operator()(long long i) const { return a[i]; }
-};
-struct PrefixOut {
-  int* p;
-  __device__ void operator()(long long i, int prefix, int) const { p[i] = prefix; }
-};
-
-// per-item bases of a scanned enumeration array
-__global__ void __launch_bounds__(1024) k_item_bases(Ctx c, const int* prefix, const long long* total,
-                                                     int base_field, int count_field, int stat_field) {
-  const int n = c.hdr->n_items;
-  const int i = threadIdx.x;
-  if (i >= n) return;
-  const long long ne = c.ctr->n_enum;
+// The apply level of a scan of an enumeration array (flags -> prefix), then,
+// in the CTA that finishes last, every item's base and count in that prefix
+// (its slots are the enumeration range [SLOT_BASE, SLOT_BASE + SLOT_N)).
+__global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, const int* flags, int* prefix, const int* tile_offs,
+                                                     const long long* total, int base_field, int count_field,
+                                                     int stat_field, unsigned* done) {
+  __shared__ int s_warp[32];
+  const long long n = c.ctr->n_enum;
+  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int carry = tile_offs[tile];
+    for (int r = 0; r < SC_IPT; ++r) {
+      const long long i = tile * SC_TILE + r * SC_T + threadIdx.x;
+      const int v = i < n ? flags[i] : 0;
+      int tot;
+      const int ex = block_excl_scan(v, s_warp, &tot);
+      if (i < n) prefix[i] = carry + ex;
+      carry += tot;
+    }
+  }
+  if (!last_cta(done)) return;
   const long long tot = *total;
-  const long long sb = c.item_i[i * II_COUNT + II_SLOT_BASE];
-  const long long se = sb + c.item_i[i * II_COUNT + II_SLOT_N];
-  const long long b = sb < ne ? prefix[sb] : tot;
-  const long long e = se < ne ? prefix[se] : tot;
-  c.item_i[i * II_COUNT + base_field] = (int)b;
-  if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
-  if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
+  for (int i = threadIdx.x; i < c.hdr->n_items; i += blockDim.x) {
+    const long long sb = c.item_i[i * II_COUNT + II_SLOT_BASE];
+    const long long se = sb + c.item_i[i * II_COUNT + II_SLOT_N];
+    const long long b = sb < n ? __ldcg(prefix + sb) : tot;
+    const long long e = se < n ? __ldcg(prefix + se) : tot;
+    c.item_i[i * II_COUNT + base_field] = (int)b;
+    if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
+    if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
+  }
 }
 
 // publish write: one warp per enumerated slot (grid-strided), the block's 4 KiB
@@ -2440,8 +2492,7 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   SegHeadIn fin{c.rec_key[sel]};
   SegHeadOut fout{c.seg_start};
   const int grid = lc.sm_count * 2;
-  k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums);
-  k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_rec_live, &c.ctr->n_seg);
+  k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums, &c.ctr->n_seg, &c.ctr->done_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
   k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c, sel);
   *launches += 4;
@@ -2480,14 +2531,10 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
   k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c);
-  ArrIn cin{c.enum_cnt};
-  PrefixOut pout{c.pub_prefix};
-  k_scan_reduce<<<grid, SC_T, 0, s>>>(cin, &c.ctr->n_enum, c.tile_sums);
-  k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_enum, &c.ctr->scan_total);
-  k_scan_apply<<<grid, SC_T, 0, s>>>(cin, pout, &c.ctr->n_enum, c.tile_sums);
-  k_item_bases<<<1, 1024, 0, s>>>(c, c.pub_prefix, &c.ctr->scan_total, II_PUB_BASE, -1, ST_PUB);
+  k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_cnt, c.pub_prefix, c.tile_sums2, &c.ctr->scan_total, II_PUB_BASE, -1,
+                                     ST_PUB, &c.ctr->done_pub);
   k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c);
-  *launches += 6;
+  *launches += 3;
   if (lc.copyout) {
     // the copy to the host arrays runs on a side stream beside the gc stage
     // (which touches neither the staging nor the publish counts); the gc
@@ -2503,15 +2550,11 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
 
 void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
-  ArrIn gin{c.enum_gc};
-  PrefixOut gout{c.gc_prefix};
-  k_scan_reduce<<<grid, SC_T, 0, s>>>(gin, &c.ctr->n_enum, c.tile_sums);
-  k_scan_top<<<1, 1024, 0, s>>>(c.tile_sums, &c.ctr->n_enum, &c.ctr->scan_total);
-  k_scan_apply<<<grid, SC_T, 0, s>>>(gin, gout, &c.ctr->n_enum, c.tile_sums);
-  k_item_bases<<<1, 1024, 0, s>>>(c, c.gc_prefix, &c.ctr->scan_total, II_GC_BASE, II_GC_N, -1);
+  k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_gc, c.gc_prefix, c.tile_sums3, &c.ctr->scan_total2, II_GC_BASE, II_GC_N,
+                                     -1, &c.ctr->done_gc);
   k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
   k_gc_finalize<<<1, 1024, 0, s>>>(c);
-  *launches += 6;
+  *launches += 3;
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
 }
 
