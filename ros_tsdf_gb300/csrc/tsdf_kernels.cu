@@ -802,29 +802,35 @@ void radix_sort(const Ctx& c, unsigned* const* keys, unsigned* const* vals, cons
 
 // ----------------------------------------------------------------------------
 // allocation
-__global__ void k_gather_ranks(Ctx c) {
+// The new keys' (first-touch rank, hash entry) pairs for the rank sort; the
+// CTA that finishes last also writes every item's first index among the new
+// keys (exclusive prefix of the per-item new-key counts).
+__global__ void __launch_bounds__(256) k_gather_ranks(Ctx c) {
+  __shared__ int s_warp[32];
   const long long n = min(c.ctr->n_new, c.rank_cap);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     unsigned e = c.newlist[i];
     c.rank_key[0][i] = c.hash[e].rank;
     c.rank_val[0][i] = e;
   }
-}
-
-__global__ void __launch_bounds__(1024) k_alloc_prefix(Ctx c) {
-  __shared__ int s_warp[32];
-  const int n = c.hdr->n_items;
-  const int i = threadIdx.x;
-  const int v = i < n ? c.item_i[i * II_COUNT + II_NEW] : 0;
-  int tot;
-  const int ex = block_excl_scan(v, s_warp, &tot);
-  if (i < n) c.item_i[i * II_COUNT + II_NEW_BASE] = ex;
+  if (!last_cta(&c.ctr->done_gather)) return;
+  const int ni = c.hdr->n_items;
+  long long carry = 0;
+  for (int b = 0; b < ni; b += blockDim.x) {
+    const int i = b + threadIdx.x;
+    const int v = i < ni ? c.item_i[i * II_COUNT + II_NEW] : 0;
+    int tot;
+    const int ex = block_excl_scan(v, s_warp, &tot);
+    if (i < ni) c.item_i[i * II_COUNT + II_NEW_BASE] = (int)(carry + ex);
+    carry += tot;
+  }
 }
 
 // One warp per new block, in first-touch order: pop the free list, resolve
 // the pending entry, zero the 4 KiB block (the reference's new VoxelBlock()).
 __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel) {
   __shared__ long long s_pb[kMaxItems];
+  __shared__ int s_warp[32];
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
   __syncthreads();
@@ -866,29 +872,31 @@ __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel) {
       stat_add(c.item_stats, item, ST_HEAPFULL, 1);
     }
   }
-}
-
-// block_count += allocated; slot enumeration bases for publish / gc.
-__global__ void __launch_bounds__(1024) k_alloc_finalize(Ctx c) {
-  __shared__ int s_warp[32];
-  const int n = c.hdr->n_items;
-  const int i = threadIdx.x;
-  int hw = 0;
-  if (i < n) {
-    const int mi = c.items[i].map;
-    const int bc = c.mctr[mi].block_count;
-    const int nn = c.item_i[i * II_COUNT + II_NEW];
-    const int room = c.maps[mi].heap_cap - bc;
-    c.mctr[mi].block_count = bc + (nn < room ? nn : room);
-    hw = c.mctr[mi].hw;
+  // the CTA that finishes last: block_count += allocated, and the slot
+  // enumeration bases for publish / gc (items' high waters, prefix-summed)
+  if (!last_cta(&c.ctr->done_alloc)) return;
+  const int ni = h.n_items;
+  long long carry = 0;
+  for (int b = 0; b < ni; b += blockDim.x) {
+    const int i = b + threadIdx.x;
+    int hw = 0;
+    if (i < ni) {
+      const int mi = c.items[i].map;
+      const int bc = c.mctr[mi].block_count;
+      const int nn = c.item_i[i * II_COUNT + II_NEW];
+      const int room = c.maps[mi].heap_cap - bc;
+      c.mctr[mi].block_count = bc + (nn < room ? nn : room);
+      hw = __ldcg(&c.mctr[mi].hw);
+    }
+    int tot;
+    const int ex = block_excl_scan(hw, s_warp, &tot);
+    if (i < ni) {
+      c.item_i[i * II_COUNT + II_SLOT_BASE] = (int)(carry + ex);
+      c.item_i[i * II_COUNT + II_SLOT_N] = hw;
+    }
+    carry += tot;
   }
-  int tot;
-  const int ex = block_excl_scan(hw, s_warp, &tot);
-  if (i < n) {
-    c.item_i[i * II_COUNT + II_SLOT_BASE] = ex;
-    c.item_i[i * II_COUNT + II_SLOT_N] = hw;
-  }
-  if (i == 0) c.ctr->n_enum = tot;
+  if (threadIdx.x == 0) c.ctr->n_enum = carry;
 }
 
 // ----------------------------------------------------------------------------
@@ -1073,6 +1081,8 @@ __device__ __forceinline__ void mask_counts(const unsigned* m, int t, int a[4]) 
 
 // Per segment: its batch item (the scan of the entry of its first record) and,
 // for segments longer than one update chunk, a place on the heavy list.
+__device__ void heavy_plan_cta(const Ctx& c);
+
 __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
   __shared__ long long s_pb[kMaxItems];
   const BatchHdr h = *c.hdr;
@@ -1091,6 +1101,7 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
       c.heavy[k] = (int)j;
     }
   }
+  if (last_cta(&c.ctr->done_classify)) heavy_plan_cta(c);
 }
 
 
@@ -1098,10 +1109,12 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
 // Heavy segments: a multi-CTA counting sort of their updates into per-voxel
 // bins, ordered by point index.  plan -> per-chunk voxel counts -> per-voxel
 // scan over chunks -> ordered placement.  Segments whose chunks exceed the
-// scratch capacity fall back to the single-CTA passes in k_update.
-__global__ void __launch_bounds__(1024) k_heavy_plan(Ctx c) {
+// scratch capacity fall back to the single-CTA passes in k_update.  The plan
+// runs in the last CTA of k_seg_classify, which lists the heavy segments (it
+// reads the list through L2).
+__device__ void heavy_plan_cta(const Ctx& c) {
   __shared__ int s_warp[32];
-  const long long nh = c.ctr->n_heavy;
+  const long long nh = __ldcg(&c.ctr->n_heavy);
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
   const long long hcap = c.hchunk_cap / 2;
@@ -1110,7 +1123,7 @@ __global__ void __launch_bounds__(1024) k_heavy_plan(Ctx c) {
     const long long h = b + threadIdx.x;
     int nch = 0;
     if (h < nh) {
-      const long long j = c.heavy[h];
+      const long long j = __ldcg(c.heavy + h);
       const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
       nch = (int)((b1 - c.seg_start[j] + UPD_T - 1) / UPD_T);
     }
@@ -1128,7 +1141,7 @@ __global__ void __launch_bounds__(1024) k_heavy_plan(Ctx c) {
     long long n = 0;
     if (planned > 0) {
       const long long h = planned - 1;
-      const long long j = c.heavy[h];
+      const long long j = __ldcg(c.heavy + h);
       const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
       n = c.hchunk_base[h] + (b1 - c.seg_start[j] + UPD_T - 1) / UPD_T;
     }
@@ -2328,18 +2341,16 @@ __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
       set_error(c.ctr, ERR_HASH_FULL);
     }
   }
-}
-
-__global__ void __launch_bounds__(1024) k_gc_finalize(Ctx c) {
-  const int n = c.hdr->n_items;
-  const int i = threadIdx.x;
-  if (i >= n) return;
-  const int mi = c.items[i].map;
-  const int g = c.item_i[i * II_COUNT + II_GC_N];
-  const int bc = c.mctr[mi].block_count - g;
-  c.mctr[mi].block_count = bc;
-  c.item_stats[i * ST_COUNT + ST_GC] = g;
-  c.item_stats[i * ST_COUNT + ST_BC] = bc;
+  // the CTA that finishes last: block_count -= collected
+  if (!last_cta(&c.ctr->done_gcapply)) return;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) {
+    const int mi = c.items[i].map;
+    const int g = c.item_i[i * II_COUNT + II_GC_N];
+    const int bc = c.mctr[mi].block_count - g;
+    c.mctr[mi].block_count = bc;
+    c.item_stats[i * ST_COUNT + ST_GC] = g;
+    c.item_stats[i * ST_COUNT + ST_BC] = bc;
+  }
 }
 
 // ----------------------------------------------------------------------------
@@ -2463,14 +2474,11 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
   *launches += 1;
   radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
              lc.rank_passes, c.max_tiles_rank, lc.sm_count, s, launches);
-  k_alloc_prefix<<<1, 1024, 0, s>>>(c);
-  *launches += 1;
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1);
-  k_alloc_finalize<<<1, 1024, 0, s>>>(c);
-  *launches += 2;
+  *launches += 1;
 }
 
 void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
@@ -2500,12 +2508,11 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 
 void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int sel = lc.rec_passes & 1;
-  k_heavy_plan<<<1, 1024, 0, s>>>(c);
   k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c, sel);
   k_heavy_scan<<<lc.sm_count * 8, HS_T, 0, s>>>(c, sel);
   k_heavy_scan_large<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c, sel);
   k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
-  *launches += 5;
+  *launches += 4;
 }
 
 void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
@@ -2553,8 +2560,7 @@ void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* laun
   k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_gc, c.gc_prefix, c.tile_sums3, &c.ctr->scan_total2, II_GC_BASE, II_GC_N,
                                      -1, &c.ctr->done_gc);
   k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
-  k_gc_finalize<<<1, 1024, 0, s>>>(c);
-  *launches += 3;
+  *launches += 2;
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
 }
 
