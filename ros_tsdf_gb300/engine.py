@@ -208,17 +208,24 @@ class Engine:
         return res
 
     # -- served mode --------------------------------------------------------
-    def submit(self, map_id: int, xyz, origin, pub_cap: int = 400000):
-        """Queue a scan; returns a handle for wait().  Buffers are kept alive by the handle."""
+    def submit(self, map_id: int, xyz, origin, pub_cap: int = 400000, pinned: bool = False):
+        """Queue a scan; returns a handle for wait().  Buffers are kept alive by the handle.
+        pinned: copy the points into page-locked memory and receive the voxels
+        in page-locked arrays (the engine's fast host path)."""
         a, stride = _as_points(xyz)
+        if pinned and a.shape[0]:
+            p = self.pinned_empty(a.shape, np.float32)
+            p[:] = a
+            a, stride = p, a.shape[1] * 4
         sc = L.Scan()
         sc.map_id = int(map_id)
         sc.stride_bytes = stride
         sc.n_points = a.shape[0]
         sc.xyz = a.ctypes.data if a.shape[0] else None
         sc.origin[:] = [float(v) for v in origin]
-        pos = np.empty((pub_cap, 3), np.float32)
-        data = np.empty((pub_cap, 2), np.float32)
+        alloc = self.pinned_empty if pinned else (lambda shape, dt: np.empty(shape, dt))
+        pos = alloc((pub_cap, 3), np.float32)
+        data = alloc((pub_cap, 2), np.float32)
         rs = L.ScanResult()
         rs.pub_pos = pos.ctypes.data
         rs.pub_data = data.ctypes.data

@@ -238,9 +238,11 @@ def test_map_lifecycle_and_admission(built):
         assert r.stats["alloc_blocks_before"] == 0
 
 
-def test_served_mode_isolation(built):
+@pytest.mark.parametrize("pinned", [False, True])
+def test_served_mode_isolation(built, pinned):
     """Scans submitted asynchronously from many maps (continuous batching over
-    two lanes) give each map exactly its alone-and-in-order result."""
+    two lanes) give each map exactly its alone-and-in-order result, with
+    pageable buffers and with pinned ones (kernel staging and copy-out)."""
     from ros_tsdf_gb300 import Engine, workloads as W
 
     specs = _mixed_specs()[:6]
@@ -253,7 +255,7 @@ def test_served_mode_isolation(built):
         order = [(i, k) for k in range(3) for i in rng.permutation(len(specs))]
         tickets = {}
         for i, k in order:
-            tickets[(i, k)] = eng.submit(mids[i], *scans[i][k], pub_cap=1 << 20)
+            tickets[(i, k)] = eng.submit(mids[i], *scans[i][k], pub_cap=1 << 20, pinned=pinned)
             time.sleep(float(rng.uniform(0, 0.002)))
         results = {key: eng.wait(t, timeout_ms=60000) for key, t in tickets.items()}
     for i, s in enumerate(specs):
