@@ -119,6 +119,15 @@ struct Request {
   bool done = false;
 };
 
+// Where a caller's buffer lives: pageable host memory (or unknown), pinned
+// host memory mapped for the device, or device / managed memory; dev is the
+// address kernels use.
+enum { PTR_PAGEABLE = 0, PTR_PINNED = 1, PTR_DEVICE = 2 };
+struct PtrInfo {
+  int where = PTR_PAGEABLE;
+  const void* dev = nullptr;
+};
+
 struct Lane {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr, side2 = nullptr;
@@ -153,6 +162,7 @@ struct Lane {
   };
   std::vector<Staged> staged;
   std::vector<int> maps;
+  std::vector<PtrInfo> ptrs;  // per item: points, pub_pos, pub_data
 };
 
 }  // namespace
@@ -335,6 +345,10 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   CK(cudaMallocHost(&L.h_stats, sizeof(long long) * ST_COUNT * c.max_maps));
   CK(cudaMallocHost(&L.h_ctr, sizeof(LaneCounters)));
   CK(cudaMallocHost(&L.h_mctr, sizeof(MapCounters) * c.max_maps));
+  CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&x.out_stats), L.h_stats, 0));
+  CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&x.out_ctr), L.h_ctr, 0));
+  CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&x.out_mctr), L.h_mctr, 0));
+  x.n_mctr = c.max_maps;
   return TSDF_OK;
 }
 
@@ -408,21 +422,29 @@ tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_
   return TSDF_OK;
 }
 
-bool device_accessible(const void* p, const void** dev_ptr) {
+// One pointer query: where a caller's buffer lives and the address kernels use.
+PtrInfo ptr_info(const void* p) {
+  PtrInfo r;
   cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return r;
   }
   if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
-    *dev_ptr = a.devicePointer ? a.devicePointer : p;
-    return true;
+    r.where = PTR_DEVICE;
+    r.dev = a.devicePointer ? a.devicePointer : p;
+  } else if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    r.where = PTR_PINNED;
+    r.dev = a.devicePointer;
   }
-  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
-    *dev_ptr = a.devicePointer;
-    return true;
-  }
-  return false;
+  return r;
+}
+
+bool device_accessible(const void* p, const void** dev_ptr) {
+  const PtrInfo r = ptr_info(p);
+  if (r.where == PTR_PAGEABLE) return false;
+  *dev_ptr = r.dev;
+  return true;
 }
 
 // Device or managed memory, which kernels read in place.  Host memory is
@@ -430,16 +452,10 @@ bool device_accessible(const void* p, const void** dev_ptr) {
 // latency on every point load): pinned memory by k_stage_points, one launch
 // for the batch; pageable memory by the DMA engine, one copy per scan.
 bool device_resident(const void* p, const void** dev_ptr) {
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
-    *dev_ptr = a.devicePointer ? a.devicePointer : p;
-    return true;
-  }
-  return false;
+  const PtrInfo r = ptr_info(p);
+  if (r.where != PTR_DEVICE) return false;
+  *dev_ptr = r.dev;
+  return true;
 }
 
 // Validate a batch and enqueue it on lane L (asynchronous).  On success the
@@ -485,35 +501,40 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   if (total > c.max_batch_points)
     return fail(eng, TSDF_ERR_CAPACITY, "batch has " + std::to_string(total) + " points; capacity " +
                                             std::to_string(c.max_batch_points));
+  // where every buffer lives (one pointer query each)
+  L.ptrs.resize(3 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    L.ptrs[3 * i] = scans[i].n_points > 0 ? ptr_info(scans[i].xyz) : PtrInfo();
+    L.ptrs[3 * i + 1] = ptr_info(res[i].pub_pos);
+    L.ptrs[3 * i + 2] = res[i].pub_format == TSDF_PUB_ARRAYS ? ptr_info(res[i].pub_data) : PtrInfo();
+  }
   // inputs
   long long chunks = 0;
   bool copyout = false;
   // staging that pageable outputs need (pinned outputs use what is left)
   long long pageable_need = 0;
   for (int i = 0; i < n; ++i) {
-    const void* q = nullptr;
     if (res[i].pub_format == TSDF_PUB_ARRAYS && res[i].pub_cap > 0 &&
-        !(device_accessible(res[i].pub_pos, &q) && device_accessible(res[i].pub_data, &q)))
+        (L.ptrs[3 * i + 1].where == PTR_PAGEABLE || L.ptrs[3 * i + 2].where == PTR_PAGEABLE))
       pageable_need += res[i].pub_cap;
   }
   for (int i = 0; i < n; ++i) {
     const tsdf_scan& s = scans[i];
     ItemDev& it = items[i];
-    const void* dp = nullptr;
+    const PtrInfo& pin = L.ptrs[3 * i];
     it.chunk_base = chunks;
     if (s.n_points == 0) {
       it.pts = L.d_points;
-    } else if (device_resident(s.xyz, &dp)) {
-      it.pts = (const char*)dp;
+    } else if (pin.where == PTR_DEVICE) {
+      it.pts = (const char*)pin.dev;
     } else {
       // the bytes the points span: a strided view into wider records (a
       // PointCloud2 buffer) ends 12 bytes into its last record
       long long nb = (s.n_points - 1) * (long long)s.stride_bytes + 12;
       if (bytes + nb > c.max_batch_points * 16) return fail(eng, TSDF_ERR_CAPACITY, "point staging full");
-      const void* mp = nullptr;
-      if ((reinterpret_cast<uintptr_t>(s.xyz) & 3) == 0 && device_accessible(s.xyz, &mp)) {
+      if ((reinterpret_cast<uintptr_t>(s.xyz) & 3) == 0 && pin.where == PTR_PINNED) {
         // pinned: copied in by k_stage_points, one launch for the batch
-        it.src = (const char*)mp;
+        it.src = (const char*)pin.dev;
         it.src_bytes = nb;
         chunks += (nb + kStageChunk - 1) / kStageChunk;
       } else {
@@ -523,20 +544,21 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
       bytes += (nb + 15) & ~15ll;
     }
     // outputs
-    const void* pp = nullptr;
-    const void* pd = nullptr;
+    const PtrInfo& ppos = L.ptrs[3 * i + 1];
+    const PtrInfo& pdat = L.ptrs[3 * i + 2];
+    const void* pp = ppos.dev;
+    const void* pd = pdat.dev;
     it.out_cap = std::max<long long>(res[i].pub_cap, 0);
     it.out_fmt = res[i].pub_format;
     if (it.out_fmt == TSDF_PUB_TSDF_MSG) {
-      if (it.out_cap > 0 && !device_accessible(res[i].pub_pos, &pp))
+      if (it.out_cap > 0 && ppos.where == PTR_PAGEABLE)
         return fail(eng, TSDF_ERR_INVALID_ARG, "a Tsdf message output needs a pinned or device buffer");
       it.out_pos = (float*)pp;
       it.out_data = nullptr;
     } else if (it.out_fmt != TSDF_PUB_ARRAYS) {
       return fail(eng, TSDF_ERR_INVALID_ARG, "unknown pub_format");
-    } else if (it.out_cap > 0 && device_accessible(res[i].pub_pos, &pp) && device_accessible(res[i].pub_data, &pd)) {
-      const void* q = nullptr;
-      const bool in_hbm = device_resident(res[i].pub_pos, &q) && device_resident(res[i].pub_data, &q);
+    } else if (it.out_cap > 0 && ppos.where != PTR_PAGEABLE && pdat.where != PTR_PAGEABLE) {
+      const bool in_hbm = ppos.where == PTR_DEVICE && pdat.where == PTR_DEVICE;
       if (!in_hbm && pub_staged + it.out_cap + pageable_need <= c.max_publish) {
         // pinned host arrays: published into device staging, then streamed
         // out by k_pub_copyout in whole 16-byte stores
@@ -581,10 +603,8 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   CK(cudaMemcpyAsync(L.d_items, items, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
   TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
-  CK(cudaMemcpyAsync(L.h_stats, L.ctx.item_stats, sizeof(long long) * ST_COUNT * n, cudaMemcpyDeviceToHost, L.stream));
-  CK(cudaMemcpyAsync(L.h_ctr, L.ctx.ctr, sizeof(LaneCounters), cudaMemcpyDeviceToHost, L.stream));
-  CK(cudaMemcpyAsync(L.h_mctr, eng->d_mctr, sizeof(MapCounters) * eng->maps.size(), cudaMemcpyDeviceToHost,
-                     L.stream));
+  // the step's stats and counters reach L.h_stats / h_ctr / h_mctr through
+  // k_step_report, the graph's last kernel
   CK(cudaEventRecord(L.ev_done, L.stream));
   for (int i = 0; i < n; ++i) {
     eng->maps[scans[i].map_id].in_flight = true;

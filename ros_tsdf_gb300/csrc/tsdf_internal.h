@@ -164,6 +164,12 @@ struct Ctx {
   HEntry* hash;                  // all maps' tables
   const MapDev* maps;
   MapCounters* mctr;
+  // pinned host mirrors (device-mapped) that k_step_report fills at the end of
+  // every step: per-item stats, the lane's counters, every map's counters
+  long long* out_stats;
+  LaneCounters* out_ctr;
+  MapCounters* out_mctr;
+  int n_mctr;
   // lane state
   const BatchHdr* hdr;
   const ItemDev* items;

@@ -2353,6 +2353,19 @@ __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
   }
 }
 
+// The step's results for the host, written into its pinned mirrors by the
+// graph's last kernel (instead of three copies after the graph): the items'
+// stats, the lane's counters (error flags) and every map's counters.
+__global__ void __launch_bounds__(256) k_step_report(Ctx c) {
+  const int t = threadIdx.x;
+  const long long ns = (long long)c.hdr->n_items * ST_COUNT;
+  for (long long i = t; i < ns; i += blockDim.x) c.out_stats[i] = c.item_stats[i];
+  const unsigned* src = reinterpret_cast<const unsigned*>(c.ctr);
+  unsigned* dst = reinterpret_cast<unsigned*>(c.out_ctr);
+  for (int i = t; i < (int)(sizeof(LaneCounters) / 4); i += blockDim.x) dst[i] = src[i];
+  for (int i = t; i < c.n_mctr; i += blockDim.x) c.out_mctr[i] = c.mctr[i];
+}
+
 // ----------------------------------------------------------------------------
 // map maintenance
 __global__ void k_map_init(int* free_list, unsigned long long* slot_key, int* nnz, long long heap_base,
@@ -2562,6 +2575,8 @@ void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* laun
   k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
   *launches += 2;
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
+  k_step_report<<<1, 256, 0, s>>>(c);
+  *launches += 1;
 }
 
 void launch_map_init(float2* voxels, unsigned long long* slot_key, int* nnz, int* free_list, HEntry* hash,
