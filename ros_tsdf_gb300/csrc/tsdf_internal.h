@@ -120,6 +120,8 @@ struct LaneCounters {
   long long n_seg;        // segments (distinct blocks updated)
   long long n_enum;       // enumerated slots for publish / gc
   long long n_co_chunks;  // copy-out chunks of the published outputs (k_pub_copyout)
+  long long co_split_item;   // the publish kernel's two parts: items [0, split) and [split, n)
+  long long co_split_chunk;  // first copy-out chunk of the second part
   long long scan_total;   // scratch for scans
   long long n_heavy;      // segments with more records than one update chunk
   unsigned long long bin_cursor;  // bump allocator of the heavy-segment bins

@@ -2113,9 +2113,11 @@ __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
 // The apply level of a scan of an enumeration array (flags -> prefix), then,
 // in the CTA that finishes last, every item's base and count in that prefix
 // (its slots are the enumeration range [SLOT_BASE, SLOT_BASE + SLOT_N)).
+__device__ void copyout_plan_cta(const Ctx& c, int* s_warp);
+
 __global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, const int* flags, int* prefix, const int* tile_offs,
                                                      const long long* total, int base_field, int count_field,
-                                                     int stat_field, unsigned* done) {
+                                                     int stat_field, unsigned* done, int plan_copyout) {
   __shared__ int s_warp[32];
   const long long n = c.ctr->n_enum;
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
@@ -2141,22 +2143,36 @@ __global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, const int* flags, in
     if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
     if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
   }
+  if (plan_copyout) {
+    __syncthreads();
+    copyout_plan_cta(c, s_warp);
+  }
 }
 
 // publish write: one warp per enumerated slot (grid-strided), the block's 4 KiB
 // loaded by the warp at once; voxels in ascending local index
 // (getVoxelCoordinatesFromLocalVoxelIndex, tsdf_handler.cu:520-534)
-__global__ void __launch_bounds__(256) k_pub_write(Ctx c) {
+// part < 0: every item; part 0 / 1: the items before / from the split that
+// the copy-out plan chose (the first part's copy-out overlaps the second
+// part's writes).
+__global__ void __launch_bounds__(256) k_pub_write(Ctx c, int part) {
   __shared__ int s_sb[kMaxItems];
   __shared__ float s_pos[256 / 32][160];  // a warp's compacted output words of one round
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const long long n = c.ctr->n_enum;
+  const long long ne = c.ctr->n_enum;
+  long long e0 = 0, n = ne;
+  if (part >= 0) {
+    const long long sp = c.ctr->co_split_item;
+    const long long i0 = part == 0 ? 0 : sp, i1 = part == 0 ? sp : h.n_items;
+    e0 = i0 < h.n_items ? s_sb[i0] : ne;
+    n = i1 < h.n_items ? s_sb[i1] : ne;
+  }
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
-  for (long long e = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; e < n; e += nw) {
+  for (long long e = e0 + ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); e < n; e += nw) {
     if (c.enum_cnt[e] == 0) continue;
     const int item = find_item_i(s_sb, h.n_items, e);
     const ItemDev& it = c.items[item];
@@ -2250,9 +2266,11 @@ __device__ __forceinline__ CopyArray copy_array(const Ctx& c, int item, bool dat
   return a;
 }
 
-// Chunk bases of every item's two arrays (one CTA; items <= kMaxItems).
-__global__ void __launch_bounds__(1024) k_copyout_plan(Ctx c) {
-  __shared__ int s_warp[32];
+// Chunk bases of every item's two arrays, and the split of the items into
+// the publish kernel's two parts at about half the chunks (run by the last
+// CTA of the publish scan, right after it wrote the publish counts).
+__device__ void copyout_plan_cta(const Ctx& c, int* s_warp) {
+  __shared__ int s_split;
   const int ni = c.hdr->n_items;
   long long carry = 0;
   for (int b = 0; b < ni; b += blockDim.x) {
@@ -2272,17 +2290,30 @@ __global__ void __launch_bounds__(1024) k_copyout_plan(Ctx c) {
     carry += tot;
     __syncthreads();
   }
-  if (threadIdx.x == 0) c.ctr->n_co_chunks = carry;
+  if (threadIdx.x == 0) s_split = ni;
+  __syncthreads();
+  const long long half = carry / 2;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x)
+    if (c.item_i[i * II_COUNT + II_CO_BASE] >= half && (i == 0 || c.item_i[(i - 1) * II_COUNT + II_CO_BASE] < half))
+      atomicMin(&s_split, i);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c.ctr->n_co_chunks = carry;
+    c.ctr->co_split_item = s_split;
+    c.ctr->co_split_chunk = s_split < ni ? c.item_i[s_split * II_COUNT + II_CO_BASE] : carry;
+  }
 }
 
-__global__ void __launch_bounds__(256) k_pub_copyout(Ctx c) {
+// part 0 / 1: the chunks of the items before / from the split
+__global__ void __launch_bounds__(256) k_pub_copyout(Ctx c, int part) {
   __shared__ int s_cb[kMaxItems];
   const int ni = c.hdr->n_items;
   for (int i = threadIdx.x; i < ni; i += blockDim.x) s_cb[i] = c.item_i[i * II_COUNT + II_CO_BASE];
   __syncthreads();
-  const long long nch = c.ctr->n_co_chunks;
+  const long long ch0 = part == 0 ? 0 : c.ctr->co_split_chunk;
+  const long long nch = part == 0 ? c.ctr->co_split_chunk : c.ctr->n_co_chunks;
   const int t = threadIdx.x;
-  for (long long ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+  for (long long ch = ch0 + blockIdx.x; ch < nch; ch += gridDim.x) {
     int lo = 0, hi = ni - 1;  // the last item whose first chunk is <= ch
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -2552,26 +2583,34 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
   const int grid = lc.sm_count * 2;
   k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c);
   k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_cnt, c.pub_prefix, c.tile_sums2, &c.ctr->scan_total, II_PUB_BASE, -1,
-                                     ST_PUB, &c.ctr->done_pub);
-  k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c);
-  *launches += 3;
-  if (lc.copyout) {
-    // the copy to the host arrays runs on a side stream beside the gc stage
-    // (which touches neither the staging nor the publish counts); the gc
-    // stage joins it
-    cudaEventRecord(lc.ev_fork, s);
-    cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
-    k_copyout_plan<<<1, 1024, 0, lc.side>>>(c);
-    k_pub_copyout<<<lc.sm_count * 4, 256, 0, lc.side>>>(c);
-    cudaEventRecord(lc.ev_join, lc.side);
-    *launches += 2;
+                                     ST_PUB, &c.ctr->done_pub, lc.copyout);
+  *launches += 2;
+  if (!lc.copyout) {
+    k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c, -1);
+    *launches += 1;
+    return;
   }
+  // pinned host outputs: the items in two parts; each part's copy to the
+  // host arrays runs on a side stream as soon as its voxels are written (the
+  // first beside the second part's writes, the second beside the gc stage,
+  // which touches neither the staging nor the publish counts); the gc stage
+  // joins them
+  k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c, 0);
+  cudaEventRecord(lc.ev_fork, s);
+  cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
+  k_pub_copyout<<<lc.sm_count * 4, 256, 0, lc.side>>>(c, 0);
+  k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c, 1);
+  cudaEventRecord(lc.ev_join2, s);
+  cudaStreamWaitEvent(lc.side, lc.ev_join2, 0);
+  k_pub_copyout<<<lc.sm_count * 4, 256, 0, lc.side>>>(c, 1);
+  cudaEventRecord(lc.ev_join, lc.side);
+  *launches += 4;
 }
 
 void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
   k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_gc, c.gc_prefix, c.tile_sums3, &c.ctr->scan_total2, II_GC_BASE, II_GC_N,
-                                     -1, &c.ctr->done_gc);
+                                     -1, &c.ctr->done_gc, 0);
   k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
   *launches += 2;
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
