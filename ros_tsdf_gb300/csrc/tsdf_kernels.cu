@@ -3,6 +3,8 @@
 //
 // Stages (each a handful of grid-fixed kernels, so a step captures as one
 // CUDA graph and replays for any batch composition):
+//   init         pinned host scans copied into HBM by one kernel (when the
+//                caller passed pinned points); step counters zeroed
 //   ray_blocks   persistent work queue over (scan, point chunk): truncation
 //                segment + block DDA per point; lookup / lock-free CAS
 //                insertion of every block into the map's hash table
@@ -28,11 +30,19 @@
 //                masks give each update its place in point order).
 //                (tsdf_handler.cu:604-665)
 //   publish      in-radius blocks counted, prefix-summed, compacted to the
-//                output arrays or a serialized Tsdf message
+//                output arrays or a serialized Tsdf message; for pinned host
+//                arrays into device staging, then streamed to the host in
+//                whole 16-byte stores on a side stream
 //                (tsdf_handler.cu:767-825, publisher.cpp:9-31)
 //   gc           out-of-radius blocks compacted, pushed to the free list in
 //                ascending slot order, hash entries tombstoned
-//                (tsdf_handler.cu:836-952)
+//                (tsdf_handler.cu:836-952); the step's stats and counters
+//                written into the host's pinned mirrors
+//
+// Single-CTA follow-ups (a scan's top level, per-item bases, allocation and
+// gc bookkeeping, the heavy-segment plan, the copy-out plan) run in the last
+// CTA to finish the kernel before them (an atomic ticket after a fence), so
+// they need no launch of their own and no CTA waits on another.
 //
 // Float arithmetic uses explicit round-to-nearest intrinsics (no FMA
 // contraction) so every value matches the sequential CPU restatement bit for
