@@ -599,14 +599,16 @@ __device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total) {
 }
 
 // True in the CTA that finishes last.  Every thread fences its own writes
-// before its CTA takes a ticket, so the last CTA sees all of them through L2
-// (it reads them with __ldcg).  All threads of every CTA must call it.
+// before its CTA takes a ticket, and the last CTA fences again after taking
+// the last one, so it sees all of them through L2 (it reads them with
+// __ldcg).  All threads of every CTA must call it.
 __device__ __forceinline__ bool last_cta(unsigned* done) {
   __shared__ bool s_last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
   __syncthreads();
+  if (s_last) __threadfence();
   return s_last;
 }
 
