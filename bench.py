@@ -11,8 +11,9 @@ value   points integrated / s, inputs resident in HBM, device time from CUDA
         events recorded on the engine's stream around the step's kernels; L2
         is flushed (512 MiB write) between timed steps.
 e2e     same workload through tsdf_integrate_batch with pinned host input and
-        output buffers: host->device copy of the points and the publish
-        output landing in host memory are inside the (wall-clock) timed step.
+        output buffers: the points read into HBM over the host link and the
+        published voxels streamed back to host memory are inside the
+        (wall-clock) timed step.
 plain   the same scans integrated one scan per call (tsdf_integrate), the
         reference's calling pattern.
 

@@ -134,3 +134,25 @@ def test_pointcloud2_view_and_tsdf_message_layout():
     assert struct.unpack_from("<5f", m, 12) == (0.5, 3.0, 0.0, 1.0, 2.0)
     d = P.decode_tsdf_msg(m)
     assert np.array_equal(d["pos"], pos) and np.array_equal(d["data"], dat)
+
+
+def test_bench_profiles_cover_stage_kernels():
+    """Every kernel that bench.py's roofline line attributes to a stage has a
+    committed ncu summary for the headline workload with its per-unit DRAM
+    bytes (the `traffic` key), and every summary names the ncu command that
+    made it."""
+    import importlib.util
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    spec = importlib.util.spec_from_file_location("bench_mod", root / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    stats = {"blocks_touched": 25000, "published_blocks": 24000, "n_points": 180000}
+    for stage, (kernels, unit) in bench.STAGE_KERNELS.items():
+        for k in kernels:
+            v = bench.traffic_from_profiles(k, "multimap32")
+            assert v is not None and v > 0, f"{k}: no dram_bytes_per_unit in profiles/{k}_multimap32.md"
+        assert bench.stage_traffic(stage, "multimap32", stats) > 0
+    for p in (root / "profiles").glob("*.md"):
+        assert "ncu " in p.read_text() and "--clock-control none" in p.read_text(), p.name
