@@ -56,7 +56,8 @@ typedef enum tsdf_status {
   TSDF_ERR_HASH_FULL = 7,         /* a map's hash table has no free entry     */
   TSDF_ERR_BUSY = 8,              /* map already has a scan in flight         */
   TSDF_ERR_NOT_READY = 9,         /* tsdf_poll: request still running         */
-  TSDF_ERR_BAD_POINTS = 10        /* warning: some points were skipped        */
+  TSDF_ERR_BAD_POINTS = 10,       /* warning: some points were skipped        */
+  TSDF_ERR_NO_POSE = 11           /* pose buffer: stamp outside its samples    */
 } tsdf_status;
 
 typedef struct tsdf_engine tsdf_engine;
@@ -308,6 +309,26 @@ tsdf_status tsdf_device_alloc(tsdf_engine* eng, void** p, int64_t bytes);
 tsdf_status tsdf_device_free(tsdf_engine* eng, void* p);
 /* kind: 0 host->device, 1 device->host, 2 device->device; synchronous. */
 tsdf_status tsdf_copy(tsdf_engine* eng, void* dst, const void* src, int64_t bytes, int kind);
+
+/* ---- sensor origin from stamped poses (host only) -------------------------
+ * Replaces Transformer::getLidarPositionInPointCloudFrame
+ * (tsdf_package/src/transformer.cpp:21-56), which asks TF2 for the transform
+ * from the lidar frame to the cloud's frame at the cloud's stamp and maps the
+ * lidar frame's origin through it: the result is that transform's
+ * translation.  The caller adds the translations it receives (stamp in
+ * nanoseconds, > 0); a lookup returns the sample at that stamp, or the linear
+ * interpolation in double of the two samples around it (ratio = (stamp -
+ * t0) / (t1 - t0)), rounded to float like the reference's Vector3f; stamp 0
+ * returns the latest sample.  A stamp before the first or after the last
+ * sample is TSDF_ERR_NO_POSE (TF2 raises an extrapolation error there).  The
+ * buffer keeps the `capacity` newest samples; a sample at an existing stamp
+ * replaces it.  Thread-safe. */
+typedef struct tsdf_pose_buffer tsdf_pose_buffer;
+tsdf_status tsdf_pose_buffer_create(int64_t capacity, tsdf_pose_buffer** out);
+tsdf_status tsdf_pose_buffer_add(tsdf_pose_buffer* buf, int64_t stamp_ns, const double translation[3]);
+tsdf_status tsdf_pose_buffer_origin(tsdf_pose_buffer* buf, int64_t stamp_ns, float origin[3]);
+int64_t tsdf_pose_buffer_size(tsdf_pose_buffer* buf);
+void tsdf_pose_buffer_destroy(tsdf_pose_buffer* buf);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,7 @@ ERR_HASH_FULL = 7
 ERR_BUSY = 8
 ERR_NOT_READY = 9
 ERR_BAD_POINTS = 10
+ERR_NO_POSE = 11
 
 PUB_ARRAYS = 0
 PUB_TSDF_MSG = 1
@@ -29,7 +30,7 @@ def tsdf_msg_bytes(cap: int) -> int:
 
 STATUS_NAMES = {
     0: "OK", 1: "INVALID_ARG", 2: "HEAP_FULL", 3: "PUBLISH_OVERFLOW", 4: "CUDA", 5: "CAPACITY",
-    6: "SPIN_LIMIT", 7: "HASH_FULL", 8: "BUSY", 9: "NOT_READY", 10: "BAD_POINTS",
+    6: "SPIN_LIMIT", 7: "HASH_FULL", 8: "BUSY", 9: "NOT_READY", 10: "BAD_POINTS", 11: "NO_POSE",
 }
 
 STAT_FIELDS = [
@@ -121,6 +122,11 @@ SIGNATURES = [
     ("tsdf_device_alloc", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int64]),
     ("tsdf_device_free", C.c_int, [C.c_void_p, C.c_void_p]),
     ("tsdf_copy", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int]),
+    ("tsdf_pose_buffer_create", C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
+    ("tsdf_pose_buffer_add", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
+    ("tsdf_pose_buffer_origin", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
+    ("tsdf_pose_buffer_size", C.c_int64, [C.c_void_p]),
+    ("tsdf_pose_buffer_destroy", None, [C.c_void_p]),
 ]
 
 _lib = None

@@ -12,6 +12,7 @@
 #include <time.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <chrono>
@@ -1474,6 +1475,65 @@ tsdf_status tsdf_host_alloc(void** p, int64_t bytes) {
 }
 
 tsdf_status tsdf_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? TSDF_OK : TSDF_ERR_CUDA; }
+
+// Stamped sensor translations, kept sorted by stamp (see include/tsdf_c.h).
+struct tsdf_pose_buffer {
+  int64_t cap = 0;
+  std::deque<std::pair<int64_t, std::array<double, 3>>> s;
+  std::mutex mu;
+};
+
+tsdf_status tsdf_pose_buffer_create(int64_t capacity, tsdf_pose_buffer** out) {
+  if (!out || capacity < 1) return TSDF_ERR_INVALID_ARG;
+  *out = new tsdf_pose_buffer();
+  (*out)->cap = capacity;
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_pose_buffer_add(tsdf_pose_buffer* buf, int64_t stamp_ns, const double translation[3]) {
+  if (!buf || !translation || stamp_ns <= 0) return TSDF_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(buf->mu);
+  const std::array<double, 3> t = {translation[0], translation[1], translation[2]};
+  auto it = std::lower_bound(buf->s.begin(), buf->s.end(), stamp_ns,
+                             [](const std::pair<int64_t, std::array<double, 3>>& a, int64_t v) { return a.first < v; });
+  if (it != buf->s.end() && it->first == stamp_ns)
+    it->second = t;
+  else
+    buf->s.insert(it, {stamp_ns, t});
+  while ((int64_t)buf->s.size() > buf->cap) buf->s.pop_front();
+  return TSDF_OK;
+}
+
+tsdf_status tsdf_pose_buffer_origin(tsdf_pose_buffer* buf, int64_t stamp_ns, float origin[3]) {
+  if (!buf || !origin || stamp_ns < 0) return TSDF_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(buf->mu);
+  if (buf->s.empty()) return TSDF_ERR_NO_POSE;
+  std::array<double, 3> r;
+  if (stamp_ns == 0) {
+    r = buf->s.back().second;
+  } else {
+    if (stamp_ns < buf->s.front().first || stamp_ns > buf->s.back().first) return TSDF_ERR_NO_POSE;
+    auto hi = std::lower_bound(buf->s.begin(), buf->s.end(), stamp_ns,
+                               [](const std::pair<int64_t, std::array<double, 3>>& a, int64_t v) { return a.first < v; });
+    if (hi->first == stamp_ns) {
+      r = hi->second;
+    } else {
+      const auto lo = hi - 1;
+      const double ratio = (double)(stamp_ns - lo->first) / (double)(hi->first - lo->first);
+      for (int k = 0; k < 3; ++k) r[k] = lo->second[k] + (hi->second[k] - lo->second[k]) * ratio;
+    }
+  }
+  for (int k = 0; k < 3; ++k) origin[k] = (float)r[k];
+  return TSDF_OK;
+}
+
+int64_t tsdf_pose_buffer_size(tsdf_pose_buffer* buf) {
+  if (!buf) return 0;
+  std::lock_guard<std::mutex> lk(buf->mu);
+  return (int64_t)buf->s.size();
+}
+
+void tsdf_pose_buffer_destroy(tsdf_pose_buffer* buf) { delete buf; }
 
 tsdf_status tsdf_device_alloc(tsdf_engine* eng, void** p, int64_t bytes) {
   if (!eng || !p || bytes < 0) return TSDF_ERR_INVALID_ARG;

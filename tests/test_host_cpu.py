@@ -156,3 +156,33 @@ def test_bench_profiles_cover_stage_kernels():
         assert bench.stage_traffic(stage, "multimap32", stats) > 0
     for p in (root / "profiles").glob("*.md"):
         assert "ncu " in p.read_text() and "--clock-control none" in p.read_text(), p.name
+
+
+def test_pose_buffer_origin_lookup(built):
+    """The sensor origin from stamped translations: exact samples, linear
+    interpolation in double rounded to float32, the latest sample for stamp
+    0, errors outside the samples, replacement at an equal stamp, and the
+    capacity keeping the newest samples."""
+    from ros_tsdf_gb300.poses import NoPoseError, PoseBuffer
+
+    with PoseBuffer(capacity=3) as b:
+        with pytest.raises(NoPoseError):
+            b.origin(0)
+        b.add(2_000_000_000, (10.0, 20.0, -30.0))
+        b.add(1_000_000_000, (0.0, 0.0, 0.0))
+        assert np.array_equal(b.origin(1_000_000_000), np.float32([0, 0, 0]))
+        assert np.array_equal(b.origin(1_250_000_000), np.float32([2.5, 5.0, -7.5]))
+        r = (1_100_000_000 - 1_000_000_000) / (2_000_000_000 - 1_000_000_000)
+        assert np.array_equal(b.origin(1_100_000_000), np.float32([10.0 * r, 20.0 * r, -30.0 * r]))
+        assert np.array_equal(b.origin(0), np.float32([10, 20, -30]))
+        for bad in (999_999_999, 2_000_000_001):
+            with pytest.raises(NoPoseError):
+                b.origin(bad)
+        b.add(2_000_000_000, (1.0, 1.0, 1.0))   # same stamp: replaced
+        assert np.array_equal(b.origin(2_000_000_000), np.float32([1, 1, 1]))
+        b.add(3_000_000_000, (3.0, 3.0, 3.0))
+        b.add(4_000_000_000, (4.0, 4.0, 4.0))   # capacity 3: the oldest sample goes
+        assert len(b) == 3
+        with pytest.raises(NoPoseError):
+            b.origin(1_500_000_000)
+        assert np.array_equal(b.origin(3_500_000_000), np.float32([3.5, 3.5, 3.5]))
