@@ -357,7 +357,14 @@ def run_ours(args, rank, world, local, pg):
 
 
 def algorithmic_bytes(s: dict) -> dict:
-    """Per-step algorithmic bytes ('Roofline')."""
+    """Per-step algorithmic bytes.  Whole step: 12 B per point read, 16 B per
+    distinct voxel updated (8-B read + 8-B write), 16 B per block touched (its
+    hash entry), 20 B per new block (entry write + free-list pop), 16 B per
+    allocated block at step start twice (its key read by publish and by gc),
+    4096 B per publishing block, 20 B per published voxel, 20 B per collected
+    block.  Update stage: every touched block read and written back (8192 B).
+    Publish stage: the publishing blocks, the published voxels and the slot
+    scan."""
     whole = (12 * s["n_points"] + 16 * s["distinct_voxels"] + 16 * s["blocks_touched"] + 20 * s["new_blocks"]
              + 16 * s["alloc_blocks_before"] + 4096 * s["published_blocks"] + 20 * s["published"]
              + 16 * s["alloc_blocks_before"] + 20 * s["gc_blocks"])
@@ -430,7 +437,7 @@ def stage_traffic(stage: str, workload: str, stats: dict):
 
 
 def run_serving(args, local: int) -> dict:
-    """configs[3]-shaped serving loop: 64 clients with device-resident maps,
+    """The serving loop: 64 clients with device-resident maps,
     Poisson arrivals at 10 Hz each, lidar and voxel size drawn per client.
     The same trace is replayed through the served engine (scheduler thread,
     continuous batching, two lanes) and through the plain path (one

@@ -39,15 +39,15 @@ def main():
 
     oracle.build()
     rows = []
-    rows.append(("configs[0] plain_small (16x64, vs 0.5, T 4)", W.plain_small(seed=0, heap_blocks=1 << 16), 20))
+    rows.append(("plain_small (16x64, vs 0.5, T 4)", W.plain_small(seed=0, heap_blocks=1 << 16), 20))
     mm = W.multimap32(32, base_seed=1000, heap_blocks=1 << 16)
-    rows.append(("configs[1] multimap32 map 10 (64x1024)", mm[10], 5))
-    rows.append(("configs[1] multimap32 map 14 (sensor inside a box)", mm[14], 5))
-    rows.append(("configs[2] large_stream (64x1024, vs 0.1, T 0.4)", W.large_stream(seed=2000), 5))
+    rows.append(("multimap32 map 10 (64x1024)", mm[10], 5))
+    rows.append(("multimap32 map 14 (sensor inside a box)", mm[14], 5))
+    rows.append(("large_stream (64x1024, vs 0.1, T 0.4)", W.large_stream(seed=2000), 5))
     for vs in (0.05, 0.2):
         sv = [s for s in W.serving64() if abs(s.params.voxel_size - vs) < 1e-9][0]
-        rows.append((f"configs[3] serving64 client, vs {vs}, T {4 * vs:g}", replace(sv, heap_blocks=1 << 20), 3))
-    rows.append(("configs[4] stress8 map 0 (128x2048, vs 0.05, T 0.2)", replace(W.stress8(1)[0], heap_blocks=1 << 21), 2))
+        rows.append((f"serving64 client, vs {vs}, T {4 * vs:g}", replace(sv, heap_blocks=1 << 20), 3))
+    rows.append(("stress8 map 0 (128x2048, vs 0.05, T 0.2)", replace(W.stress8(1)[0], heap_blocks=1 << 21), 2))
     print("| config | scans | voxels compared | max abs sdf err | mean abs sdf err | max abs weight err "
           "| max sdf err / T | float-only voxels | fp64-only voxels |")
     print("|---|---|---|---|---|---|---|---|---|")

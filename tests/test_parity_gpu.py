@@ -1,6 +1,6 @@
 """GPU parity of the engine against the CPU oracle, through the C-ABI.
 
-Bar (from the benchmark spec): block set, hash contents (key -> slot), heap
+Bar: block set, hash contents (key -> slot), heap
 occupancy / free list and published voxel set bit-exact; weights exact; sdf
 within 1e-5 * truncation_distance.  The engine applies every voxel's updates
 in the oracle's order, so sdf is asserted bit-exact too (a stronger check).
@@ -396,7 +396,7 @@ def test_update_division_matches_cuda_fdiv(built):
 
 def test_autotune_choice_keeps_parity(built, tmp_path):
     """The autotuner times candidates, caches its choice, and the chosen
-    launch parameters reproduce the oracle on configs[0] run map by map."""
+    launch parameters reproduce the oracle on the plain_small workload."""
     from ros_tsdf_gb300 import Engine, autotune, workloads as W
 
     specs = [W.plain_small(seed=s, heap_blocks=1 << 14) for s in (0, 1)]
