@@ -6,7 +6,7 @@ same trace can be replayed through the plain path (one synchronous
 
 Scan-to-publish latency of a request = the time its published voxels are in
 the caller's buffers minus its arrival time.  Served: arrival is the moment
-the driver submits it (the driver submits at the scheduled arrival time and
+the replay loop submits it (it submits at the scheduled arrival time and
 reports how late it ever was); completion is the engine's own CLOCK_MONOTONIC
 stamp.  Plain: arrival is the scheduled time (a request waits while the
 single server is busy), completion is when `tsdf_integrate` returns.
@@ -158,7 +158,7 @@ class ServingRig:
         return {"requests": len(pending), "points": pts, "points_per_s": pts / span if span > 0 else 0.0,
                 "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99), "max_ms": max(lat) if lat else 0.0,
                 "p99_ms_by_rays": {str(k): percentile(v, 99) for k, v in sorted(lat_by_rays.items())},
-                "driver_max_late_ms": late, "statuses": statuses, "span_s": span}
+                "submit_max_late_ms": late, "statuses": statuses, "span_s": span}
 
     def run_plain(self, trace: list[Request], at_once: bool = False) -> dict:
         """One synchronous tsdf_integrate per request, in arrival order, on
