@@ -107,7 +107,9 @@ def sum_over_ranks(pg, v: float) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms; entering
+    waits (up to 2 s) for the first sample, so the sampler is running before
+    the timed region starts."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -125,6 +127,9 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t_end = time.time() + 2.0
+            while not self.rows and self.proc.poll() is None and time.time() < t_end:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
@@ -135,7 +140,7 @@ class ClockSampler:
 
     def __exit__(self, *a):
         if self.proc:
-            time.sleep(0.25)
+            time.sleep(0.1)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=2)
@@ -329,7 +334,8 @@ def run_ours(args, rank, world, local, pg):
     e2e_t = max_over_ranks(pg, e2e_t)
     e2e = {"value": total_pts / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
            "d2h_bytes_per_step": int(d2h / args.steps), "ms_per_step": e2e_t * 1000.0 / args.steps,
-           "path": "tsdf_integrate_batch, pinned host in/out (publish kernel writes host memory over C2C)"}
+           "path": ("tsdf_integrate_batch, pinned host in/out (points read over NVLink-C2C by the staging kernel, "
+                    "published voxels streamed back by the copy-out kernel)")}
 
     # ---- plain: one scan per call, host pageable arrays (reference calling pattern)
     plain = None
