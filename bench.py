@@ -483,45 +483,11 @@ def run_serving(args, local: int) -> dict:
     return out
 
 
-def main():
-    args = parse()
-    rank, world, local, pg = dist_init(args.gpus)
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        specs = make_workload(args.workload, 0, args.heap_blocks)
-        n_steps = args.warmup + args.steps
-        scans = gen_scans(specs, n_steps)
-        threads = os.cpu_count() or 1
-        v, t = cpu_baseline_run(specs, scans, n_steps, args.warmup, threads)
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000.0 / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
-                "config": {"workload": args.workload, "maps": len(specs), "per_step": "one scan per map"},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": min(threads, len(specs)), "kind": "port",
-                                 "sample": f"all {args.steps} timed steps of the workload ({args.warmup} warm-up), "
-                                           "one host thread per map"},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "note": "reference CUDA path unbuildable here (CDP1 device-side cudaDeviceSynchronize is "
-                        "rejected by CUDA 13; Eigen/PCL/ROS2 absent); timed its algorithm as host code"}
-        print(json.dumps(line))
-        return
-    if args.serving_only:
-        if rank == 0:
-            print(json.dumps({"serving": run_serving(args, local)}))
-        return
-    tuned = None
-    if not args.no_autotune:
-        from ros_tsdf_gb300 import autotune
-
-        specs0 = make_workload(args.workload, rank, args.heap_blocks)
-        sample = gen_scans(specs0, 4)
-        best = autotune.tune(specs0, sample, steps=3, device=local)
-        args.bucket_size, args.ray_chunk, args.ray_threads = best["bucket_size"], best["ray_chunk"], best["ray_threads"]
-        tuned = dict(best, source="ros_tsdf_gb300.autotune on the first 4 scans of every map")
-    r = run_ours(args, rank, world, local, pg)
-    peak, peak_kind = load_peaks()
+def result_line(args, r: dict, world: int, tuned, peak: float, peak_kind: str) -> dict:
+    """The JSON line of our arm from run_ours's result: metric and value, the
+    workload config, e2e, the roofline of the dominant stage (algorithmic
+    bytes over its CUDA-event time, traffic from the ncu summaries), the stage
+    times, per-step counters, clocks and the engine's launch count."""
     ab = algorithmic_bytes(r["stats"])
     stages = r["stages"]
     n = args.steps
@@ -562,6 +528,49 @@ def main():
         "call_ms_per_step": (sum(r["wall_ms"]) / max(len(r["wall_ms"]), 1)) if r.get("wall_ms") else None,
         "clocks": r["clocks"], "gpu_launches": r["gpu_launches"],
     }
+    return line
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_init(args.gpus)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        specs = make_workload(args.workload, 0, args.heap_blocks)
+        n_steps = args.warmup + args.steps
+        scans = gen_scans(specs, n_steps)
+        threads = os.cpu_count() or 1
+        v, t = cpu_baseline_run(specs, scans, n_steps, args.warmup, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000.0 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
+                "config": {"workload": args.workload, "maps": len(specs), "per_step": "one scan per map"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": min(threads, len(specs)), "kind": "port",
+                                 "sample": f"all {args.steps} timed steps of the workload ({args.warmup} warm-up), "
+                                           "one host thread per map"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference CUDA path unbuildable here (CDP1 device-side cudaDeviceSynchronize is "
+                        "rejected by CUDA 13; Eigen/PCL/ROS2 absent); timed its algorithm as host code"}
+        print(json.dumps(line))
+        return
+    if args.serving_only:
+        if rank == 0:
+            print(json.dumps({"serving": run_serving(args, local)}))
+        return
+    tuned = None
+    if not args.no_autotune:
+        from ros_tsdf_gb300 import autotune
+
+        specs0 = make_workload(args.workload, rank, args.heap_blocks)
+        sample = gen_scans(specs0, 4)
+        best = autotune.tune(specs0, sample, steps=3, device=local)
+        args.bucket_size, args.ray_chunk, args.ray_threads = best["bucket_size"], best["ray_chunk"], best["ray_threads"]
+        tuned = dict(best, source="ros_tsdf_gb300.autotune on the first 4 scans of every map")
+    r = run_ours(args, rank, world, local, pg)
+    peak, peak_kind = load_peaks()
+    line = result_line(args, r, world, tuned, peak, peak_kind)
     if rank == 0 and not args.no_cpu_baseline:
         threads = min(os.cpu_count() or 1, len(r["specs"]))
         v, t = cpu_baseline_run(r["specs"], r["scans"], min(args.warmup + 3, args.warmup + args.steps),

@@ -186,3 +186,60 @@ def test_pose_buffer_origin_lookup(built):
         with pytest.raises(NoPoseError):
             b.origin(1_500_000_000)
         assert np.array_equal(b.origin(3_500_000_000), np.float32([3.5, 3.5, 3.5]))
+
+
+def test_bench_result_line_contract():
+    """bench.py's JSON line carries every key of the benchmark contract, with
+    the roofline of the dominant stage and the e2e record, from a synthetic
+    run result (no GPU)."""
+    import importlib.util
+    import json
+    from pathlib import Path
+    from types import SimpleNamespace
+
+    from ros_tsdf_gb300 import workloads as W
+
+    root = Path(__file__).resolve().parent.parent
+    spec = importlib.util.spec_from_file_location("bench_mod2", root / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    stats = {k: 1000.0 for k in ("n_points", "distinct_voxels", "blocks_touched", "new_blocks", "alloc_blocks_before",
+                                 "published_blocks", "published", "gc_blocks", "voxel_updates")}
+    stages = {"init": (0.01, 1), "update": (0.18, 1), "publish": (0.06, 1), "ray_voxels": (0.09, 1)}
+    r = {"value": 3.0e8, "ms_per_step": 0.58, "stats": stats, "stages": stages, "specs": W.multimap32(4),
+         "timed_pts": 1.8e6, "wall_ms": [0.7, 0.7], "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []},
+         "gpu_launches": 390, "plain": None,
+         "e2e": {"value": 2.1e8, "unit": bench.UNIT, "h2d_bytes_per_step": 2, "d2h_bytes_per_step": 3}}
+    args = SimpleNamespace(steps=10, warmup=3, workload="multimap32", bucket_size=1, ray_chunk=32, ray_threads=256)
+    line = bench.result_line(args, r, 1, None, 6692.8, "measured")
+    json.dumps(line)
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "e2e", "roofline", "clocks", "gpu_launches"):
+        assert k in line, k
+    assert line["config"]["workload"] == "multimap32" and line["scaling"] == "weak"
+    rf = line["roofline"]
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
+        assert k in rf, k
+    assert rf["stage"] == "update" and rf["kernel"] == "k_hot_chains+k_heavy_update+k_update"
+    assert abs(rf["achieved"] - 8192 * 1000 / 0.18e-3 / 1e9) < 1e-9 and abs(rf["frac"] - rf["achieved"] / 6692.8) < 1e-12
+    assert rf["traffic"] > 0
+    for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"):
+        assert k in line["e2e"], k
+
+    # main() end to end around a stubbed run: prints exactly one JSON line
+    import contextlib
+    import io
+    import sys as _sys
+
+    bench.run_ours = lambda *a: r
+    bench.dist_init = lambda n: (0, 1, 0, None)
+    argv = _sys.argv
+    _sys.argv = ["bench.py", "--steps", "10", "--warmup", "3", "--serving-s", "0", "--no-cpu-baseline", "--no-autotune"]
+    out = io.StringIO()
+    try:
+        with contextlib.redirect_stdout(out):
+            bench.main()
+    finally:
+        _sys.argv = argv
+    lines = [x for x in out.getvalue().splitlines() if x.strip()]
+    assert len(lines) == 1 and json.loads(lines[0])["value"] == 3.0e8
