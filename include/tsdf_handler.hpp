@@ -149,6 +149,37 @@ class TSDFHandler {
   tsdf_scan_stats last_stats_{};
 };
 
+// Transformer::getLidarPositionInPointCloudFrame (transformer.cpp:21-56)
+// without a TF2 lookup per scan: the lidar-to-cloud translations are added as
+// they arrive; origin(stamp) is the sample at that stamp or the linear
+// interpolation of the two around it (std::out_of_range outside them, where
+// TF2 throws its extrapolation error).
+class PoseBuffer {
+ public:
+  explicit PoseBuffer(int64_t capacity = 1024) {
+    if (tsdf_pose_buffer_create(capacity, &buf_) != TSDF_OK) throw std::runtime_error("tsdf_pose_buffer_create");
+  }
+  ~PoseBuffer() { tsdf_pose_buffer_destroy(buf_); }
+  PoseBuffer(const PoseBuffer&) = delete;
+  PoseBuffer& operator=(const PoseBuffer&) = delete;
+
+  void add(int64_t stamp_ns, double x, double y, double z) {
+    const double t[3] = {x, y, z};
+    if (tsdf_pose_buffer_add(buf_, stamp_ns, t) != TSDF_OK) throw std::runtime_error("tsdf_pose_buffer_add");
+  }
+  Vector3f origin(int64_t stamp_ns = 0) const {
+    Vector3f v{};
+    const tsdf_status st = tsdf_pose_buffer_origin(buf_, stamp_ns, v.data);
+    if (st == TSDF_ERR_NO_POSE) throw std::out_of_range("no pose around the requested stamp");
+    if (st != TSDF_OK) throw std::runtime_error("tsdf_pose_buffer_origin");
+    return v;
+  }
+  int64_t size() const { return tsdf_pose_buffer_size(buf_); }
+
+ private:
+  tsdf_pose_buffer* buf_ = nullptr;
+};
+
 }  // namespace tsdf
 
 #endif  // TSDF_HANDLER_HPP

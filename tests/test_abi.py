@@ -83,3 +83,36 @@ def test_cpp_dropin_header_compiles(tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'include'}", str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_cpp_pose_buffer_runs(built, tmp_path):
+    """The C++ drop-in's PoseBuffer, linked against the engine library, looks up
+    origins on the host (no GPU call): interpolation, latest sample, and
+    std::out_of_range outside the samples."""
+    import subprocess
+
+    from ros_tsdf_gb300 import _lib
+
+    lib = _lib.lib_path()
+    src = tmp_path / "pose.cpp"
+    src.write_text(r'''
+#include "tsdf_handler.hpp"
+#include <cstdio>
+int main() {
+  tsdf::PoseBuffer b(8);
+  b.add(1000000000, 0.0, 0.0, 0.0);
+  b.add(2000000000, 10.0, -20.0, 30.0);
+  tsdf::Vector3f o = b.origin(1500000000);
+  if (o(0) != 5.0f || o(1) != -10.0f || o(2) != 15.0f) return 1;
+  if (b.origin(0)(2) != 30.0f || b.size() != 2) return 2;
+  try { b.origin(2500000000); return 3; } catch (const std::out_of_range&) {}
+  std::puts("ok");
+  return 0;
+}
+''')
+    exe = tmp_path / "pose"
+    r = subprocess.run(["g++", "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{lib.parent}",
+                        f"-l:{lib.name}", f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0 and run.stdout.strip() == "ok", (run.returncode, run.stderr)
