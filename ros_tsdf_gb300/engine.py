@@ -211,7 +211,10 @@ class Engine:
     def submit(self, map_id: int, xyz, origin, pub_cap: int = 400000, pinned: bool = False):
         """Queue a scan; returns a handle for wait().  Buffers are kept alive by the handle.
         pinned: copy the points into page-locked memory and receive the voxels
-        in page-locked arrays (the engine's fast host path)."""
+        in page-locked arrays (the engine's fast host path).  The page-locked
+        buffers are allocated per call, which costs milliseconds: a sustained
+        loop should keep its own (`pinned_empty`) and pass them to the C-ABI
+        as ros_tsdf_gb300.serving.ServingRig does."""
         a, stride = _as_points(xyz)
         if pinned and a.shape[0]:
             p = self.pinned_empty(a.shape, np.float32)
