@@ -4,9 +4,13 @@ A sequential restatement of ros_tsdf's algorithm in C++ (tsdf_oracle.cpp),
 used by tests/, __graft_entry__.smoke() and the CPU-baseline legs of
 bench.py as the checker.  The engine never imports it.
 
-Parity status: unpinned by the reference (ros_tsdf has no tests or golden
-vectors and cannot be built here); pinned by hand-derived known-answer tests in
-tests/test_oracle_kat.py.
+Parity status: pinned to the reference's own code.  ros_tsdf ships no tests
+or golden vectors, so oracle/ref.py compiles its tsdf_handler.cu and
+tsdf_container.cu as sequential host code (oracle/ref_harness.cpp) and
+tests/test_reference_pin.py checks the oracle against that program point by
+point (segments, DDA cells, local indices, distance and weight updates) and
+scan by scan (published voxels, hash contents, heap, every voxel).  The
+hand-derived known-answer tests (tests/test_oracle_kat.py) remain.
 """
 from __future__ import annotations
 
@@ -98,6 +102,10 @@ def lib() -> C.CDLL:
         L.oracle_apply_update.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.c_float,
                                           C.c_float]
         L.oracle_derived.argtypes = [C.POINTER(_Params), C.POINTER(C.c_int32)]
+        L.oracle_stages.restype = C.c_int64
+        L.oracle_stages.argtypes = [C.POINTER(_Params), C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
         _lib = L
     return _lib
 
@@ -161,6 +169,36 @@ class OracleMap:
             self.L.oracle_map_destroy(self.h)
         except Exception:
             pass
+
+
+def point_stages(params, xyz, origin) -> dict:
+    """Per-point stages of a scan (oracle_stages): segments, block and voxel
+    DDA cells, and per voxel cell the local index, distance and weight
+    updates, as flat arrays with per-point counts."""
+    L = lib()
+    a = np.ascontiguousarray(np.asarray(xyz, np.float32)[:, :3])
+    n = a.shape[0]
+    dv = (C.c_int32 * 4)()
+    L.oracle_derived(C.byref(params_c(params)), dv)
+    vmax, amax = int(dv[0]), int(dv[1])
+    cap_b, cap_v = max(n * amax, 1), max(n * vmax, 1)
+    seg = np.zeros((max(n, 1), 6), np.float32)
+    nb = np.zeros(max(n, 1), np.int32)
+    nv = np.zeros(max(n, 1), np.int32)
+    valid = np.zeros(max(n, 1), np.int32)
+    bcells = np.empty((cap_b, 3), np.float32)
+    vcells = np.empty((cap_v, 3), np.float32)
+    local = np.empty(cap_v, np.int32)
+    dist = np.empty(cap_v, np.float32)
+    wt = np.empty(cap_v, np.float32)
+    capped = L.oracle_stages(C.byref(params_c(params)), a.ctypes.data if n else None, n, _f3(origin),
+                             seg.ctypes.data, nb.ctypes.data, bcells.ctypes.data, cap_b, nv.ctypes.data,
+                             vcells.ctypes.data, local.ctypes.data, dist.ctypes.data, wt.ctypes.data, cap_v,
+                             valid.ctypes.data)
+    tb, tv = int(nb[:n].sum()), int(nv[:n].sum())
+    return {"segment": seg[:n], "nb": nb[:n], "block_cells": bcells[:tb], "nv": nv[:n], "voxel_cells": vcells[:tv],
+            "local": local[:tv], "dist": dist[:tv], "weight": wt[:tv], "valid": valid[:n].astype(bool),
+            "capped": int(capped)}
 
 
 def integrate_many(maps: list, scans: list, origins, pub_cap: int = 0, threads: int | None = None):

@@ -4,12 +4,15 @@
 // engine in ros_tsdf_gb300/: only tests/, __graft_entry__.smoke() and the
 // CPU-baseline legs of bench.py may load it.  The product never links it.
 //
-// Parity status: UNPINNED by the reference.  ros_tsdf ships no tests, golden
-// vectors or fixtures, and its code cannot be built here (it needs Eigen, PCL
-// and ROS2, and its kernels use CUDA dynamic-parallelism device-side
-// cudaDeviceSynchronize, which CUDA 13 rejects).  The oracle is pinned instead
-// by known-answer tests derived by hand from the reference's formulas
-// (tests/test_oracle_kat.py).
+// Parity status: PINNED to the reference's own code.  ros_tsdf ships no tests,
+// golden vectors or fixtures, and its GPU path cannot be built here (its
+// kernels use CUDA dynamic-parallelism device-side cudaDeviceSynchronize,
+// which CUDA 13 rejects).  oracle/ref.py therefore compiles its
+// tsdf_handler.cu and tsdf_container.cu unchanged as sequential host code
+// (kernel launches rewritten into loops; CUDA, Eigen and PCL replaced by host
+// stand-ins, oracle/ref_shim/), and tests/test_reference_pin.py checks this
+// oracle against that program stage by stage and scan by scan.  Known-answer
+// tests derived by hand from the formulas remain (tests/test_oracle_kat.py).
 //
 // What it restates (all paths relative to the ros_tsdf project):
 //   tsdf_package/src/cuda/tsdf_handler.cu
@@ -702,6 +705,65 @@ float oracle_weight_update(float d) { return weight_update(d); }
 
 void oracle_apply_update(float* sdf, float* w, float dist, float wt, float maxw) {
   apply_update(sdf, w, dist, wt, maxw);
+}
+
+// Per-point stages of n points (the order integrate() computes them in), for
+// the point-by-point comparison with the reference's own device functions:
+//   seg[6i..6i+5]     truncation segment start, end    (tsdf_handler.cu:112-133)
+//   nb[i] block cells, centres appended to bcells      (:146-245 at block size)
+//   nv[i] voxel cells, centres appended to vcells      (:146-245 at voxel size)
+//   per voxel cell: local index (-1 when outside 0..7 on an axis), distance
+//   and weight update                                  (:507-512, :562-593)
+//   valid[i] = 0 for a point integrate() skips (then nb = nv = 0)
+// Cells beyond cap_b / cap_v are not written.  Returns the number of points
+// whose block or voxel DDA hit its cap.
+int64_t oracle_stages(const or_params* p, const float* xyz, int64_t n, const float origin[3], float* seg, int32_t* nb,
+                      float* bcells, int64_t cap_b, int32_t* nv, float* vcells, int32_t* local, float* dist, float* wt,
+                      int64_t cap_v, int32_t* valid) {
+  Derived<float> d = derive<float>(p->voxel_size, p->truncation_distance, p->max_weight, p->publish_distance_squared,
+                                   p->garbage_collect_distance_squared);
+  V3<float> org{origin[0], origin[1], origin[2]};
+  std::vector<Cell<float>> cells(std::max(d.vmax, d.amax) + 1);
+  int64_t ob = 0, ov = 0, capped = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    V3<float> pt{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]}, a, b;
+    nb[i] = nv[i] = 0;
+    valid[i] = segment(pt, org, d.T, &a, &b) && key_in_range(a, d) && key_in_range(b, d);
+    if (!valid[i]) continue;
+    const float s6[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+    std::memcpy(seg + 6 * i, s6, sizeof(s6));
+    for (int pass = 0; pass < 2; ++pass) {
+      int ovf;
+      int nc = traverse(a, b, pass == 0 ? d.bs : d.vs, pass == 0 ? d.amax : d.vmax, cells.data(), &ovf);
+      capped += ovf;
+      for (int j = 0; j < nc; ++j) {
+        const V3<float>& x = cells[j].c;
+        if (pass == 0) {
+          if (ob < cap_b) {
+            bcells[3 * ob] = x.x, bcells[3 * ob + 1] = x.y, bcells[3 * ob + 2] = x.z;
+          }
+          ob++;
+          nb[i]++;
+          continue;
+        }
+        if (ov < cap_v) {
+          vcells[3 * ov] = x.x, vcells[3 * ov + 1] = x.y, vcells[3 * ov + 2] = x.z;
+          float fx, fy, fz;
+          V3<float> c{center(x.x, d.bs, &fx), center(x.y, d.bs, &fy), center(x.z, d.bs, &fz)};
+          V3<float> bl{c.x - d.half_bs, c.y - d.half_bs, c.z - d.half_bs};
+          V3<float> df{(x.x - bl.x) / d.vs, (x.y - bl.y) / d.vs, (x.z - bl.z) / d.vs};
+          float ix = std::floor(df.x), iy = std::floor(df.y), iz = std::floor(df.z);
+          bool in = ix >= 0.0f && ix < 8.0f && iy >= 0.0f && iy < 8.0f && iz >= 0.0f && iz < 8.0f;
+          local[ov] = in ? (int32_t)(ix + iy * float(kVoxelsPerSide) + iz * float(kVoxelsPerSide * kVoxelsPerSide)) : -1;
+          dist[ov] = distance_update(x, pt, org);
+          wt[ov] = weight_update(dist[ov]);
+        }
+        ov++;
+        nv[i]++;
+      }
+    }
+  }
+  return capped;
 }
 
 // Derived constants of initGlobalVars: {vmax, amax, rmax, margin}.
