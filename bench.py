@@ -17,10 +17,16 @@ e2e     same workload through tsdf_integrate_batch with pinned host input and
 plain   the same scans integrated one scan per call (tsdf_integrate), the
         reference's calling pattern.
 
---impl reference times the reference's algorithm on the host cores (the CPU
-oracle, a restatement of ros_tsdf's integration call; the CUDA original
-cannot be built: it needs CUDA dynamic parallelism with device-side
-cudaDeviceSynchronize, removed in CUDA 12+, plus Eigen/PCL/ROS2).
+--impl reference times ros_tsdf's own integration code on the host cores:
+its tsdf_handler.cu / tsdf_container.cu compiled as sequential host programs
+(oracle/ref.py, one process per map, as many at once as cores and host memory
+allow).  Its CUDA build cannot run here: it needs CUDA dynamic parallelism
+with device-side cudaDeviceSynchronize, which CUDA 12+ removed.  Where the
+reference programs are not built, the CPU oracle (a restatement of the same
+code) is timed instead and the line says so.
+
+parity  the engine's 18 per-scan counters of every step, for every map,
+        compared with the CPU oracle integrating the same scans.
 """
 from __future__ import annotations
 
@@ -162,6 +168,64 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML every millisecond
+    (read-only queries), so that even a timed region of a few milliseconds is
+    sampled.  Same summary() as ClockSampler."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device: int):
+        import ctypes as C
+
+        self.C = C
+        self.nv = C.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.nv.nvmlDeviceGetHandleByIndex_v2(C.c_uint(device), C.byref(self.h)) != 0:
+            raise RuntimeError("nvmlDeviceGetHandleByIndex failed")
+        self.reasons_fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = C.c_uint()
+        self.max_mhz = float(mx.value) if self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx)) == 0 else None
+        self.rows = []
+        self.stop = False
+
+    def _loop(self):
+        C = self.C
+        mhz, rs = C.c_uint(), C.c_ulonglong()
+        while not self.stop:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, C.byref(rs)) == 0:
+                self.rows.append((float(mhz.value), int(rs.value)))
+            time.sleep(0.001)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop = True
+        self.t.join(timeout=1.0)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "samples": 0}
+        reasons = sorted({n for _, r in self.rows for b, n in self.REASONS.items() if r & b})
+        return {"sm_mhz": statistics.median(m for m, _ in self.rows), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.rows), "source": "NVML, 1 ms"}
+
+
+def clock_sampler(device: int):
+    try:
+        return NvmlClocks(device)
+    except Exception:
+        return ClockSampler(device)
+
+
 # ---------------------------------------------------------------------------
 def make_workload(name: str, rank: int, heap_blocks: int = 1 << 16):
     from ros_tsdf_gb300 import workloads as W
@@ -249,13 +313,14 @@ def run_ours(args, rank, world, local, pg):
 
     mids_of = {eng: mids}
     stats_steps = []
+    stats_all = []
     dev_ms = []
     wall_ms = []
     eng.set_stage_timing(2)
     stage_acc = {}
     launches0 = 0
     barrier(pg)
-    with ClockSampler(local) as clk:
+    with clock_sampler(local) as clk:
         for k in range(n_steps):
             if k == args.warmup:
                 eng.reset_stage_times()
@@ -268,6 +333,7 @@ def run_ours(args, rank, world, local, pg):
             st, stat = batch_run(eng, a3)
             wall = time.perf_counter() - t0
             step_ms = eng.step_times()[0] - before
+            stats_all.append(st)
             if k >= args.warmup:
                 dev_ms.append(step_ms)
                 wall_ms.append(wall * 1000.0)
@@ -298,7 +364,7 @@ def run_ours(args, rank, world, local, pg):
     if args.no_e2e:
         return dict(value=value, ms_per_step=ms_per_step, e2e=None, plain=None, stats=mstats, stages=stage_acc,
                     clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
-                    dev_ms=dev_ms, wall_ms=wall_ms)
+                    dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
     eng2 = new_engine()
     mids_of[eng2] = [eng2.create_map(s.params, s.heap_blocks) for s in specs]
     pin_in = []
@@ -359,24 +425,38 @@ def run_ours(args, rank, world, local, pg):
 
     return dict(value=value, ms_per_step=ms_per_step, e2e=e2e, plain=plain, stats=mstats, stages=stage_acc,
                 clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
-                dev_ms=dev_ms, wall_ms=wall_ms)
+                dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
 
 
 def algorithmic_bytes(s: dict) -> dict:
-    """Per-step algorithmic bytes.  Whole step: 12 B per point read, 16 B per
-    distinct voxel updated (8-B read + 8-B write), 16 B per block touched (its
-    hash entry), 20 B per new block (entry write + free-list pop), 16 B per
-    allocated block at step start twice (its key read by publish and by gc),
-    4096 B per publishing block, 20 B per published voxel, 20 B per collected
-    block.  Update stage: every touched block read and written back (8192 B).
-    Publish stage: the publishing blocks, the published voxels and the slot
-    scan."""
-    whole = (12 * s["n_points"] + 16 * s["distinct_voxels"] + 16 * s["blocks_touched"] + 20 * s["new_blocks"]
-             + 16 * s["alloc_blocks_before"] + 4096 * s["published_blocks"] + 20 * s["published"]
-             + 16 * s["alloc_blocks_before"] + 20 * s["gc_blocks"])
-    update = 8192 * s["blocks_touched"]
-    publish = 4096 * s["published_blocks"] + 20 * s["published"] + 24 * s["alloc_blocks_before"]
-    return {"step": whole, "update": update, "publish": publish}
+    """Per-step algorithmic bytes from the step's counters.
+
+    Whole step: 12 B per point (float3 read), 16 B per distinct voxel updated
+    (8-B read + 8-B write), 16 B per distinct block touched (its 16-B hash
+    entry), 20 B per new block (entry write + free-list pop), 16 B per block
+    allocated at step start twice (its key read by publish and by gc), 4096 B
+    per publishing block, 20 B per published voxel (12-B position + 8-B data),
+    20 B per collected block (entry write + push).
+
+    Per stage, the same terms where the stage does the work: ray_blocks and
+    ray_voxels each read the points and one entry per touched block;
+    alloc_order + alloc write the new blocks' entries; update reads and writes
+    the distinct voxels and reads the touched blocks' entries; publish reads the
+    keys, the publishing blocks and writes the published voxels; gc reads the
+    keys and writes the collected blocks' entries."""
+    N, V, K = s["n_points"], s["distinct_voxels"], s["blocks_touched"]
+    A, Pb, Pv = s["alloc_blocks_before"], s["published_blocks"], s["published"]
+    Kn, G = s["new_blocks"], s["gc_blocks"]
+    stage = {
+        "ray_blocks": 12 * N + 16 * K,
+        "ray_voxels": 12 * N + 16 * K,
+        "alloc": 20 * Kn,
+        "update": 16 * V + 16 * K,
+        "publish": 16 * A + 4096 * Pb + 20 * Pv,
+        "gc": 16 * A + 20 * G,
+    }
+    whole = 12 * N + 16 * V + 16 * K + 20 * Kn + 32 * A + 4096 * Pb + 20 * Pv + 20 * G
+    return {"step": whole, **stage}
 
 
 def load_peaks():
@@ -387,8 +467,9 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline_run(specs, scans, n_steps, warmup, threads):
-    """The oracle (reference algorithm as host code) on the same scans."""
+def port_baseline_run(specs, scans, n_steps, warmup, threads):
+    """The CPU oracle (a restatement of the reference's code) on the same
+    scans, one std::thread per map."""
     import oracle as O
 
     maps = [O.OracleMap(s.params, s.heap_blocks) for s in specs]
@@ -404,6 +485,52 @@ def cpu_baseline_run(specs, scans, n_steps, warmup, threads):
             t += dt
             pts += sum(x.shape[0] for x in xs)
     return pts / t, t
+
+
+def reference_run(specs, scans, n_steps, warmup):
+    """ros_tsdf's own integration code as host programs (oracle/ref.py): one
+    process per map integrates that map's scans 0..n_steps-1 through
+    processPointCloudAndUpdateVoxels; each call is timed inside the process.
+    Throughput = points of the scans after the warm-up / their summed call
+    time x the processes that ran at once (each process is one thread, so
+    that is the cores used).  Returns None where the programs are not built."""
+    from oracle import ref as R
+
+    if not R.available("float"):
+        return None
+    jobs = [(sp.params, [scans[m][k] for k in range(n_steps)]) for m, sp in enumerate(specs)]
+    t0 = time.perf_counter()
+    res, procs = R.run_many(jobs)
+    wall = time.perf_counter() - t0
+    secs = sum(r.scans[k].seconds for r in res for k in range(warmup, n_steps))
+    pts = sum(scans[m][k][0].shape[0] for m in range(len(specs)) for k in range(warmup, n_steps))
+    counts = [[r.scans[k].count for k in range(n_steps)] for r in res]
+    return {"value": pts / (secs / procs), "cores": procs, "seconds": secs, "wall_s": wall, "points": pts,
+            "counts": counts}
+
+
+def oracle_parity(specs, scans, stats_all, threads):
+    """Compare the engine's per-scan counters of every step and map with the
+    CPU oracle integrating the same scans (all 18 fields)."""
+    import oracle as O
+
+    maps = [O.OracleMap(s.params, s.heap_blocks, detail=True) for s in specs]
+    mism = []
+    caps = {f: 0 for f in ("block_overflow", "voxel_overflow", "route_overflow", "missing_updates", "bad_local",
+                           "heap_full_drops")}
+    for k, eng_stats in enumerate(stats_all):
+        xs = [scans[m][k][0] for m in range(len(specs))]
+        orgs = [scans[m][k][1] for m in range(len(specs))]
+        _, ost = O.integrate_many(maps, xs, orgs, pub_cap=0, threads=threads)
+        for m, (e, o) in enumerate(zip(eng_stats, ost)):
+            for f in O.STAT_FIELDS:
+                if e[f] != o[f] and len(mism) < 8:
+                    mism.append(f"step {k} map {m} {f}: engine {e[f]} oracle {o[f]}")
+            for f in caps:
+                caps[f] += o[f]
+    return {"parity": not mism, "checked": f"{len(O.STAT_FIELDS)} counters x {len(specs)} maps x "
+                                           f"{len(stats_all)} steps vs the CPU oracle",
+            "mismatches": mism, "caps": caps}
 
 
 def traffic_from_profiles(kernel: str, workload: str):
@@ -483,47 +610,56 @@ def run_serving(args, local: int) -> dict:
     return out
 
 
+def workload_config(workload: str, specs, points_per_step: float) -> dict:
+    """The workload's identity, the same in both arms' lines."""
+    return {"workload": workload, "maps": len(specs), "points_per_step": points_per_step,
+            "voxel_size": sorted({s.params.voxel_size for s in specs}),
+            "truncation_distance": sorted({s.params.truncation_distance for s in specs}),
+            "scans": "one seeded synthetic scan per map per step, the same scans in both arms"}
+
+
+STAGE_BYTES = {"ray_blocks": "ray_blocks", "ray_voxels": "ray_voxels", "alloc": "alloc", "alloc_order": "alloc",
+               "update": "update", "publish": "publish", "gc": "gc"}
+
+
 def result_line(args, r: dict, world: int, tuned, peak: float, peak_kind: str) -> dict:
     """The JSON line of our arm from run_ours's result: metric and value, the
-    workload config, e2e, the roofline of the dominant stage (algorithmic
-    bytes over its CUDA-event time, traffic from the ncu summaries), the stage
-    times, per-step counters, clocks and the engine's launch count."""
+    workload config, e2e, the roofline of the dominant stage (its algorithmic
+    bytes, algorithmic_bytes(), over its CUDA-event time; DRAM traffic from
+    the ncu summaries), the stage times, per-step counters, clocks and the
+    engine's launch count."""
     ab = algorithmic_bytes(r["stats"])
     stages = r["stages"]
     n = args.steps
     stage_ms = {k: v[0] / max(v[1], 1) for k, v in stages.items()}
     dom = max(stage_ms, key=stage_ms.get)
-    if dom == "update":
-        dom_bytes = ab["update"]
-    elif dom == "publish":
-        dom_bytes = ab["publish"]
-    else:
-        dom_bytes = ab["step"] * stage_ms[dom] / max(sum(stage_ms.values()), 1e-9)
+    dom_bytes = ab[STAGE_BYTES[dom]] if dom in STAGE_BYTES else 0.0
     kernel = "+".join(STAGE_KERNELS[dom][0]) if dom in STAGE_KERNELS else dom
     achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
     step_gbs = ab["step"] / (r["ms_per_step"] / 1000.0) / 1e9
+    traffic = stage_traffic(dom, args.workload, r["stats"])
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": n, "warmup": args.warmup,
         "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
-        "config": {"workload": args.workload, "maps": len(r["specs"]),
-                   "points_per_step": r["timed_pts"] / n,
-                   "voxel_size": sorted({s.params.voxel_size for s in r["specs"]}),
-                   "truncation_distance": sorted({s.params.truncation_distance for s in r["specs"]}),
-                   "l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step",
+        "config": workload_config(args.workload, r["specs"], r["timed_pts"] / n),
+        "method": {"l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step",
                    "timing": ("device time of each timed step from two CUDA events on the engine's stream around "
                               "it (its graph carries no events); stage_ms_per_step from "
-                              f"{min(args.steps, 5)} further steps with events around every stage"),
-                   "launch": tuned or {"bucket_size": args.bucket_size, "ray_chunk": args.ray_chunk,
-                                       "ray_threads": args.ray_threads, "source": "command line"}},
+                              f"{min(args.steps, 5)} further steps with events around every stage")},
+        "launch": tuned or {"bucket_size": args.bucket_size, "ray_chunk": args.ray_chunk,
+                            "ray_threads": args.ray_threads, "source": "command line"},
         "e2e": r["e2e"], "plain": r["plain"],
         "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": stage_traffic(dom, args.workload, r["stats"]),
+                     "algorithmic_bytes": dom_bytes, "traffic": traffic,
+                     "traffic_over_algorithmic": (traffic / dom_bytes) if traffic and dom_bytes else None,
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / peak},
         "stage_ms_per_step": stage_ms,
+        "algorithmic_bytes_per_step": ab,
         "per_step": {k: r["stats"][k] for k in ("n_points", "voxel_updates", "distinct_voxels", "blocks_touched",
-                                                "new_blocks", "published", "published_blocks", "gc_blocks")},
+                                                "new_blocks", "alloc_blocks_before", "published",
+                                                "published_blocks", "gc_blocks")},
         "voxel_updates_per_s": r["stats"]["voxel_updates"] / (r["ms_per_step"] / 1000.0),
         "call_ms_per_step": (sum(r["wall_ms"]) / max(len(r["wall_ms"]), 1)) if r.get("wall_ms") else None,
         "clocks": r["clocks"], "gpu_launches": r["gpu_launches"],
@@ -531,29 +667,45 @@ def result_line(args, r: dict, world: int, tuned, peak: float, peak_kind: str) -
     return line
 
 
+def reference_line(args) -> dict:
+    """The reference arm: ros_tsdf's own code on the host cores, on our arm's
+    workload, metric and unit."""
+    specs = make_workload(args.workload, 0, args.heap_blocks)
+    n_steps = args.warmup + args.steps
+    scans = gen_scans(specs, n_steps)
+    pts = sum(scans[m][k][0].shape[0] for m in range(len(specs)) for k in range(args.warmup, n_steps))
+    ref = reference_run(specs, scans, n_steps, args.warmup)
+    if ref is not None:
+        v, cores, kind = ref["value"], ref["cores"], "reference"
+        sample = (f"every map integrates scans 0..{n_steps - 1} through processPointCloudAndUpdateVoxels, one "
+                  f"process per map ({cores} at once); the {args.steps} scans after {args.warmup} warm-up scans "
+                  "are timed per call")
+        ms = ref["seconds"] / cores * 1000.0 / args.steps
+    else:
+        threads = os.cpu_count() or 1
+        v, t = port_baseline_run(specs, scans, n_steps, args.warmup, threads)
+        cores, kind, ms = min(threads, len(specs)), "port", t * 1000.0 / args.steps
+        sample = f"all {args.steps} timed steps ({args.warmup} warm-up), one host thread per map"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
+            "config": workload_config(args.workload, specs, pts / args.steps),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": ("ros_tsdf's tsdf_handler.cu and tsdf_container.cu compiled as sequential host programs "
+                     "(kernel launches become loops; its CUDA build needs device-side cudaDeviceSynchronize, "
+                     "which CUDA 13 rejects)") if kind == "reference" else
+                    "reference programs not built here: the CPU oracle, a restatement of its code, was timed"}
+    return line
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
-        if rank != 0:
-            return
-        specs = make_workload(args.workload, 0, args.heap_blocks)
-        n_steps = args.warmup + args.steps
-        scans = gen_scans(specs, n_steps)
-        threads = os.cpu_count() or 1
-        v, t = cpu_baseline_run(specs, scans, n_steps, args.warmup, threads)
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000.0 / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
-                "config": {"workload": args.workload, "maps": len(specs), "per_step": "one scan per map"},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": min(threads, len(specs)), "kind": "port",
-                                 "sample": f"all {args.steps} timed steps of the workload ({args.warmup} warm-up), "
-                                           "one host thread per map"},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "note": "reference CUDA path unbuildable here (CDP1 device-side cudaDeviceSynchronize is "
-                        "rejected by CUDA 13; Eigen/PCL/ROS2 absent); timed its algorithm as host code"}
-        print(json.dumps(line))
+        if rank == 0:
+            print(json.dumps(reference_line(args)))
         return
     if args.serving_only:
         if rank == 0:
@@ -571,13 +723,27 @@ def main():
     r = run_ours(args, rank, world, local, pg)
     peak, peak_kind = load_peaks()
     line = result_line(args, r, world, tuned, peak, peak_kind)
+    threads = min(os.cpu_count() or 1, len(r["specs"]))
+    if rank == 0:
+        line["parity"] = oracle_parity(r["specs"], r["scans"], r["stats_all"], threads)
     if rank == 0 and not args.no_cpu_baseline:
-        threads = min(os.cpu_count() or 1, len(r["specs"]))
-        v, t = cpu_baseline_run(r["specs"], r["scans"], min(args.warmup + 3, args.warmup + args.steps),
-                                args.warmup, threads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"first {args.warmup} steps untimed then 3 timed steps of the same "
-                                          "workload, one host thread per map"}
+        n_cpu = min(args.warmup + 3, args.warmup + args.steps)
+        pv, pt = port_baseline_run(r["specs"], r["scans"], n_cpu, args.warmup, threads)
+        port = {"value": pv, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"scans 0..{n_cpu - 1} of every map, the last {n_cpu - args.warmup} timed, one host "
+                          "thread per map"}
+        ref = reference_run(r["specs"], r["scans"], n_cpu, args.warmup)
+        if ref is not None:
+            eng_counts = [[r["stats_all"][k][m]["published"] for k in range(n_cpu)] for m in range(len(r["specs"]))]
+            line["cpu_baseline"] = {
+                "value": ref["value"], "unit": UNIT, "cores": ref["cores"], "kind": "reference",
+                "sample": (f"ros_tsdf's own integration code as host programs (one process per map, "
+                           f"{ref['cores']} at once) on scans 0..{n_cpu - 1} of every map, the last "
+                           f"{n_cpu - args.warmup} timed per call"),
+                "publish_counts_equal_engine": ref["counts"] == eng_counts,
+                "port": port}
+        else:
+            line["cpu_baseline"] = port
     if rank == 0 and args.serving_s > 0 and args.workload == "multimap32":
         line["serving"] = run_serving(args, local)
     if rank == 0:

@@ -278,3 +278,54 @@ def centre_to_key(centre: np.ndarray, size: float) -> np.ndarray:
     (tsdf_handler.cu:65-85): exact for |key| < 2^20."""
     c = np.asarray(centre, np.float64)
     return np.rint((c - size / 2.0) / size).astype(np.int64)
+
+
+# ---- timing (the CPU legs of bench.py) ----------------------------------------
+
+BYTES_PER_PROCESS = 7 << 30  # the reference's fixed heap twice (host and "device" copy) plus the hash table
+
+
+def concurrency(n_jobs: int) -> int:
+    """Processes to run at once: one per host core, bounded by the host memory
+    each reference process needs (its 524288-block heap is allocated twice)."""
+    cores = os.cpu_count() or 1
+    avail = None
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    by_mem = max(1, int(0.75 * avail) // BYTES_PER_PROCESS) if avail else 1
+    return max(1, min(cores, n_jobs, by_mem))
+
+
+def run_many(jobs, *, procs: int | None = None, pow_mode: str = "float", timeout: float = 1800.0):
+    """Run several maps, one reference process per map, at most `procs` at a
+    time.  jobs: [(params, scans)].  Returns ([RefResult per job], procs).
+    Publish data is not returned (counts and per-scan seconds are)."""
+    prog = PROGRAMS[pow_mode]
+    if not available(pow_mode):
+        raise RuntimeError(f"{prog} is not built for this machine (oracle.ref.build())")
+    procs = procs or concurrency(len(jobs))
+    results: list = [None] * len(jobs)
+    with tempfile.TemporaryDirectory(prefix="tsdf_ref_") as td:
+        pending = list(range(len(jobs)))
+        running: list = []
+        while pending or running:
+            while pending and len(running) < procs:
+                j = pending.pop(0)
+                params, scans = jobs[j]
+                inp, out = Path(td) / f"in{j}.bin", Path(td) / f"out{j}.bin"
+                _write_input(inp, params, scans, FLAG_INTEGRATE | FLAG_NO_PUBLISH_DATA, (), ())
+                p = subprocess.Popen([str(prog), str(inp), str(out)], stdout=subprocess.DEVNULL,
+                                     stderr=subprocess.PIPE, text=True)
+                running.append((j, p, out))
+            j, p, out = running.pop(0)
+            _, err = p.communicate(timeout=timeout)
+            if p.returncode != 0:
+                for _, q, _ in running:
+                    q.kill()
+                raise RuntimeError(f"reference harness exited {p.returncode}: {err[-2000:]}")
+            results[j] = _parse(out.read_bytes())
+    return results, procs

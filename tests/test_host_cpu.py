@@ -208,7 +208,7 @@ def test_bench_result_line_contract():
     stages = {"init": (0.01, 1), "update": (0.18, 1), "publish": (0.06, 1), "ray_voxels": (0.09, 1)}
     r = {"value": 3.0e8, "ms_per_step": 0.58, "stats": stats, "stages": stages, "specs": W.multimap32(4),
          "timed_pts": 1.8e6, "wall_ms": [0.7, 0.7], "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []},
-         "gpu_launches": 390, "plain": None,
+         "gpu_launches": 390, "plain": None, "scans": None, "stats_all": [],
          "e2e": {"value": 2.1e8, "unit": bench.UNIT, "h2d_bytes_per_step": 2, "d2h_bytes_per_step": 3}}
     args = SimpleNamespace(steps=10, warmup=3, workload="multimap32", bucket_size=1, ray_chunk=32, ray_threads=256)
     line = bench.result_line(args, r, 1, None, 6692.8, "measured")
@@ -221,8 +221,15 @@ def test_bench_result_line_contract():
     for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
         assert k in rf, k
     assert rf["stage"] == "update" and rf["kernel"] == "k_hot_chains+k_heavy_update+k_update"
-    assert abs(rf["achieved"] - 8192 * 1000 / 0.18e-3 / 1e9) < 1e-9 and abs(rf["frac"] - rf["achieved"] / 6692.8) < 1e-12
-    assert rf["traffic"] > 0
+    # the update stage's algorithmic bytes: 16 B per distinct voxel (read +
+    # write) and 16 B per touched block's entry
+    assert abs(rf["achieved"] - (16 * 1000 + 16 * 1000) / 0.18e-3 / 1e9) < 1e-9
+    assert abs(rf["frac"] - rf["achieved"] / 6692.8) < 1e-12
+    # ... and the fraction recomputes from the line's own counters and stage times
+    ps, sm = line["per_step"], line["stage_ms_per_step"]
+    again = (16 * ps["distinct_voxels"] + 16 * ps["blocks_touched"]) / (sm["update"] / 1e3) / 1e9 / rf["peak"]
+    assert abs(again - rf["frac"]) < 1e-12
+    assert rf["traffic"] > 0 and rf["traffic_over_algorithmic"] > 0
     for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"):
         assert k in line["e2e"], k
 
@@ -233,6 +240,7 @@ def test_bench_result_line_contract():
 
     bench.run_ours = lambda *a: r
     bench.dist_init = lambda n: (0, 1, 0, None)
+    bench.oracle_parity = lambda *a: {"parity": True}
     argv = _sys.argv
     _sys.argv = ["bench.py", "--steps", "10", "--warmup", "3", "--serving-s", "0", "--no-cpu-baseline", "--no-autotune"]
     out = io.StringIO()
@@ -243,3 +251,4 @@ def test_bench_result_line_contract():
         _sys.argv = argv
     lines = [x for x in out.getvalue().splitlines() if x.strip()]
     assert len(lines) == 1 and json.loads(lines[0])["value"] == 3.0e8
+    assert json.loads(lines[0])["parity"]["parity"] is True
