@@ -219,7 +219,9 @@ tsdf_status tsdf_forget(tsdf_engine* eng, uint64_t ticket);
  * order an empty map allocates them).  No map is touched.  xyz and kxyz may
  * be host or device memory.  *count = total (kxyz holds min(total, cap)).
  * TSDF_ERR_BAD_POINTS when points were skipped; TSDF_ERR_CAPACITY when
- * n_points x block-DDA cap exceeds the engine's scratch. */
+ * n_points x block-DDA cap exceeds the engine's scratch; TSDF_ERR_INVALID_ARG
+ * when voxel_size or truncation_distance is not finite and positive, or when
+ * a DDA cap ceil(2T / vs) * 4 exceeds 2^24 cells. */
 tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, const float* xyz, int64_t n_points,
                                   int stride_bytes, const float origin[3], int32_t* kxyz, int64_t cap,
                                   int64_t* count);
@@ -231,7 +233,8 @@ tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, c
  * nothing: xyz_dev and kxyz_dev are caller-owned device buffers and the
  * scratch is a fixed file-scope device array (about 1.2 MB per GPU that loads
  * the library, kept until exit).  Limit: n_points x ceil(2T / (8 vs)) * 4 <=
- * 32768, else TSDF_ERR_CAPACITY.  Runs on the current device, on `stream`
+ * 32768, else TSDF_ERR_CAPACITY; parameters as for tsdf_enumerate_blocks,
+ * else TSDF_ERR_INVALID_ARG.  Runs on the current device, on `stream`
  * (a cudaStream_t; NULL = default stream), and returns after *count is known.
  * The first call on a device resolves the array's address there and should
  * come before any stream capture.  Calls share the array: calls that overlap
@@ -322,11 +325,18 @@ tsdf_status tsdf_copy(tsdf_engine* eng, void* dst, const void* src, int64_t byte
  * returns the latest sample.  A stamp before the first or after the last
  * sample is TSDF_ERR_NO_POSE (TF2 raises an extrapolation error there).  The
  * buffer keeps the `capacity` newest samples; a sample at an existing stamp
- * replaces it.  Thread-safe. */
+ * replaces it.  Thread-safe.
+ * tsdf_pose_buffer_origin answers at once.  tsdf_pose_buffer_origin_wait first
+ * waits up to timeout_ms for a sample at or after the stamp to be added (the
+ * reference waits up to 1000 ms in lookupTransform, transformer.cpp:34, so a
+ * cloud that arrives just before its /tf sample still gets an origin), then
+ * answers as tsdf_pose_buffer_origin. */
 typedef struct tsdf_pose_buffer tsdf_pose_buffer;
 tsdf_status tsdf_pose_buffer_create(int64_t capacity, tsdf_pose_buffer** out);
 tsdf_status tsdf_pose_buffer_add(tsdf_pose_buffer* buf, int64_t stamp_ns, const double translation[3]);
 tsdf_status tsdf_pose_buffer_origin(tsdf_pose_buffer* buf, int64_t stamp_ns, float origin[3]);
+tsdf_status tsdf_pose_buffer_origin_wait(tsdf_pose_buffer* buf, int64_t stamp_ns, int64_t timeout_ms,
+                                         float origin[3]);
 int64_t tsdf_pose_buffer_size(tsdf_pose_buffer* buf);
 void tsdf_pose_buffer_destroy(tsdf_pose_buffer* buf);
 

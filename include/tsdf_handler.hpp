@@ -167,9 +167,12 @@ class PoseBuffer {
     const double t[3] = {x, y, z};
     if (tsdf_pose_buffer_add(buf_, stamp_ns, t) != TSDF_OK) throw std::runtime_error("tsdf_pose_buffer_add");
   }
-  Vector3f origin(int64_t stamp_ns = 0) const {
+  // timeout_ms > 0: wait that long for a sample at or after the stamp, as
+  // TF2's lookupTransform does (the reference passes 1000 ms).
+  Vector3f origin(int64_t stamp_ns = 0, int64_t timeout_ms = 0) const {
     Vector3f v{};
-    const tsdf_status st = tsdf_pose_buffer_origin(buf_, stamp_ns, v.data);
+    const tsdf_status st = timeout_ms > 0 ? tsdf_pose_buffer_origin_wait(buf_, stamp_ns, timeout_ms, v.data)
+                                          : tsdf_pose_buffer_origin(buf_, stamp_ns, v.data);
     if (st == TSDF_ERR_NO_POSE) throw std::out_of_range("no pose around the requested stamp");
     if (st != TSDF_OK) throw std::runtime_error("tsdf_pose_buffer_origin");
     return v;

@@ -125,6 +125,7 @@ SIGNATURES = [
     ("tsdf_pose_buffer_create", C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
     ("tsdf_pose_buffer_add", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
     ("tsdf_pose_buffer_origin", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
+    ("tsdf_pose_buffer_origin_wait", C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.POINTER(C.c_float)]),
     ("tsdf_pose_buffer_size", C.c_int64, [C.c_void_p]),
     ("tsdf_pose_buffer_destroy", None, [C.c_void_p]),
 ]

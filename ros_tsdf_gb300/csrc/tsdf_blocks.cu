@@ -328,6 +328,20 @@ long long eb_scratch_bytes(long long max_inc, long long* set_cap_out) {
   return eb_bytes(max_inc);
 }
 
+int eb_check(float voxel_size, float truncation_distance, long long n_points, long long max_inc) {
+  if (!(voxel_size > 0.0f) || !(truncation_distance > 0.0f) || !std::isfinite(voxel_size) ||
+      !std::isfinite(truncation_distance))
+    return 1;
+  // the DDA caps of initGlobalVars (tsdf_handler.cu:1311, :1315), checked as
+  // floats before they are converted to int
+  const float t2 = truncation_distance * 2.0f;
+  const float vmax = std::ceil(t2 / voxel_size) * 4.0f;
+  const float amax = std::ceil(t2 / (voxel_size * (float)kVoxelsPerSide)) * 4.0f;
+  if (!(vmax >= 4.0f && vmax <= (float)(1 << 24)) || !(amax >= 4.0f && amax <= (float)(1 << 24))) return 1;
+  if (n_points > max_inc / (long long)amax) return 2;
+  return 0;
+}
+
 // Enqueue the enumeration on `s` using `scratch` (eb_scratch_bytes(max_inc)
 // bytes, 256-byte aligned).  kxyz_dev: device-accessible output; the counters
 // {total, bad} are left in the scratch for eb_read_counts.
@@ -449,10 +463,9 @@ extern "C" tsdf_status tsdf_enumerate_blocks_noalloc(const tsdf_params* params, 
   if (!params || !origin || !count || n_points < 0 || (n_points > 0 && !xyz_dev) || cap < 0 ||
       (cap > 0 && !kxyz_dev) || stride_bytes < 12 || (stride_bytes & 3))
     return TSDF_ERR_INVALID_ARG;
-  if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f)) return TSDF_ERR_INVALID_ARG;
-  const float bs = params->voxel_size * (float)kVoxelsPerSide;
-  const int amax = (int)(std::ceil(params->truncation_distance * 2.0f / bs) * 4.0f);
-  if (amax <= 0 || n_points * (long long)amax > kNoAllocMaxInc) return TSDF_ERR_CAPACITY;
+  const int chk = eb_check(params->voxel_size, params->truncation_distance, n_points, kNoAllocMaxInc);
+  if (chk == 1) return TSDF_ERR_INVALID_ARG;
+  if (chk == 2) return TSDF_ERR_CAPACITY;
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return TSDF_ERR_CUDA;
   void* scratch = nullptr;

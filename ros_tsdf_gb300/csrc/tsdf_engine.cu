@@ -1293,13 +1293,16 @@ tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, c
   if (!eng || !params || !origin || !count || n_points < 0 || (n_points > 0 && !xyz) || cap < 0 ||
       (cap > 0 && !kxyz) || stride_bytes < 12 || (stride_bytes & 3))
     return TSDF_ERR_INVALID_ARG;
-  if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f)) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   if (eng->sched_running) return fail(eng, TSDF_ERR_BUSY, "served mode owns the lanes");
+  const long long max_inc = eng->cfg.max_batch_points * (long long)(eng->cfg.max_routes - 4);
+  const int chk = eb_check(params->voxel_size, params->truncation_distance, n_points, max_inc);
+  if (chk == 1) return fail(eng, TSDF_ERR_INVALID_ARG, "voxel_size and truncation_distance must be finite and positive");
+  if (chk == 2) return fail(eng, TSDF_ERR_CAPACITY, "points x block-DDA cap exceed the enumeration scratch");
   CK(cudaSetDevice(eng->device));
   Lane& L = eng->lanes[0];
   if (!eng->eb_scratch) {
-    eng->eb_max_inc = eng->cfg.max_batch_points * (long long)(eng->cfg.max_routes - 4);
+    eng->eb_max_inc = max_inc;
     CK(cudaMalloc(&eng->eb_scratch, (size_t)eb_scratch_bytes(eng->eb_max_inc, nullptr)));
     CK(cudaMalloc(&eng->eb_out, (size_t)eng->eb_max_inc * 3 * sizeof(int32_t)));
   }
@@ -1481,6 +1484,7 @@ struct tsdf_pose_buffer {
   int64_t cap = 0;
   std::deque<std::pair<int64_t, std::array<double, 3>>> s;
   std::mutex mu;
+  std::condition_variable added;  // notified by every tsdf_pose_buffer_add
 };
 
 tsdf_status tsdf_pose_buffer_create(int64_t capacity, tsdf_pose_buffer** out) {
@@ -1492,21 +1496,25 @@ tsdf_status tsdf_pose_buffer_create(int64_t capacity, tsdf_pose_buffer** out) {
 
 tsdf_status tsdf_pose_buffer_add(tsdf_pose_buffer* buf, int64_t stamp_ns, const double translation[3]) {
   if (!buf || !translation || stamp_ns <= 0) return TSDF_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(buf->mu);
-  const std::array<double, 3> t = {translation[0], translation[1], translation[2]};
-  auto it = std::lower_bound(buf->s.begin(), buf->s.end(), stamp_ns,
-                             [](const std::pair<int64_t, std::array<double, 3>>& a, int64_t v) { return a.first < v; });
-  if (it != buf->s.end() && it->first == stamp_ns)
-    it->second = t;
-  else
-    buf->s.insert(it, {stamp_ns, t});
-  while ((int64_t)buf->s.size() > buf->cap) buf->s.pop_front();
+  {
+    std::lock_guard<std::mutex> lk(buf->mu);
+    const std::array<double, 3> t = {translation[0], translation[1], translation[2]};
+    auto it = std::lower_bound(buf->s.begin(), buf->s.end(), stamp_ns,
+                               [](const std::pair<int64_t, std::array<double, 3>>& a, int64_t v) { return a.first < v; });
+    if (it != buf->s.end() && it->first == stamp_ns)
+      it->second = t;
+    else
+      buf->s.insert(it, {stamp_ns, t});
+    while ((int64_t)buf->s.size() > buf->cap) buf->s.pop_front();
+  }
+  buf->added.notify_all();
   return TSDF_OK;
 }
 
-tsdf_status tsdf_pose_buffer_origin(tsdf_pose_buffer* buf, int64_t stamp_ns, float origin[3]) {
-  if (!buf || !origin || stamp_ns < 0) return TSDF_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(buf->mu);
+namespace {
+
+// The lookup of tsdf_pose_buffer_origin with buf->mu held.
+tsdf_status pose_lookup(tsdf_pose_buffer* buf, int64_t stamp_ns, float origin[3]) {
   if (buf->s.empty()) return TSDF_ERR_NO_POSE;
   std::array<double, 3> r;
   if (stamp_ns == 0) {
@@ -1525,6 +1533,26 @@ tsdf_status tsdf_pose_buffer_origin(tsdf_pose_buffer* buf, int64_t stamp_ns, flo
   }
   for (int k = 0; k < 3; ++k) origin[k] = (float)r[k];
   return TSDF_OK;
+}
+
+}  // namespace
+
+tsdf_status tsdf_pose_buffer_origin(tsdf_pose_buffer* buf, int64_t stamp_ns, float origin[3]) {
+  if (!buf || !origin || stamp_ns < 0) return TSDF_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(buf->mu);
+  return pose_lookup(buf, stamp_ns, origin);
+}
+
+tsdf_status tsdf_pose_buffer_origin_wait(tsdf_pose_buffer* buf, int64_t stamp_ns, int64_t timeout_ms,
+                                         float origin[3]) {
+  if (!buf || !origin || stamp_ns < 0 || timeout_ms < 0) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::mutex> lk(buf->mu);
+  // TF2's lookupTransform with a timeout (transformer.cpp:34) waits for the
+  // sample that brackets the stamp; a stamp before the oldest sample cannot
+  // be helped by waiting.
+  auto ready = [&] { return !buf->s.empty() && (stamp_ns == 0 || buf->s.back().first >= stamp_ns); };
+  buf->added.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready);
+  return pose_lookup(buf, stamp_ns, origin);
 }
 
 int64_t tsdf_pose_buffer_size(tsdf_pose_buffer* buf) {

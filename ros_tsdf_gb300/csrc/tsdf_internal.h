@@ -266,6 +266,11 @@ void launch_check_div(unsigned long long seed, long long n, unsigned long long* 
 
 // Block enumeration of one scan (tsdf_blocks.cu).
 long long eb_scratch_bytes(long long max_inc, long long* set_cap_out);
+// Parameters and size of one enumeration: 0 when it fits max_inc block
+// incidences, 1 for parameters that are not finite and positive or whose DDA
+// caps do not fit an int, 2 when n_points x block-DDA cap exceeds max_inc.
+// eb_launch may only be called after eb_check returned 0.
+int eb_check(float voxel_size, float truncation_distance, long long n_points, long long max_inc);
 int eb_launch(void* scratch, long long max_inc, const float* xyz_dev, long long n, int stride, const float origin[3],
               float voxel_size, float truncation_distance, int32_t* kxyz_dev, long long cap, int sm_count,
               cudaStream_t s);

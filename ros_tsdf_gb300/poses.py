@@ -40,10 +40,16 @@ class PoseBuffer:
         if st != L.OK:
             raise ValueError(f"tsdf_pose_buffer_add: {L.STATUS_NAMES.get(st, st)}")
 
-    def origin(self, stamp_ns: int = 0) -> np.ndarray:
-        """Translation at stamp_ns (0: the latest sample)."""
+    def origin(self, stamp_ns: int = 0, timeout_ms: int = 0) -> np.ndarray:
+        """Translation at stamp_ns (0: the latest sample).  With timeout_ms > 0
+        a stamp newer than every sample waits up to that long for a sample
+        that reaches it (TF2's lookupTransform timeout; the reference waits
+        1000 ms)."""
         out = (C.c_float * 3)()
-        st = self.lib.tsdf_pose_buffer_origin(self.h, int(stamp_ns), out)
+        if timeout_ms > 0:
+            st = self.lib.tsdf_pose_buffer_origin_wait(self.h, int(stamp_ns), int(timeout_ms), out)
+        else:
+            st = self.lib.tsdf_pose_buffer_origin(self.h, int(stamp_ns), out)
         if st == L.ERR_NO_POSE:
             raise NoPoseError(f"no pose around stamp {stamp_ns}")
         if st != L.OK:

@@ -188,6 +188,33 @@ def test_pose_buffer_origin_lookup(built):
         assert np.array_equal(b.origin(3_500_000_000), np.float32([3.5, 3.5, 3.5]))
 
 
+def test_pose_buffer_waits_for_a_late_sample(built):
+    """A cloud stamped after the newest pose waits (up to its timeout) for the
+    sample that reaches its stamp, as TF2's lookupTransform with a timeout
+    does; without one in time it fails after the timeout."""
+    import threading
+    import time
+
+    from ros_tsdf_gb300.poses import NoPoseError, PoseBuffer
+
+    with PoseBuffer(capacity=8) as b:
+        b.add(1_000_000_000, (0.0, 0.0, 0.0))
+        t = threading.Timer(0.05, lambda: b.add(2_000_000_000, (2.0, 4.0, 6.0)))
+        t.start()
+        t0 = time.monotonic()
+        got = b.origin(1_500_000_000, timeout_ms=2000)
+        waited = time.monotonic() - t0
+        t.join()
+        assert np.array_equal(got, np.float32([1.0, 2.0, 3.0]))
+        assert 0.03 < waited < 1.5
+        t0 = time.monotonic()
+        with pytest.raises(NoPoseError):
+            b.origin(5_000_000_000, timeout_ms=40)
+        assert time.monotonic() - t0 >= 0.035
+        with pytest.raises(NoPoseError):      # before the oldest sample: no wait helps
+            b.origin(10, timeout_ms=1000)
+
+
 def test_bench_result_line_contract():
     """bench.py's JSON line carries every key of the benchmark contract, with
     the roofline of the dominant stage and the e2e record, from a synthetic
