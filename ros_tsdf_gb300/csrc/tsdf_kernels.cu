@@ -1661,7 +1661,6 @@ __global__ void __launch_bounds__(128) k_hot_chains(Ctx c) {
 }
 
 __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
-  __shared__ __align__(16) float2 s_vox[kVoxelsPerBlock];
   // record bit masks per voxel, word-major (word w covers records 32w..32w+31)
   // so that 16-byte accesses of four consecutive voxels hit distinct banks
   __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];
@@ -1669,7 +1668,6 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
   __shared__ unsigned short s_l[kLightEntries];
   __shared__ int s_bin_run[kVoxelsPerBlock];  // light path: bins (ushort); pass-based path: per-voxel cursors
   __shared__ int s_off[kVoxelsPerBlock + 1];
-  __shared__ unsigned s_touch[kVoxelsPerBlock / 32];
   __shared__ int s_warp[32];
   __shared__ long long s_seg;
   __shared__ unsigned long long s_base;
@@ -1714,13 +1712,14 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
     const int item = c.seg_item[sj];
     const MapDev& m = c.maps[c.items[item].map];
     const float maxw = m.maxw;
-    float4* gv = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
-    float4* sv4 = reinterpret_cast<float4*>(s_vox);
-    sv4[t] = gv[t];
-    sv4[t + UPD_T] = gv[t + UPD_T];
-    if (t < kVoxelsPerBlock / 32) s_touch[t] = 0;
-    __syncthreads();  // the staged block and touch mask are shared by every path below
-    // next item: segment bounds now, its block and records further down
+    // Only the voxels that get updates are read and written: each is owned by
+    // thread l % UPD_T, which loads it once its update count is known and
+    // stores it after its chain.  The block's non-zero count moves by the
+    // owned voxels whose weight left zero (weights never return to zero).
+    float2* gv2 = c.voxels + phys * kVoxelsPerBlock;
+    int nz_delta = 0, touched = 0;
+    __syncthreads();  // s_seg's next value is read below
+    // next item: segment bounds now, its records further down
     const long long qn = s_seg;
     long long nb0 = -1, nb1 = 0;
     if (qn < nqueue && !(qn < nplanned && c.hfit[qn])) {
@@ -1755,11 +1754,8 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
           }
         });
         __syncthreads();
-        unsigned nrk = 0u, nrv = 0u;
-        if (nb0 >= 0) {
-          nrk = rk[nb0];
-          if (nb0 + t < nb1) nrv = rv[nb0 + t];
-        }
+        unsigned nrv = 0u;
+        if (nb0 >= 0 && nb0 + t < nb1) nrv = rv[nb0 + t];
         {
           int a[4];
           mask_counts(&s_mask[0][0], t, a);
@@ -1772,15 +1768,17 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
           if (t == 0) s_off[kVoxelsPerBlock] = tot;
         }
         __syncthreads();
-        if (nb0 >= 0) {
-          const float4* ngv = reinterpret_cast<const float4*>(c.voxels + (h.key_lo + nrk) * kVoxelsPerBlock);
-          prefetch_l1(ngv + t);
-          prefetch_l1(ngv + t + UPD_T);
-          if ((nrv & 31u) != 0u) {
-            const uint2* ne0 = c.entries + (nrv >> 5);
-            prefetch_l1(ne0);
-            prefetch_l1(ne0 + (nrv & 31u) - 1);
-          }
+        // the owned voxels with updates, loaded now: the rank phase hides the latency
+        float2 ov[kVoxelsPerBlock / UPD_T];
+#pragma unroll
+        for (int j = 0; j < kVoxelsPerBlock / UPD_T; ++j) {
+          const int l = t + UPD_T * j;
+          ov[j] = s_off[l + 1] > s_off[l] ? gv2[l] : make_float2(0.f, 0.f);
+        }
+        if ((nrv & 31u) != 0u) {
+          const uint2* ne0 = c.entries + (nrv >> 5);
+          prefetch_l1(ne0);
+          prefetch_l1(ne0 + (nrv & 31u) - 1);
         }
         for (int k = 0; k < cnt; ++k) {
           const int l = s_l[eoff + k];
@@ -1790,13 +1788,16 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
           s_bin[s_off[l] + rank] = (unsigned short)(eoff + k);
         }
         __syncthreads();
-        for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
+#pragma unroll
+        for (int j = 0; j < kVoxelsPerBlock / UPD_T; ++j) {
+          const int l = t + UPD_T * j;
           const int b = s_off[l], e = s_off[l + 1];
           if (e == b) continue;
-          float sdf = s_vox[l].x, w = s_vox[l].y;
+          float sdf = ov[j].x, w = ov[j].y;
           for (int a = b; a < e; ++a) update_voxel(&sdf, &w, s_d[s_bin[a]], maxw);
-          s_vox[l] = make_float2(sdf, w);
-          atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+          gv2[l] = make_float2(sdf, w);
+          nz_delta += (int)(w != 0.0f) - (int)(ov[j].y != 0.0f);
+          ++touched;
         }
         __syncthreads();
       }
@@ -1870,21 +1871,19 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
         for (int l = t; l < kVoxelsPerBlock; l += UPD_T) {
           const int b = s_off[l], e = s_off[l + 1];
           if (e == b) continue;
-          float sdf = s_vox[l].x;
-          const float w = apply_chain(&sdf, s_vox[l].y, c.bin_d + base + b, e - b, maxw);
-          s_vox[l] = make_float2(sdf, w);
-          atomicOr(&s_touch[l >> 5], 1u << (l & 31));
+          const float2 v0 = gv2[l];
+          float sdf = v0.x;
+          const float w = apply_chain(&sdf, v0.y, c.bin_d + base + b, e - b, maxw);
+          gv2[l] = make_float2(sdf, w);
+          nz_delta += (int)(w != 0.0f) - (int)(v0.y != 0.0f);
+          ++touched;
         }
       }
       __syncthreads();
     }
-    const float4 va = sv4[t], vb = sv4[t + UPD_T];
-    gv[t] = va;
-    gv[t + UPD_T] = vb;
-    // one reduction for the three block totals: non-zero weights, touched
-    // voxels, applied updates
-    int nz = (va.y != 0.0f) + (va.w != 0.0f) + (vb.y != 0.0f) + (vb.w != 0.0f);
-    int touched = t < kVoxelsPerBlock / 32 ? __popc(s_touch[t]) : 0;
+    // one reduction for the three block totals: change of the non-zero
+    // weights, touched voxels, applied updates
+    int nz = nz_delta;
     int upd = (int)n_upd;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -1901,7 +1900,7 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
     if (t == 0) {
       int a = 0, b = 0, u = 0;
       for (int w = 0; w < UPD_T / 32; ++w) a += s_warp[3 * w], b += s_warp[3 * w + 1], u += s_warp[3 * w + 2];
-      c.nnz[phys] = a;
+      c.nnz[phys] += a;
       stat_add(c.item_stats, item, ST_UPD, u);
       stat_add(c.item_stats, item, ST_DVOX, b);
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
