@@ -94,6 +94,14 @@ typedef struct tsdf_engine_cfg {
   int hot_chains;           /* capacity of the grid-wide list of long voxel
                                update chains per step (default 65536, even;
                                chains beyond it run inside their block's CTA) */
+  int sdf_mode;             /* 0 (default): every voxel's updates applied one
+                               by one in point order, bit-identical to the
+                               reference's update rule.  1: the long chains
+                               of the grid-wide list (voxels with more than
+                               128 updates in a step) as one composition of
+                               their updates' affine maps in double, rounded
+                               once: weights, block sets and publish sets stay
+                               exact, sdf within 1e-5 x truncation distance   */
 } tsdf_engine_cfg;
 
 /* Per-scan counters; the field order matches the oracle's. */

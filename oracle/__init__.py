@@ -201,8 +201,11 @@ def point_stages(params, xyz, origin) -> dict:
             "capped": int(capped)}
 
 
-def integrate_many(maps: list, scans: list, origins, pub_cap: int = 0, threads: int | None = None):
-    """Integrate scans[i] into maps[i] in parallel (one std::thread per map)."""
+def integrate_many(maps: list, scans: list, origins, pub_cap: int = 0, threads: int | None = None,
+                   return_published: bool = False):
+    """Integrate scans[i] into maps[i] in parallel (one std::thread per map).
+    Returns (counts, stats), and with return_published also the published
+    positions and data of each map (the first min(count, pub_cap))."""
     L = lib()
     n = len(maps)
     arrs = [np.ascontiguousarray(s, np.float32) for s in scans]
@@ -218,4 +221,9 @@ def integrate_many(maps: list, scans: list, origins, pub_cap: int = 0, threads: 
     dp = (C.c_void_p * n)(*[d.ctypes.data for d in dat])
     caps = (C.c_int64 * n)(*([pub_cap] * n))
     L.oracle_integrate_many(hs, n, xs, ns, 12, org, pp, dp, caps, cnt, st, threads or os.cpu_count() or 1)
-    return [int(c) for c in cnt], [{f: int(getattr(s, f)) for f in STAT_FIELDS} for s in st]
+    counts = [int(c) for c in cnt]
+    stats = [{f: int(getattr(s, f)) for f in STAT_FIELDS} for s in st]
+    if not return_published:
+        return counts, stats
+    kept = [min(c, pub_cap) for c in counts]
+    return counts, stats, [p[:k] for p, k in zip(pos, kept)], [d[:k] for d, k in zip(dat, kept)]

@@ -49,7 +49,7 @@ class EngineCfg(C.Structure):
     _fields_ = [("device", C.c_int), ("max_maps", C.c_int), ("pool_blocks", C.c_int64),
                 ("max_batch_points", C.c_int64), ("max_publish", C.c_int64), ("bucket_size", C.c_int),
                 ("ray_threads", C.c_int), ("ray_chunk", C.c_int), ("max_routes", C.c_int), ("lanes", C.c_int),
-                ("no_graphs", C.c_int), ("hot_chains", C.c_int)]
+                ("no_graphs", C.c_int), ("hot_chains", C.c_int), ("sdf_mode", C.c_int)]
 
 
 class ScanStats(C.Structure):

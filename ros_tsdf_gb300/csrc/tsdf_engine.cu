@@ -318,6 +318,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   x.hbin_cap = std::min<long long>(entry_cap, std::max<long long>(1ll << 23, npts * 32));
   TRY(dalloc(eng, &x.hbin, x.hbin_cap, tr));
   x.hot_cap = c.hot_chains;
+  x.sdf_scan = c.sdf_mode == 1 ? 1 : 0;
   TRY(dalloc(eng, &x.hot, x.hot_cap, tr));
   TRY(dalloc(eng, &x.hmask, (long long)(x.hchunk_cap / 2 + 1) * (kVoxelsPerBlock / 32), tr));
   x.entry_cap = entry_cap;
@@ -865,6 +866,7 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   if (c.lanes <= 0) c.lanes = 1;
   if (c.hot_chains <= 0) c.hot_chains = 1 << 16;
   if (c.hot_chains < 2 || c.hot_chains > (1 << 24)) return TSDF_ERR_INVALID_ARG;
+  if (c.sdf_mode != 0 && c.sdf_mode != 1) return TSDF_ERR_INVALID_ARG;
   c.hot_chains &= ~1;
   if (c.lanes > kMaxLanes) c.lanes = kMaxLanes;
   if (c.max_routes < 8 || c.max_routes > 64) return TSDF_ERR_INVALID_ARG;

@@ -207,6 +207,7 @@ struct Ctx {
   HotChain* hot;                 // [hot_cap]: long chains in the first half, the rest in the second
   unsigned* hmask;               // [hchunk_cap/2][16] voxels of a planned heavy segment on the hot list
   long long hot_cap;
+  int sdf_scan;                  // engine sdf_mode 1: hot chains as one affine-map composition
   int hchunk_cap;
   int max_tiles_rank;
   int max_tiles_rec;

@@ -73,10 +73,10 @@ class Engine:
     def __init__(self, device: int = 0, max_maps: int = 64, pool_blocks: int = 1 << 18,
                  max_batch_points: int = 1 << 20, max_publish: int = 1 << 23, bucket_size: int = 1,
                  ray_threads: int = 256, ray_chunk: int = 32, max_routes: int = 16, lanes: int = 1,
-                 graphs: bool = True, hot_chains: int = 0):
+                 graphs: bool = True, hot_chains: int = 0, sdf_mode: int = 0):
         self.lib = L.load()
         cfg = L.EngineCfg(device, max_maps, pool_blocks, max_batch_points, max_publish, bucket_size,
-                          ray_threads, ray_chunk, max_routes, lanes, 0 if graphs else 1, hot_chains)
+                          ray_threads, ray_chunk, max_routes, lanes, 0 if graphs else 1, hot_chains, sdf_mode)
         h = C.c_void_p()
         st = self.lib.tsdf_engine_create(C.byref(cfg), C.byref(h))
         if st != L.OK:

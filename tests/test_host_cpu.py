@@ -237,7 +237,8 @@ def test_bench_result_line_contract():
          "timed_pts": 1.8e6, "wall_ms": [0.7, 0.7], "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []},
          "gpu_launches": 390, "plain": None, "scans": None, "stats_all": [],
          "e2e": {"value": 2.1e8, "unit": bench.UNIT, "h2d_bytes_per_step": 2, "d2h_bytes_per_step": 3}}
-    args = SimpleNamespace(steps=10, warmup=3, workload="multimap32", bucket_size=1, ray_chunk=32, ray_threads=256)
+    args = SimpleNamespace(steps=10, warmup=3, workload="multimap32", bucket_size=1, ray_chunk=32, ray_threads=256,
+                           sdf_mode=0)
     line = bench.result_line(args, r, 1, None, 6692.8, "measured")
     json.dumps(line)
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
