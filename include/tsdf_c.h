@@ -57,7 +57,8 @@ typedef enum tsdf_status {
   TSDF_ERR_BUSY = 8,              /* map already has a scan in flight         */
   TSDF_ERR_NOT_READY = 9,         /* tsdf_poll: request still running         */
   TSDF_ERR_BAD_POINTS = 10,       /* warning: some points were skipped        */
-  TSDF_ERR_NO_POSE = 11           /* pose buffer: stamp outside its samples    */
+  TSDF_ERR_NO_POSE = 11,          /* pose buffer: stamp outside its samples    */
+  TSDF_ERR_INVARIANT = 12         /* tsdf_map_check: a map invariant is broken */
 } tsdf_status;
 
 typedef struct tsdf_engine tsdf_engine;
@@ -260,6 +261,32 @@ tsdf_status tsdf_dump_blocks(tsdf_engine* eng, int map_id, int32_t* kxyz, int32_
 tsdf_status tsdf_dump_free_list(tsdf_engine* eng, int map_id, int32_t* out, int64_t cap, int64_t* block_count);
 /* The 512 voxels of one heap slot. */
 tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, tsdf_voxel* out512);
+
+/* Host-side invariant check of an idle map (the reference has none; its
+ * races can corrupt the table silently).  Copies the map's block keys, free
+ * list, hash table, non-zero counts and weights to the host and counts
+ * violations of:
+ *   - every allocated slot holds a distinct block key;
+ *   - the free list's free part (entries block_count..heap_blocks-1) and the
+ *     allocated slots together name every heap slot exactly once;
+ *   - every allocated key is found by the hash table's probe sequence, at
+ *     its slot, and the table holds no other live entry;
+ *   - no entry is left pending or ranked from a step;
+ *   - each allocated block's non-zero count equals its voxels with a
+ *     non-zero weight, and every free slot's count is zero.
+ * TSDF_OK when all hold, TSDF_ERR_INVARIANT otherwise; *out (may be NULL)
+ * receives the counts. */
+typedef struct tsdf_map_check_report {
+  int64_t allocated;          /* allocated slots (block_count)                 */
+  int64_t duplicate_keys;     /* allocated slots whose key another slot holds  */
+  int64_t free_list_errors;   /* heap slots named zero or several times        */
+  int64_t unfindable_keys;    /* allocated keys the probe does not find        */
+  int64_t slot_mismatches;    /* found entries pointing at another slot        */
+  int64_t stray_entries;      /* live entries without an allocated slot        */
+  int64_t pending_entries;    /* entries left pending or ranked                */
+  int64_t nnz_mismatches;     /* blocks whose non-zero count is wrong          */
+} tsdf_map_check_report;
+tsdf_status tsdf_map_check(tsdf_engine* eng, int map_id, tsdf_map_check_report* out);
 
 /* Map snapshot and restore.  The reference has neither (its one map lives and
  * dies with the process); they let a serving loop evict a map and admit it

@@ -20,10 +20,13 @@
 #ifndef TSDF_HANDLER_HPP
 #define TSDF_HANDLER_HPP
 
+#include <array>
 #include <cstdint>
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "tsdf_c.h"
@@ -91,12 +94,53 @@ inline void initGlobalVars(float voxel_size, float truncation_distance, float ma
 }
 
 // Hash table + block heap of one map (tsdf_container.cuh:112-133).
+// Host-side views of a map's state, copied out of the device.  The reference's
+// getCudaHashTable() / getCudaBlockHeap() (tsdf_container.cuh:121-125) hand
+// out device pointers to its own HashTable / BlockHeap structs; this engine
+// keeps its hash table and heap in its own layout, so the accessors return
+// what those structs hold instead.
+struct HashTableView {
+  std::vector<std::array<int32_t, 3>> keys;  // block coordinates floor(centre / block size)
+  std::vector<int32_t> heap_pos;             // heap slot of each block (ascending)
+};
+struct BlockHeapView {
+  int64_t block_count = 0;                   // allocated blocks (BlockHeap::block_count)
+  std::vector<int32_t> free_blocks;          // BlockHeap::free_blocks, heap_blocks entries
+};
+
 class TSDFContainer {
  public:
   TSDFContainer(tsdf_engine* eng, int64_t heap_blocks) : eng_(eng) {
     detail::Globals& g = detail::globals();
     if (!g.set) throw std::runtime_error("initGlobalVars must be called before TSDFHandler()");
     detail::check(eng_, tsdf_map_create(eng_, &g.params, heap_blocks, &map_), "tsdf_map_create");
+  }
+  // tsdf_container.cuh:121-122: the allocated blocks and their heap slots.
+  HashTableView getCudaHashTable() const {
+    HashTableView v;
+    int64_t n = 0;
+    detail::check(eng_, tsdf_dump_blocks(eng_, map_, nullptr, nullptr, 0, &n), "tsdf_dump_blocks");
+    v.keys.resize((size_t)n);
+    v.heap_pos.resize((size_t)n);
+    detail::check(eng_, tsdf_dump_blocks(eng_, map_, n ? v.keys[0].data() : nullptr, v.heap_pos.data(), n, &n),
+                  "tsdf_dump_blocks");
+    return v;
+  }
+  // tsdf_container.cuh:124-125: block count and free list.
+  BlockHeapView getCudaBlockHeap() const {
+    BlockHeapView v;
+    tsdf_map_info info{};
+    detail::check(eng_, tsdf_map_info_get(eng_, map_, &info), "tsdf_map_info_get");
+    v.free_blocks.resize((size_t)info.heap_blocks);
+    detail::check(eng_, tsdf_dump_free_list(eng_, map_, v.free_blocks.data(), info.heap_blocks, &v.block_count),
+                  "tsdf_dump_free_list");
+    return v;
+  }
+  // The 512 voxels of one heap slot (BlockHeap::blocks[slot].voxels).
+  std::vector<tsdf_voxel> blockVoxels(int32_t slot) const {
+    std::vector<tsdf_voxel> out(512);
+    detail::check(eng_, tsdf_dump_block_voxels(eng_, map_, slot, out.data()), "tsdf_dump_block_voxels");
+    return out;
   }
   ~TSDFContainer() {
     if (map_ >= 0) tsdf_map_destroy(eng_, map_);
@@ -105,10 +149,12 @@ class TSDFContainer {
   TSDFContainer& operator=(const TSDFContainer&) = delete;
   int mapId() const { return map_; }
   tsdf_engine* engine() const { return eng_; }
+  const tsdf_params& params() const { return params_; }
 
  private:
   tsdf_engine* eng_;
   int map_ = -1;
+  tsdf_params params_ = detail::globals().params;
 };
 
 class TSDFHandler {
@@ -127,16 +173,47 @@ class TSDFHandler {
   void processPointCloudAndUpdateVoxels(const PointXYZ* points, int64_t n, Vector3f* lidar_position_h,
                                         Vector3f* publish_voxels_pos_h, int* publish_voxels_size_h,
                                         Voxel* publish_voxels_data_h, int64_t capacity = PUBLISH_VOXELS_MAX_SIZE) {
-    const int start = *publish_voxels_size_h;
-    if (start < 0 || start > capacity) throw std::runtime_error("publish_voxels_size out of range");
+    integrate_records(points ? &points[0].x : nullptr, n, (int)sizeof(PointXYZ), lidar_position_h,
+                      publish_voxels_pos_h, publish_voxels_size_h, publish_voxels_data_h, capacity);
+  }
+
+  // tsdf_handler.cuh:50-51 as the reference declares it: a pointer-like
+  // cloud (pcl::PointCloud<pcl::PointXYZ>::Ptr) whose `points` hold x, y, z
+  // as the first three floats of each record; records are read at their
+  // stride (16 bytes for pcl::PointXYZ).
+  template <class CloudPtr,
+            class = decltype(std::declval<const CloudPtr&>()->points.data()->x)>
+  void processPointCloudAndUpdateVoxels(const CloudPtr& cloud, Vector3f* lidar_position_h,
+                                        Vector3f* publish_voxels_pos_h, int* publish_voxels_size_h,
+                                        Voxel* publish_voxels_data_h) {
+    const auto& pts = cloud->points;
+    using P = typename std::decay<decltype(pts[0])>::type;
+    static_assert(sizeof(P) >= 12 && sizeof(P) % 4 == 0, "point records must hold x, y, z floats");
+    integrate_records(pts.empty() ? nullptr : &pts[0].x, (int64_t)pts.size(), (int)sizeof(P), lidar_position_h,
+                      publish_voxels_pos_h, publish_voxels_size_h, publish_voxels_data_h, PUBLISH_VOXELS_MAX_SIZE);
+  }
+
+  // tsdf_handler.cuh:58-59, getVoxelBlocks (+ removeRedundantVoxels): the
+  // distinct voxel blocks the block DDA of every point visits, in first-touch
+  // order, as block centres computed like getVolumeCenterFromPoint
+  // (floor(x * scale) / scale + half block, tsdf_handler.cu:65-85).  The map
+  // is not changed.  Returns the number of blocks (the first `capacity` are
+  // written).
+  int getVoxelBlocks(const PointXYZ* points, int64_t n, const Vector3f* lidar_position, Vector3f* voxel_blocks,
+                     int capacity) const {
+    const tsdf_params& p = container_.params();
+    std::vector<int32_t> keys((size_t)capacity * 3 + 3);
     int64_t count = 0;
-    tsdf_status st = tsdf_integrate(container_.engine(), container_.mapId(), reinterpret_cast<const float*>(points),
-                                    n, (int)sizeof(PointXYZ), lidar_position_h->data,
-                                    reinterpret_cast<float*>(publish_voxels_pos_h + start),
-                                    publish_voxels_data_h + start, capacity - start, &count, &last_stats_);
-    detail::check(container_.engine(), st, "processPointCloudAndUpdateVoxels");
-    last_status_ = st;
-    *publish_voxels_size_h = start + (int)count;
+    const tsdf_status st = tsdf_enumerate_blocks(container_.engine(), &p, reinterpret_cast<const float*>(points), n,
+                                                 (int)sizeof(PointXYZ), lidar_position->data, keys.data(), capacity,
+                                                 &count);
+    detail::check(container_.engine(), st, "getVoxelBlocks");
+    const float bs = p.voxel_size * 8.0f;
+    const float scale = 1.0f / bs;
+    const float half = bs / 2.0f;
+    for (int64_t i = 0; i < count && i < capacity; ++i)
+      for (int a = 0; a < 3; ++a) voxel_blocks[i].data[a] = (float)keys[3 * i + a] / scale + half;
+    return (int)count;
   }
 
   tsdf_status lastStatus() const { return last_status_; }
@@ -144,6 +221,20 @@ class TSDFHandler {
   const TSDFContainer& container() const { return container_; }
 
  private:
+  void integrate_records(const float* xyz, int64_t n, int stride, Vector3f* lidar_position_h,
+                         Vector3f* publish_voxels_pos_h, int* publish_voxels_size_h, Voxel* publish_voxels_data_h,
+                         int64_t capacity) {
+    const int start = *publish_voxels_size_h;
+    if (start < 0 || start > capacity) throw std::runtime_error("publish_voxels_size out of range");
+    int64_t count = 0;
+    tsdf_status st = tsdf_integrate(container_.engine(), container_.mapId(), xyz, n, stride, lidar_position_h->data,
+                                    reinterpret_cast<float*>(publish_voxels_pos_h + start),
+                                    publish_voxels_data_h + start, capacity - start, &count, &last_stats_);
+    detail::check(container_.engine(), st, "processPointCloudAndUpdateVoxels");
+    last_status_ = st;
+    *publish_voxels_size_h = start + (int)count;
+  }
+
   TSDFContainer container_;
   tsdf_status last_status_ = TSDF_OK;
   tsdf_scan_stats last_stats_{};

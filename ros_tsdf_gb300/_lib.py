@@ -19,6 +19,7 @@ ERR_BUSY = 8
 ERR_NOT_READY = 9
 ERR_BAD_POINTS = 10
 ERR_NO_POSE = 11
+ERR_INVARIANT = 12
 
 PUB_ARRAYS = 0
 PUB_TSDF_MSG = 1
@@ -30,7 +31,7 @@ def tsdf_msg_bytes(cap: int) -> int:
 
 STATUS_NAMES = {
     0: "OK", 1: "INVALID_ARG", 2: "HEAP_FULL", 3: "PUBLISH_OVERFLOW", 4: "CUDA", 5: "CAPACITY",
-    6: "SPIN_LIMIT", 7: "HASH_FULL", 8: "BUSY", 9: "NOT_READY", 10: "BAD_POINTS", 11: "NO_POSE",
+    6: "SPIN_LIMIT", 7: "HASH_FULL", 8: "BUSY", 9: "NOT_READY", 10: "BAD_POINTS", 11: "NO_POSE", 12: "INVARIANT",
 }
 
 STAT_FIELDS = [
@@ -80,6 +81,11 @@ class MapInfo(C.Structure):
                 ("hash_entries", C.c_int64), ("hash_used", C.c_int64), ("rehashes", C.c_int64)]
 
 
+class MapCheckReport(C.Structure):
+    _fields_ = [(f, C.c_int64) for f in ("allocated", "duplicate_keys", "free_list_errors", "unfindable_keys",
+                                         "slot_mismatches", "stray_entries", "pending_entries", "nnz_mismatches")]
+
+
 # (name, restype, argtypes) of every symbol include/tsdf_c.h declares
 SIGNATURES = [
     ("tsdf_engine_create", C.c_int, [C.POINTER(EngineCfg), C.POINTER(C.c_void_p)]),
@@ -106,6 +112,7 @@ SIGNATURES = [
     ("tsdf_dump_blocks", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_free_list", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_dump_block_voxels", C.c_int, [C.c_void_p, C.c_int, C.c_int32, C.c_void_p]),
+    ("tsdf_map_check", C.c_int, [C.c_void_p, C.c_int, C.POINTER(MapCheckReport)]),
     ("tsdf_map_snapshot", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("tsdf_map_restore", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(C.c_int)]),
     ("tsdf_check_division", C.c_int, [C.c_void_p, C.c_uint64, C.c_int64, C.POINTER(C.c_int64),

@@ -28,6 +28,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/tsdf_c.h"
 #include "tsdf_internal.h"
 
@@ -44,6 +46,16 @@ constexpr long long kFlushBytes = 512ll << 20;
 
 const char* kStageNames[STAGE_COUNT] = {"init",        "ray_blocks", "alloc_order", "alloc", "ray_voxels",
                                         "route_sort", "heavy_bins",  "update",      "publish",     "gc"};
+
+// An NVTX range for the lifetime of a scope: the host side of every entry
+// point and pipeline phase shows up by name in a profiler's timeline (nvtx3 is
+// header-only; without an attached tool a range costs a few nanoseconds).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 int64_t now_ns() {
   timespec ts;
@@ -396,6 +408,7 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
 }
 
 tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout) {
+  NvtxRange nvtx_range("tsdf launch_pipeline");
   const bool timed = eng->stage_timing;
   L.timed = timed;
   if (eng->cfg.no_graphs) {
@@ -463,6 +476,7 @@ bool device_resident(const void* p, const void** dev_ptr) {
 // Validate a batch and enqueue it on lane L (asynchronous).  On success the
 // lane is busy until finish_batch.
 tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans, tsdf_scan_result* res) {
+  NvtxRange nvtx_range("tsdf start_batch");
   const tsdf_engine_cfg& c = eng->cfg;
   if (n <= 0 || n > c.max_maps) return fail(eng, TSDF_ERR_INVALID_ARG, "batch size out of range");
   BatchHdr* hdr = reinterpret_cast<BatchHdr*>(L.h_desc);
@@ -620,6 +634,7 @@ tsdf_status maybe_rehash(tsdf_engine* eng, int map_id, Lane& L);
 
 // Wait for lane L's batch and deliver its results.
 tsdf_status finish_batch(tsdf_engine* eng, Lane& L, int n, tsdf_scan_result* res) {
+  NvtxRange nvtx_range("tsdf finish_batch");
   CK(cudaEventSynchronize(L.ev_done));
   if (L.step_timed) {
     float ms = 0;
@@ -954,6 +969,7 @@ tsdf_status tsdf_engine_get_cfg(tsdf_engine* eng, tsdf_engine_cfg* out, int* sm_
 }
 
 tsdf_status tsdf_map_create(tsdf_engine* eng, const tsdf_params* p, int64_t heap_blocks, int* map_id) {
+  NvtxRange nvtx_range("tsdf_map_create");
   if (!eng || !p || !map_id) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   CK(cudaSetDevice(eng->device));
@@ -1077,6 +1093,7 @@ SnapLayout snap_layout(long long heap_blocks, long long hw) {
 }  // namespace
 
 tsdf_status tsdf_map_snapshot(tsdf_engine* eng, int map_id, void* out, int64_t cap, int64_t* bytes) {
+  NvtxRange nvtx_range("tsdf_map_snapshot");
   if (!eng || !bytes) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
@@ -1113,6 +1130,7 @@ tsdf_status tsdf_map_snapshot(tsdf_engine* eng, int map_id, void* out, int64_t c
 
 tsdf_status tsdf_map_restore(tsdf_engine* eng, const void* snapshot, int64_t bytes, int64_t heap_blocks,
                              int* map_id) {
+  NvtxRange nvtx_range("tsdf_map_restore");
   if (!eng || !snapshot || !map_id) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   CK(cudaSetDevice(eng->device));
@@ -1183,6 +1201,7 @@ tsdf_status tsdf_map_info_get(tsdf_engine* eng, int map_id, tsdf_map_info* out) 
 }
 
 tsdf_status tsdf_integrate_batch(tsdf_engine* eng, int n, const tsdf_scan* scans, tsdf_scan_result* results) {
+  NvtxRange nvtx_range("tsdf_integrate_batch");
   if (!eng || !scans || !results || n <= 0) return TSDF_ERR_INVALID_ARG;
   {
     std::unique_lock<std::recursive_mutex> lk(eng->mu);
@@ -1209,6 +1228,7 @@ tsdf_status tsdf_integrate_batch(tsdf_engine* eng, int n, const tsdf_scan* scans
 tsdf_status tsdf_integrate(tsdf_engine* eng, int map_id, const float* xyz, int64_t n_points, int stride_bytes,
                            const float origin[3], float* pub_pos, tsdf_voxel* pub_data, int64_t pub_cap,
                            int64_t* pub_count, tsdf_scan_stats* stats) {
+  NvtxRange nvtx_range("tsdf_integrate");
   if (!eng || !origin) return TSDF_ERR_INVALID_ARG;
   tsdf_scan s{};
   s.map_id = map_id;
@@ -1227,6 +1247,7 @@ tsdf_status tsdf_integrate(tsdf_engine* eng, int map_id, const float* xyz, int64
 }
 
 tsdf_status tsdf_submit(tsdf_engine* eng, const tsdf_scan* scan, tsdf_scan_result* result, uint64_t* ticket) {
+  NvtxRange nvtx_range("tsdf_submit");
   if (!eng || !scan || !result || !ticket) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   if (scan->map_id < 0 || scan->map_id >= (int)eng->maps.size() || !eng->maps[scan->map_id].live)
@@ -1254,6 +1275,7 @@ tsdf_status tsdf_poll(tsdf_engine* eng, uint64_t ticket) {
 }
 
 tsdf_status tsdf_wait(tsdf_engine* eng, uint64_t ticket, int64_t timeout_ms) {
+  NvtxRange nvtx_range("tsdf_wait");
   if (!eng) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   auto it = eng->tickets.find(ticket);
@@ -1292,6 +1314,7 @@ tsdf_status tsdf_forget(tsdf_engine* eng, uint64_t ticket) {
 tsdf_status tsdf_enumerate_blocks(tsdf_engine* eng, const tsdf_params* params, const float* xyz, int64_t n_points,
                                   int stride_bytes, const float origin[3], int32_t* kxyz, int64_t cap,
                                   int64_t* count) {
+  NvtxRange nvtx_range("tsdf_enumerate_blocks");
   if (!eng || !params || !origin || !count || n_points < 0 || (n_points > 0 && !xyz) || cap < 0 ||
       (cap > 0 && !kxyz) || stride_bytes < 12 || (stride_bytes & 3))
     return TSDF_ERR_INVALID_ARG;
@@ -1390,6 +1413,103 @@ tsdf_status tsdf_dump_free_list(tsdf_engine* eng, int map_id, int32_t* out, int6
     *block_count = mc.block_count;
   }
   return TSDF_OK;
+}
+
+namespace {
+
+// The device hash of tsdf_kernels.cu (MurmurHash3 64-bit finalizer), on the host.
+unsigned long long mix64_host(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+}  // namespace
+
+tsdf_status tsdf_map_check(tsdf_engine* eng, int map_id, tsdf_map_check_report* out) {
+  NvtxRange nvtx_range("tsdf_map_check");
+  if (!eng) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  if (map_id < 0 || map_id >= (int)eng->maps.size() || !eng->maps[map_id].live)
+    return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+  if (!map_idle(eng, map_id)) return fail(eng, TSDF_ERR_BUSY, "map has a scan in flight or queued");
+  CK(cudaSetDevice(eng->device));
+  const MapHost& m = eng->maps[map_id];
+  MapCounters mc;
+  CK(cudaMemcpy(&mc, eng->d_mctr + map_id, sizeof(mc), cudaMemcpyDeviceToHost));
+  const long long cap = m.dev.heap_cap, hw = mc.hw, base = m.dev.heap_base;
+  const int G = eng->cfg.bucket_size;
+  std::vector<unsigned long long> keys((size_t)hw);
+  std::vector<int> fl((size_t)cap), nnz((size_t)cap);
+  std::vector<HEntry> tab((size_t)m.hash_entries);
+  std::vector<float2> vox((size_t)hw * kVoxelsPerBlock);
+  if (hw > 0) {
+    CK(cudaMemcpy(keys.data(), eng->slot_key + base, 8 * hw, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(vox.data(), eng->voxels + base * kVoxelsPerBlock, sizeof(float2) * kVoxelsPerBlock * hw,
+                  cudaMemcpyDeviceToHost));
+  }
+  CK(cudaMemcpy(fl.data(), eng->free_list + base, 4 * cap, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(nnz.data(), eng->nnz + base, 4 * cap, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(tab.data(), eng->hash + m.dev.hash_base, sizeof(HEntry) * m.hash_entries, cudaMemcpyDeviceToHost));
+  tsdf_map_check_report r{};
+  std::unordered_map<unsigned long long, long long> slot_of;
+  for (long long s = 0; s < hw; ++s) {
+    if (keys[s] == kEmptyKey) continue;
+    ++r.allocated;
+    if (!slot_of.emplace(keys[s], s).second) ++r.duplicate_keys;
+  }
+  // free part + allocated slots = every slot once
+  std::vector<int> seen((size_t)cap, 0);
+  for (long long i = mc.block_count; i < cap; ++i) {
+    const int s = fl[(size_t)i];
+    if (s < 0 || s >= cap)
+      ++r.free_list_errors;
+    else
+      ++seen[(size_t)s];
+  }
+  for (long long s = 0; s < hw; ++s)
+    if (keys[s] != kEmptyKey) ++seen[(size_t)s];
+  for (long long s = 0; s < cap; ++s)
+    if (seen[(size_t)s] != 1) ++r.free_list_errors;
+  if (r.allocated != mc.block_count) ++r.free_list_errors;
+  // every allocated key found by the probe sequence at its slot
+  const unsigned mask = m.dev.hash_mask;
+  for (const auto& kv : slot_of) {
+    const unsigned long long h = mix64_host(kv.first);
+    long long found = -1;
+    bool stop = false;
+    for (unsigned p = 0; p <= mask && found < 0 && !stop; ++p) {
+      const unsigned b = (unsigned)(h + p) & mask;
+      for (int g = 0; g < G; ++g) {
+        const HEntry& e = tab[(size_t)b * G + g];
+        if (e.key == kv.first) found = (long long)b * G + g;
+        if (e.key == kEmptyKey) stop = true;
+      }
+    }
+    if (found < 0)
+      ++r.unfindable_keys;
+    else if (tab[(size_t)found].slot != (int)kv.second)
+      ++r.slot_mismatches;
+  }
+  for (const HEntry& e : tab) {
+    if (e.key == kEmptyKey || e.key == kTombKey) continue;
+    if (e.slot == kSlotPending || e.rank != kRankNone) ++r.pending_entries;
+    auto it = slot_of.find(e.key);
+    if (it == slot_of.end() || it->second != e.slot) ++r.stray_entries;
+  }
+  for (long long s = 0; s < cap; ++s) {
+    int want = 0;
+    if (s < hw && keys[s] != kEmptyKey)
+      for (int l = 0; l < kVoxelsPerBlock; ++l) want += vox[(size_t)s * kVoxelsPerBlock + l].y != 0.0f;
+    if (nnz[(size_t)s] != want) ++r.nnz_mismatches;
+  }
+  if (out) *out = r;
+  const bool ok = !r.duplicate_keys && !r.free_list_errors && !r.unfindable_keys && !r.slot_mismatches &&
+                  !r.stray_entries && !r.pending_entries && !r.nnz_mismatches;
+  return ok ? TSDF_OK : fail(eng, TSDF_ERR_INVARIANT, "map invariant violated (see the report)");
 }
 
 tsdf_status tsdf_dump_block_voxels(tsdf_engine* eng, int map_id, int32_t slot, tsdf_voxel* out512) {

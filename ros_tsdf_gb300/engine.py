@@ -298,6 +298,19 @@ class Engine:
                     "tsdf_dump_free_list")
         return out, bc.value
 
+    def check_map(self, map_id: int) -> dict:
+        """Host-side invariant check of an idle map (tsdf_map_check): distinct
+        keys, free list + allocated slots = every slot once, every key found by
+        the hash probe at its slot, no leftover pending entries, non-zero
+        counts equal to the weights.  Returns the report; raises TsdfError
+        with it when an invariant is broken."""
+        r = L.MapCheckReport()
+        st = self.lib.tsdf_map_check(self.h, int(map_id), C.byref(r))
+        rep = {f: int(getattr(r, f)) for f, _ in L.MapCheckReport._fields_}
+        if st != L.OK:
+            raise TsdfError(st, f"tsdf_map_check: {rep}")
+        return rep
+
     def dump_block_voxels(self, map_id: int, slot: int) -> np.ndarray:
         out = np.empty((512, 2), np.float32)
         self._check(self.lib.tsdf_dump_block_voxels(self.h, map_id, int(slot), out.ctypes.data),

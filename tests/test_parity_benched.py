@@ -60,6 +60,7 @@ def map_state(eng, mid):
 
 
 def check_map(eng, mid, orc, heap, T, exact_sdf=True, what=""):
+    eng.check_map(mid)  # the engine's own invariant check (raises when broken)
     kg, sg = eng.dump_blocks(mid)
     ko, so = orc.dump_blocks()
     assert np.array_equal(kg, ko) and np.array_equal(sg, so), f"{what}: block table (key -> slot) differs"

@@ -35,7 +35,9 @@ def assert_scan_equal(r, orc_out, T, what=""):
 
 
 def assert_state_equal(eng, mid, orc, heap, voxels=True):
+    rep = eng.check_map(mid)  # raises when a map invariant is broken
     kg, sg = eng.dump_blocks(mid)
+    assert rep["allocated"] == len(sg)
     ko, so = orc.dump_blocks()
     assert np.array_equal(kg, ko) and np.array_equal(sg, so), "block table (key -> slot) differs"
     fg, bcg = eng.dump_free_list(mid)
@@ -455,12 +457,14 @@ def test_snapshot_restore_continues_identically(built):
 def test_pointcloud2_records_and_tsdf_message(built):
     """PointCloud2-style records (x, y, z at byte 8 of 32-byte points, NaN
     rows for rays without a return) integrate exactly like the packed points;
-    the Tsdf message written by the publish kernel holds the same voxels as
-    the array output, with its header and trailer."""
+    the Tsdf message written by the publish kernel holds the oracle's
+    published voxels (Voxel.msg fields sdf, weight, x, y, z), with its header
+    and trailer, also when clipped at a small cap."""
     from ros_tsdf_gb300 import Engine, pointcloud2 as P, workloads as W
 
     spec = W.plain_small(seed=3, heap_blocks=1 << 13)
     src = W.ScanSource(spec)
+    orc = _oracle(spec.params, spec.heap_blocks)
     fields = [P.PointField("t", 0, P.FLOAT64), P.PointField("x", 8, P.FLOAT32), P.PointField("y", 12, P.FLOAT32),
               P.PointField("z", 16, P.FLOAT32), P.PointField("intensity", 20, P.FLOAT32)]
     with Engine(max_maps=4, pool_blocks=4 << 13, max_batch_points=1 << 16) as eng:
@@ -480,9 +484,10 @@ def test_pointcloud2_records_and_tsdf_message(built):
             cap = (1 << 16) if k < 3 else max(ra.count // 2, 1)
             msg, rc = eng.integrate_msg(c, xyz, org, pub_cap=cap)
             d = P.decode_tsdf_msg(msg)
-            kk = min(ra.count, cap)
-            assert rc.count == ra.count and d["size"] == kk and msg.size == P_bytes(kk)
-            assert np.array_equal(d["pos"], ra.pos[:kk]) and np.array_equal(d["data"], ra.data[:kk])
+            opos, odata, ocnt, _, _ = orc.integrate(xyz, org, pub_cap=cap)
+            kk = min(ocnt, cap)
+            assert rc.count == ra.count == ocnt and d["size"] == kk and msg.size == P_bytes(kk)
+            assert np.array_equal(d["pos"], opos) and np.array_equal(d["data"], odata)
             assert d["truncation_distance"] == np.float32(spec.params.truncation_distance)
             assert d["voxel_size"] == np.float32(spec.params.voxel_size)
         assert np.array_equal(eng.dump_blocks(a)[0], eng.dump_blocks(b)[0])
