@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-served", action="store_true", help="skip the tsdf_submit leg of the workload")
     ap.add_argument("--heap-blocks", type=int, default=1 << 16, help="per-map heap capacity (blocks)")
     ap.add_argument("--pub-cap", type=int, default=1 << 20)
     ap.add_argument("--json-out", default=None)
@@ -366,7 +367,8 @@ def run_ours(args, rank, world, local, pg):
 
     # ---- e2e: pinned host buffers through the C-ABI, wall clock
     if args.no_e2e:
-        return dict(value=value, ms_per_step=ms_per_step, e2e=None, plain=None, stats=mstats, stages=stage_acc,
+        return dict(value=value, ms_per_step=ms_per_step, e2e=None, plain=None, served=None, stats=mstats,
+                    stages=stage_acc,
                     clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
                     dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
     eng2 = new_engine()
@@ -400,7 +402,7 @@ def run_ours(args, rank, world, local, pg):
             e2e_t += dt
             h2d += sum(scans[m][k][0].nbytes for m in range(len(specs)))
             d2h += sum(min(s["published"], cap) * 20 + 18 * 8 for s in st)
-    eng2.close()
+    eng2.close()  # the pinned buffers outlive it (the served leg below reuses them)
     e2e_t = max_over_ranks(pg, e2e_t)
     e2e = {"value": total_pts / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
            "d2h_bytes_per_step": int(d2h / args.steps), "ms_per_step": e2e_t * 1000.0 / args.steps,
@@ -427,9 +429,50 @@ def run_ours(args, rank, world, local, pg):
         plain = {"value": total_pts / tp, "unit": UNIT, "ms_per_step": tp * 1000.0 / args.steps,
                  "path": "tsdf_integrate one scan per call, pageable host in/out"}
 
-    return dict(value=value, ms_per_step=ms_per_step, e2e=e2e, plain=plain, stats=mstats, stages=stage_acc,
-                clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
-                dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
+    # ---- served: the same scans as requests through tsdf_submit (scheduler
+    # thread, continuous batching, two lanes), pinned host buffers; each step's
+    # 32 requests are queued at once and the step ends when the last completes
+    served = None
+    if not args.no_served:
+        eng4 = new_engine(lanes=2)
+        sm = [eng4.create_map(s.params, s.heap_blocks) for s in specs]
+        ts = 0.0
+        barrier(pg)
+        for k in range(n_steps):
+            reqs = []
+            t0 = time.perf_counter()
+            for m in range(len(specs)):
+                sc = L.Scan()
+                rs = L.ScanResult()
+                sc.map_id = sm[m]
+                sc.stride_bytes = 12
+                sc.n_points = scans[m][k][0].shape[0]
+                sc.xyz = pin_in[m][k].ctypes.data
+                sc.origin[:] = [float(v) for v in scans[m][k][1]]
+                rs.pub_pos = pin_pos[m].ctypes.data
+                rs.pub_data = pin_dat[m].ctypes.data
+                rs.pub_cap = cap
+                tk = C.c_uint64()
+                st = eng4.lib.tsdf_submit(eng4.h, C.byref(sc), C.byref(rs), C.byref(tk))
+                if st != 0:
+                    raise RuntimeError(f"tsdf_submit: {st} {eng4.lib.tsdf_last_error(eng4.h)}")
+                reqs.append((tk.value, sc, rs))
+            for tk, _, _ in reqs:
+                st = eng4.lib.tsdf_wait(eng4.h, tk, -1)
+                if st not in (0, 2, 3, 10):
+                    raise RuntimeError(f"tsdf_wait: {st}")
+                eng4.lib.tsdf_forget(eng4.h, tk)
+            dt = time.perf_counter() - t0
+            if k >= args.warmup:
+                ts += dt
+        eng4.close()
+        ts = max_over_ranks(pg, ts)
+        served = {"value": total_pts / ts, "unit": UNIT, "ms_per_step": ts * 1000.0 / args.steps,
+                  "path": "tsdf_submit + tsdf_wait, the 32 maps' scans of a step queued at once, pinned host in/out"}
+
+    return dict(value=value, ms_per_step=ms_per_step, e2e=e2e, plain=plain, served=served, stats=mstats,
+                stages=stage_acc, clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans,
+                timed_pts=timed_pts, dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
 
 
 def algorithmic_bytes(s: dict) -> dict:
@@ -576,35 +619,46 @@ def stage_traffic(stage: str, workload: str, stats: dict):
 def run_serving(args, local: int) -> dict:
     """The serving loop: 64 clients with device-resident maps,
     Poisson arrivals at 10 Hz each, lidar and voxel size drawn per client.
-    The same trace is replayed through the served engine (scheduler thread,
-    continuous batching, two lanes) and through the plain path (one
-    synchronous call per scan), each on a fresh engine."""
+    Every request integrates the client's next pose (continuous trajectories:
+    warm-up, timed trace and capacity trace take consecutive stretches), so
+    blocks are allocated and collected throughout.  The same requests are
+    replayed through the served engine (scheduler thread, continuous
+    batching, two lanes) and through the plain path (one synchronous call per
+    scan), each on a fresh engine."""
     from ros_tsdf_gb300 import Engine, serving as S
     from ros_tsdf_gb300 import workloads as W
 
     heap = 1 << 18
     specs = W.serving64(64, heap_blocks=heap)
-    n_scans = 6
-    trace = S.poisson_trace(len(specs), 10.0, args.serving_s, n_scans, seed=77)
-    warm = S.poisson_trace(len(specs), 10.0, 0.3, n_scans, seed=78)
+    n = len(specs)
+    warm = S.poisson_trace(n, 10.0, 0.3, seed=78)
+    trace = S.poisson_trace(n, 10.0, args.serving_s, seed=77, first_scan=S.scans_needed(n, warm))
+    cap_trace = S.poisson_trace(n, 10.0, max(0.5, args.serving_s / 2), seed=79,
+                                first_scan=S.scans_needed(n, warm, trace))
+    need = S.scans_needed(n, warm, trace, cap_trace)
     out = {"workload": f"serving64: 64 clients, Poisson 10 Hz each, {args.serving_s:g} s trace "
                        f"({len(trace)} scans), lidar from {{16x64, 32x512, 64x1024, 128x2048}}, voxel size from "
-                       "{0.05, 0.1, 0.2, 0.5} m, T = 4 voxel sizes, each client cycling through 6 seeded scans, "
-                       "publish cap 400000 voxels per scan, pinned host buffers"}
+                       "{0.05, 0.1, 0.2, 0.5} m, T = 4 voxel sizes, every request a new pose of its client's "
+                       "trajectory, publish capped at 400000 voxels per scan (the reference's "
+                       "PUBLISH_VOXELS_MAX_SIZE), pinned host buffers",
+           "capacity_trace": f"the next {len(cap_trace)} poses, every request queued at once"}
+    inputs = None
     for mode in ("served", "plain"):
-        eng = Engine(device=local, max_maps=64, pool_blocks=heap * len(specs) + 64, max_batch_points=1 << 20,
+        eng = Engine(device=local, max_maps=64, pool_blocks=heap * n + 64, max_batch_points=1 << 20,
                      max_publish=1 << 20, lanes=2, bucket_size=args.bucket_size, ray_chunk=args.ray_chunk,
                      ray_threads=args.ray_threads, max_routes=max(8, max(s.params.routes() for s in specs)))
-        rig = S.ServingRig(eng, specs, n_scans, pub_cap=400000)
+        if inputs is None:
+            inputs = S.prepare_inputs(eng, specs, need)
+        rig = S.ServingRig(eng, specs, need, pub_cap=400000, inputs=inputs)
         out["clients_admitted"] = rig.admitted
         if mode == "served":
             rig.run_served(warm)
             out["served"] = rig.run_served(trace)
-            out["served_capacity"] = rig.run_served(trace, at_once=True)
+            out["served_capacity"] = rig.run_served(cap_trace, at_once=True)
         else:
             rig.run_plain(warm)
             out["plain"] = rig.run_plain(trace)
-            out["plain_capacity"] = rig.run_plain(trace, at_once=True)
+            out["plain_capacity"] = rig.run_plain(cap_trace, at_once=True)
         del rig
         eng.close()
     # at 10 Hz per client both paths keep up with the offered load; the
@@ -656,7 +710,10 @@ def result_line(args, r: dict, world: int, tuned, peak: float, peak_kind: str) -
                               f"{min(args.steps, 5)} further steps with events around every stage")},
         "launch": tuned or {"bucket_size": args.bucket_size, "ray_chunk": args.ray_chunk,
                             "ray_threads": args.ray_threads, "source": "command line"},
-        "e2e": r["e2e"], "plain": r["plain"],
+        "e2e": r["e2e"], "plain": r["plain"], "served": r.get("served"),
+        "e2e_vs_plain": (r["e2e"]["value"] / r["plain"]["value"]) if r.get("e2e") and r.get("plain") else None,
+        "served_vs_plain": (r["served"]["value"] / r["plain"]["value"]) if r.get("served") and r.get("plain")
+        else None,
         "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": dom_bytes, "traffic": traffic,

@@ -31,34 +31,62 @@ class Request:
     t_arrival: float  # seconds from the start of the trace
 
 
-def poisson_trace(n_clients: int, rate_hz: float, duration_s: float, scans_per_client: int,
-                  seed: int = 77) -> list[Request]:
+def poisson_trace(n_clients: int, rate_hz: float, duration_s: float, scans_per_client: int | None = None,
+                  seed: int = 77, first_scan=None) -> list[Request]:
     """Independent Poisson arrivals per client (exponential gaps, mean
-    1/rate_hz), merged and sorted by time; each client cycles through its
-    prepared scans in order."""
+    1/rate_hz), merged and sorted by time.  Each client's requests take its
+    scans in trajectory order, starting at first_scan[client] (default 0):
+    every request integrates a new pose.  With scans_per_client the index
+    wraps around that many prepared scans instead."""
     rng = np.random.default_rng(seed)
     reqs = []
     for c in range(n_clients):
         t = float(rng.exponential(1.0 / rate_hz))
-        k = 0
+        k = int(first_scan[c]) if first_scan is not None else 0
         while t < duration_s:
-            reqs.append(Request(c, k % scans_per_client, t))
+            reqs.append(Request(c, k % scans_per_client if scans_per_client else k, t))
             k += 1
             t += float(rng.exponential(1.0 / rate_hz))
     reqs.sort(key=lambda r: (r.t_arrival, r.client))
     return reqs
 
 
+def scans_needed(n_clients: int, *traces: list[Request]) -> list[int]:
+    """Per client, one more than the highest scan index the traces use."""
+    need = [0] * n_clients
+    for tr in traces:
+        for r in tr:
+            need[r.client] = max(need[r.client], r.scan + 1)
+    return need
+
+
 def percentile(x, q):
     return float(np.percentile(np.asarray(x, np.float64), q)) if len(x) else float("nan")
+
+
+def prepare_inputs(engine: Engine, specs: list[MapSpec], scans_per_client) -> list:
+    """Per client, its first scans_per_client[c] scans in pinned host memory."""
+    per_client = scans_per_client if isinstance(scans_per_client, (list, tuple)) else \
+        [scans_per_client] * len(specs)
+    out = []
+    for c, s in enumerate(specs):
+        row = []
+        src = ScanSource(s)
+        for k in range(per_client[c]):
+            xyz, org = src.scan(k)
+            p = engine.pinned_empty(xyz.shape, np.float32)
+            p[:] = xyz
+            row.append((p, org))
+        out.append(row)
+    return out
 
 
 class ServingRig:
     """Clients, their maps (admitted while the block pool has room) and their
     pinned input scans and output slots."""
 
-    def __init__(self, engine: Engine, specs: list[MapSpec], scans_per_client: int, pub_cap: int,
-                 slots_per_client: int = 3):
+    def __init__(self, engine: Engine, specs: list[MapSpec], scans_per_client, pub_cap: int,
+                 slots_per_client: int = 3, inputs=None):
         self.eng = engine
         self.specs = specs
         self.pub_cap = pub_cap
@@ -72,16 +100,10 @@ class ServingRig:
                     raise
                 mid = -1
             self.maps.append(mid)
-        for c, s in enumerate(specs):
-            row = []
-            if self.maps[c] >= 0:
-                src = ScanSource(s)
-                for k in range(scans_per_client):
-                    xyz, org = src.scan(k)
-                    p = engine.pinned_empty(xyz.shape, np.float32)
-                    p[:] = xyz
-                    row.append((p, org))
-            self.inputs.append(row)
+        if inputs is not None:  # prepared by prepare_inputs (pinned buffers outlive engines)
+            self.inputs = inputs
+        else:
+            self.inputs = prepare_inputs(engine, specs, scans_per_client)
         self.slots = slots_per_client
         self.out_pos = [[engine.pinned_empty((pub_cap, 3), np.float32) for _ in range(slots_per_client)]
                         if m >= 0 else [] for m in self.maps]
@@ -158,7 +180,9 @@ class ServingRig:
         return {"requests": len(pending), "points": pts, "points_per_s": pts / span if span > 0 else 0.0,
                 "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99), "max_ms": max(lat) if lat else 0.0,
                 "p99_ms_by_rays": {str(k): percentile(v, 99) for k, v in sorted(lat_by_rays.items())},
-                "submit_max_late_ms": late, "statuses": statuses, "span_s": span}
+                "submit_max_late_ms": late, "statuses": statuses,
+                "publish_overflow_share": statuses.get(L.WARN_PUBLISH_OVERFLOW, 0) / len(lat) if lat else 0.0,
+                "span_s": span}
 
     def run_plain(self, trace: list[Request], at_once: bool = False) -> dict:
         """One synchronous tsdf_integrate per request, in arrival order, on
@@ -168,6 +192,7 @@ class ServingRig:
         lib, h = self.eng.lib, self.eng.h
         trace = [r for r in trace if self.maps[r.client] >= 0]
         lat, lat_by_rays, pts = [], {}, 0
+        statuses = {}
         cnt = C.c_int64()
         stats = L.ScanStats()
         t0 = time.monotonic_ns()
@@ -183,6 +208,7 @@ class ServingRig:
                                     self.pub_cap, C.byref(cnt), C.byref(stats))
             if st not in (L.OK, L.ERR_HEAP_FULL, L.WARN_PUBLISH_OVERFLOW, L.ERR_BAD_POINTS):
                 raise TsdfError(st, "tsdf_integrate")
+            statuses[int(st)] = statuses.get(int(st), 0) + 1
             ms = (time.monotonic_ns() - due) / 1e6
             lat.append(ms)
             rays = self.specs[r.client].lidar.channels * self.specs[r.client].lidar.azimuths
@@ -192,4 +218,5 @@ class ServingRig:
         return {"requests": len(trace), "points": pts, "points_per_s": pts / span if span > 0 else 0.0,
                 "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99), "max_ms": max(lat) if lat else 0.0,
                 "p99_ms_by_rays": {str(k): percentile(v, 99) for k, v in sorted(lat_by_rays.items())},
-                "span_s": span}
+                "statuses": statuses, "publish_overflow_share": statuses.get(L.WARN_PUBLISH_OVERFLOW, 0) / len(lat)
+                if lat else 0.0, "span_s": span}
