@@ -100,8 +100,8 @@ typedef struct tsdf_engine_cfg {
                                reference's update rule.  1: the long chains
                                of the grid-wide list (voxels with more than
                                128 updates in a step) as one composition of
-                               their updates' affine maps in double, rounded
-                               once: weights, block sets and publish sets stay
+                               their updates' affine maps, computed in float
+                               by a warp: weights, block sets and publish sets stay
                                exact, sdf within 1e-5 x truncation distance   */
 } tsdf_engine_cfg;
 

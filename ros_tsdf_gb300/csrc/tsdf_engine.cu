@@ -341,6 +341,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.tile_sums3, max_tiles_scan + 1, tr));
   TRY(dalloc(eng, &x.seg_start, rec_cap, tr));
   TRY(dalloc(eng, &x.seg_item, rec_cap, tr));
+  TRY(dalloc(eng, &x.seg_desc, rec_cap, tr));
   TRY(dalloc(eng, &x.enum_cnt, enum_cap, tr));
   TRY(dalloc(eng, &x.enum_gc, enum_cap, tr));
   TRY(dalloc(eng, &x.pub_prefix, enum_cap, tr));

@@ -191,6 +191,7 @@ struct Ctx {
   int* tile_sums3;               // gc-flag tile sums (likewise)
   int* seg_start;
   int* seg_item;                 // batch item (map scan) of each segment
+  int4* seg_desc;                // per segment {first record, end record, physical slot, max_weight bits}
   int* enum_cnt;                 // publish counts per enumerated slot
   int* enum_gc;                  // gc flags per enumerated slot
   int* pub_prefix;

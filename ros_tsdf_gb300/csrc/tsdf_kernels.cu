@@ -1103,11 +1103,16 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
   const unsigned* rv = c.rec_val[rec_sel];
+  const unsigned* rk = c.rec_key[rec_sel];
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nseg;
        j += (long long)gridDim.x * blockDim.x) {
     const long long b0 = c.seg_start[j];
     const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
-    c.seg_item[j] = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+    const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+    c.seg_item[j] = item;
+    // what the update kernels need first, in one 16-byte load
+    c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
+                              __float_as_int(c.maps[c.items[item].map].maxw));
     if (b1 - b0 > UPD_T) {
       unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_heavy), 1ull);
       c.heavy[k] = (int)j;
@@ -1597,68 +1602,92 @@ __device__ __forceinline__ float2 warp_chain(float sdf, float W, const float4* b
   return make_float2(sdf, W);
 }
 
+// Ordered warp reduction of affine maps s -> a s + b: lane l holds the
+// composition of the updates before those of lane l + 1; lane 0 ends with the
+// composition of all 32 (later maps applied after earlier ones).
+__device__ __forceinline__ void warp_compose(float& a, float& b, int lane) {
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const float al = __shfl_down_sync(kFull, a, off);
+    const float bl = __shfl_down_sync(kFull, b, off);
+    if ((lane & (2 * off - 1)) == 0) {
+      b = __fmaf_rn(al, b, bl);
+      a = __fmul_rn(al, a);
+    }
+  }
+}
+
 // A voxel's chain as one composition of affine maps (engine sdf_mode 1).  The
 // update rule (tsdf_handler.cu:648-654) is, in exact arithmetic,
 //   sdf' = a sdf + b,  a = W / W',  b = RN(w d) / W',  W' = RN(W + w),
-// and composing maps is associative, so the 32 lanes each compose a
-// contiguous part of the chain in double (earlier updates first) and an
-// ordered warp reduction composes the parts; the result is applied to the
-// voxel's sdf and rounded to float once.  The weights are exact: while the
-// voxel is below max_weight lane 0 runs the reference's serial float weight
-// chain (W' = RN(W + w), W = min(W', max)) and writes every W and W' into
-// the chain's bins; from max_weight on W = max and W' = RN(max + w), which
-// k_heavy_place precomputed.  The sdf then differs from the serial float
-// chain by that chain's own rounding only (contractive, |a| <= 1): within
-// 1e-5 T on every tested workload.  The reciprocal 1/W' is the float
-// reciprocal refined by one Newton step in double (relative error about
-// 2^-46).  Returns {sdf, W}, valid in lane 0.
-__device__ __forceinline__ float2 warp_chain_scan(float sdf0, float W0, float4* bins, int n, float maxw, int lane) {
-  int p = 0;  // bins [0, p) hold this chain's W and W' below max_weight
-  float w_end = W0;
-  if (W0 != maxw) {
+// and composing maps is associative.  The weights stay exact: while the voxel
+// is below max_weight the chain goes 32 updates at a time, lane 0 running the
+// reference's serial float weight chain (W' = RN(W + w), W = min(W', max))
+// over the batch from shared memory, every lane then taking its update's map
+// and a warp reduction composing the batch.  From max_weight on every
+// W = max and W' = RN(max + w), which k_heavy_place precomputed, so the 32
+// lanes each compose a contiguous part of the rest and one reduction composes
+// them.  The composition is in float (GB300's FP64 rate made a double
+// composition slower than the serial chain): every map is contractive
+// (0 <= a < 1), so its rounding stays of the order of the serial chain's own;
+// on 13,400-update chains the two differ by 3e-7 T, and the tests assert
+// 1e-5 T on every workload.  tile: 32 float2 of this warp's shared memory.
+// Returns {sdf, W}, valid in lane 0.
+__device__ __forceinline__ float2 warp_chain_scan(float sdf0, float W0, const float4* bins, int n, float maxw,
+                                                  int lane, float2* tile) {
+  float A = 1.0f, B = 0.0f;  // the composition so far (lane 0)
+  float W = W0;              // the weight chain (lane 0)
+  int base = 0;
+  bool sat = W0 == maxw;
+  while (!sat && base < n) {
+    const int m = min(32, n - base);
+    const float4 x = lane < m ? bins[base + lane] : make_float4(0.f, 1.f, 1.f, 0.f);
+    tile[lane].x = x.w;
+    __syncwarp();
     if (lane == 0) {
-      float W = W0;
-      int i = 0;
-      for (; i < n && W != maxw; ++i) {
-        float4 x = bins[i];
-        const float nw = fadd(W, x.w);
-        x.y = nw;
-        x.z = W;
-        bins[i] = x;
+      for (int k = 0; k < m; ++k) {
+        const float nw = fadd(W, tile[k].x);
+        tile[k] = make_float2(W, nw);
         W = fminf(nw, maxw);
       }
-      p = i;
-      w_end = W;
     }
-    p = __shfl_sync(kFull, p, 0);
-    w_end = __shfl_sync(kFull, w_end, 0);
-    __syncwarp();  // lane 0's bin writes before the other lanes read them
+    __syncwarp();
+    float a = 1.0f, b = 0.0f;
+    if (lane < m) {
+      const float2 ww = tile[lane];
+      const float r = __frcp_rn(ww.y);
+      a = __fmul_rn(ww.x, r);
+      b = __fmul_rn(x.x, r);
+    }
+    warp_compose(a, b, lane);
+    if (lane == 0) {
+      B = __fmaf_rn(a, B, b);
+      A = __fmul_rn(a, A);
+    }
+    sat = __shfl_sync(kFull, W == maxw, 0);
+    base += m;
+    __syncwarp();
   }
-  const int chunk = (n + 31) >> 5;
-  const int lo = min(n, lane * chunk), hi = min(n, lo + chunk);
-  double A = 1.0, B = 0.0;
-  for (int i = lo; i < hi; ++i) {
-    const float4 x = bins[i];
-    const double wp = (double)x.y;
-    const double wi = i < p ? (double)x.z : (double)maxw;
-    const double r0 = (double)__frcp_rn(x.y);
-    const double r = r0 * __fma_rn(-wp, r0, 2.0);
-    const double a = wi * r;
-    B = __fma_rn(a, B, (double)x.x * r);
-    A = a * A;
-  }
-  // ordered reduction: lane l holds the maps of updates before lane l+off's
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const double al = __shfl_down_sync(kFull, A, off);
-    const double bl = __shfl_down_sync(kFull, B, off);
-    if ((lane & (2 * off - 1)) == 0) {
-      B = __fma_rn(al, B, bl);
-      A = al * A;
+  if (base < n) {
+    const int rest = n - base;
+    const int chunk = (rest + 31) >> 5;
+    const int lo = base + min(rest, lane * chunk), hi = min(n, lo + chunk);
+    float a = 1.0f, b = 0.0f;
+    for (int i = lo; i < hi; ++i) {
+      const float4 x = bins[i];
+      const float r = __frcp_rn(x.y);
+      const float ai = __fmul_rn(maxw, r);
+      b = __fmaf_rn(ai, b, __fmul_rn(x.x, r));
+      a = __fmul_rn(ai, a);
+    }
+    warp_compose(a, b, lane);
+    if (lane == 0) {
+      B = __fmaf_rn(a, B, b);
+      A = __fmul_rn(a, A);
+      W = maxw;
     }
   }
-  const float sdf = __double2float_rn(__fma_rn(A, (double)sdf0, B));
-  return make_float2(sdf, p < n ? maxw : w_end);
+  return make_float2(__fmaf_rn(A, sdf0, B), W);
 }
 
 __device__ __forceinline__ void prefetch_l1(const void* p) {
@@ -1681,7 +1710,8 @@ __device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32],
     float2* v = c.voxels + (long long)hc.phys * kVoxelsPerBlock + hc.local;
     const float2 v0 = *v;
     if (c.sdf_scan) {
-      const float2 r = warp_chain_scan(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, lane);
+      const float2 r = warp_chain_scan(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, lane,
+                                       reinterpret_cast<float2*>(tile[0]));
       if (lane == 0) *v = r;
       continue;
     }
@@ -1742,12 +1772,9 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
   __shared__ unsigned long long s_base;
   unsigned short* s_bin = reinterpret_cast<unsigned short*>(s_bin_run);
   int* s_run = s_bin_run;
-  const BatchHdr h = *c.hdr;
   const int t = threadIdx.x;
   const long long nseg = c.ctr->n_seg;
-  const long long nrec = c.ctr->n_rec_live;
   const long long nheavy = c.ctr->n_heavy;
-  const unsigned* rk = c.rec_key[rec_sel];
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned lt_bits = (1u << (t & 31)) - 1u;
   // The queue item after the current one is claimed when the current one
@@ -1771,16 +1798,16 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
       heavy = true;
     } else {
       sj = q - nheavy;
-      const long long e1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
-      if (e1 - c.seg_start[sj] > UPD_T) continue;  // already done on the heavy path
       heavy = false;
     }
-    const long long b0 = c.seg_start[sj];
-    const long long b1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
-    const long long phys = h.key_lo + rk[b0];
+    // the segment's bounds, block and max_weight in one load (k_seg_classify)
+    const int4 desc = c.seg_desc[sj];
     const int item = c.seg_item[sj];
-    const MapDev& m = c.maps[c.items[item].map];
-    const float maxw = m.maxw;
+    if (!heavy && desc.y - desc.x > UPD_T) continue;  // already done on the heavy path
+    const long long b0 = desc.x;
+    const long long b1 = desc.y;
+    const long long phys = desc.z;
+    const float maxw = __int_as_float(desc.w);
     // Only the voxels that get updates are read and written: each is owned by
     // thread l % UPD_T, which loads it once its update count is known and
     // stores it after its chain.  The block's non-zero count moves by the
@@ -1793,8 +1820,10 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
     long long nb0 = -1, nb1 = 0;
     if (qn < nqueue && !(qn < nplanned && c.hfit[qn])) {
       const long long sjn = qn < nheavy ? (long long)c.heavy[qn] : qn - nheavy;
-      nb0 = c.seg_start[sjn];
-      nb1 = (sjn + 1 < nseg) ? c.seg_start[sjn + 1] : nrec;
+      const int4 nd = c.seg_desc[sjn];
+      prefetch_l1(c.seg_item + sjn);
+      nb0 = nd.x;
+      nb1 = nd.y;
     }
     unsigned n_upd = 0;
     bool passes = heavy;
