@@ -112,6 +112,7 @@ struct LaneCounters {
   unsigned long long q_blocks;   // work queue heads
   unsigned long long q_voxels;
   unsigned long long q_update;
+  unsigned long long q_update_warp;  // work queue of the light-segment warps
   unsigned long long q_pubwrite;
   unsigned long long q_hot;      // work queue of the hot-chain kernel
   long long n_new;        // new keys appended

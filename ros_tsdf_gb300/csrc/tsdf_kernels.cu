@@ -25,9 +25,10 @@
 //                voxels with more than 128 updates go on the hot list
 //   update       three streams: k_hot_chains (one warp per voxel with more
 //                than 128 updates), k_heavy_update (binned heavy segments,
-//                one lane per voxel) and k_update (light segments: one CTA
-//                per block, voxels staged in shared memory, per-voxel record
-//                masks give each update its place in point order).
+//                one lane per voxel) and k_update_warp (light segments: one
+//                warp per block, its records in point order, a record's
+//                updates in parallel, one lane per voxel); k_update takes the
+//                heavy segments beyond the binning capacity in passes.
 //                (tsdf_handler.cu:604-665)
 //   publish      in-radius blocks counted, prefix-summed, compacted to the
 //                output arrays or a serialized Tsdf message; for pinned host
@@ -1076,19 +1077,6 @@ __device__ __forceinline__ void zero_masks(unsigned* m, int t) {
   for (int i = 0; i < (UPD_T / 32) * kVoxelsPerBlock / 4 / UPD_T; ++i) v[t + i * UPD_T] = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// Update counts of voxels 4t..4t+3: popcounts of their four mask words, read
-// as one 16-byte load per word.
-__device__ __forceinline__ void mask_counts(const unsigned* m, int t, int a[4]) {
-  a[0] = a[1] = a[2] = a[3] = 0;
-#pragma unroll
-  for (int w = 0; w < UPD_T / 32; ++w) {
-    const uint4 x = reinterpret_cast<const uint4*>(m + w * kVoxelsPerBlock)[t];
-    a[0] += __popc(x.x);
-    a[1] += __popc(x.y);
-    a[2] += __popc(x.z);
-    a[3] += __popc(x.w);
-  }
-}
 
 
 // Per segment: its batch item (the scan of the entry of its first record) and,
@@ -1438,23 +1426,20 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
 }
 
 // ----------------------------------------------------------------------------
-// update: one CTA per block touched (updateVoxelsCuda, tsdf_handler.cu:
-// 604-665).  The block's 512 voxels are staged in shared memory with 16-byte
-// loads/stores.  Its routing records (ascending point index) are taken 128 at
-// a time; every voxel gets a 128-bit mask of the records that update it, an
-// entry's rank in its voxel's bin is a popcount of the mask below it, so each
-// bin lists its updates in ascending point order and its owner thread applies
-// them sequentially: the reference's update rule, in a fixed order.  The
-// apply_chain helper below is that rule over a bin in global memory (the
-// pass-based path).
+// update (updateVoxelsCuda, tsdf_handler.cu:604-665): every voxel's updates
+// in ascending point index, the order the reference's rule has when run
+// sequentially.
 //
-// Segments longer than one chunk (a block that many points update, e.g. the
-// blocks around a sensor standing inside an object) are binned per voxel by
-// the multi-CTA counting sort of the routing stage and updated by
+// Light segments (up to 128 routing records) run in k_update_warp, a warp per
+// block.  Segments longer than that (a block that many points update, e.g.
+// the blocks around a sensor standing inside an object) are binned per voxel
+// by the multi-CTA counting sort of the routing stage and updated by
 // k_heavy_update and k_hot_chains.  Only heavy segments beyond that sort's
-// capacity stay here, in three passes: per-voxel counts over all records,
-// ordered placement of every update into per-voxel bins in global scratch
-// (mask popcount + running per-voxel cursor), then one chain per voxel.
+// capacity go to k_update, in three passes: per-voxel counts over all
+// records, ordered placement of every update into per-voxel bins in global
+// scratch (record masks: an entry's rank among the chunk's updates of its
+// voxel is a popcount of the mask below it, plus a running per-voxel
+// cursor), then one chain per voxel (apply_chain, below).
 
 __device__ __forceinline__ float apply_chain(float* sdf_io, float w, const float* d, int n, float maxw) {
   float sdf = *sdf_io;
@@ -1727,10 +1712,6 @@ __device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32],
   }
 }
 
-// A light segment's update entries, compacted (bounds the shared memory, so
-// more CTAs fit on an SM); a segment with more goes to the pass-based path.
-constexpr int kLightEntries = 1024;
-
 // Load the up to 31 entries of one routing record, eight in flight at a time,
 // and call f(k, entry) for each.
 template <typename F>
@@ -1759,148 +1740,46 @@ __global__ void __launch_bounds__(128) k_hot_chains(Ctx c) {
   run_hot_chains(c, tile, t & 31);
 }
 
+// Heavy segments the counting sort had no room for (rare): one CTA each, in
+// passes over 128-record chunks.  Pass 0 counts every voxel's updates over
+// all records; pass 1 places each update into its voxel's bin in global
+// scratch in point order (record masks: a record's rank among the chunk's
+// records updating the voxel is a popcount of the mask below it, plus the
+// earlier chunks' counts); pass 2 runs one chain per voxel.  Only the touched
+// voxels are read and written, and the block's non-zero count moves by the
+// touched voxels whose weight left zero.
 __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
   // record bit masks per voxel, word-major (word w covers records 32w..32w+31)
   // so that 16-byte accesses of four consecutive voxels hit distinct banks
   __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];
-  __shared__ float s_d[kLightEntries];
-  __shared__ unsigned short s_l[kLightEntries];
-  __shared__ int s_bin_run[kVoxelsPerBlock];  // light path: bins (ushort); pass-based path: per-voxel cursors
+  __shared__ int s_run[kVoxelsPerBlock];  // per-voxel cursors over the chunks
   __shared__ int s_off[kVoxelsPerBlock + 1];
   __shared__ int s_warp[32];
   __shared__ long long s_seg;
   __shared__ unsigned long long s_base;
-  unsigned short* s_bin = reinterpret_cast<unsigned short*>(s_bin_run);
-  int* s_run = s_bin_run;
   const int t = threadIdx.x;
-  const long long nseg = c.ctr->n_seg;
   const long long nheavy = c.ctr->n_heavy;
+  const long long nplanned = c.ctr->n_hplanned;
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned lt_bits = (1u << (t & 31)) - 1u;
-  // The queue item after the current one is claimed when the current one
-  // starts; its segment bounds, block and records are fetched during the
-  // current segment's phases (prefetch only: no registers held), so the next
-  // iteration finds them in L1 instead of waiting on a chain of dependent
-  // global loads.
-  const long long nqueue = nheavy + nseg;
-  const long long nplanned = c.ctr->n_hplanned;
-  if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
-  __syncthreads();
-  long long q = s_seg;
-  __syncthreads();
-  for (; q < nqueue; __syncthreads(), q = s_seg, __syncthreads()) {
+  for (;;) {
     if (t == 0) s_seg = (long long)atomicAdd(&c.ctr->q_update, 1ull);
-    long long sj;
-    bool heavy;
-    if (q < nheavy) {
-      if (q < nplanned && c.hfit[q]) continue;  // k_heavy_update's
-      sj = c.heavy[q];
-      heavy = true;
-    } else {
-      sj = q - nheavy;
-      heavy = false;
-    }
-    // the segment's bounds, block and max_weight in one load (k_seg_classify)
+    __syncthreads();
+    const long long q = s_seg;
+    __syncthreads();
+    if (q >= nheavy) break;
+    if (q < nplanned && c.hfit[q]) continue;  // k_heavy_update's
+    const long long sj = c.heavy[q];
     const int4 desc = c.seg_desc[sj];
     const int item = c.seg_item[sj];
-    if (!heavy && desc.y - desc.x > UPD_T) continue;  // already done on the heavy path
     const long long b0 = desc.x;
     const long long b1 = desc.y;
     const long long phys = desc.z;
     const float maxw = __int_as_float(desc.w);
-    // Only the voxels that get updates are read and written: each is owned by
-    // thread l % UPD_T, which loads it once its update count is known and
-    // stores it after its chain.  The block's non-zero count moves by the
-    // owned voxels whose weight left zero (weights never return to zero).
     float2* gv2 = c.voxels + phys * kVoxelsPerBlock;
     int nz_delta = 0, touched = 0;
-    __syncthreads();  // s_seg's next value is read below
-    // next item: segment bounds now, its records further down
-    const long long qn = s_seg;
-    long long nb0 = -1, nb1 = 0;
-    if (qn < nqueue && !(qn < nplanned && c.hfit[qn])) {
-      const long long sjn = qn < nheavy ? (long long)c.heavy[qn] : qn - nheavy;
-      const int4 nd = c.seg_desc[sjn];
-      prefetch_l1(c.seg_item + sjn);
-      nb0 = nd.x;
-      nb1 = nd.y;
-    }
     unsigned n_upd = 0;
-    bool passes = heavy;
-    if (!heavy) {
-      // ---- light path: the whole segment in one chunk, its entries
-      // compacted in shared memory at this record's offset
-      zero_masks(&s_mask[0][0], t);
-      int cnt = 0;
-      unsigned ebase = 0;
-      if (b0 + t < b1) {
-        const unsigned v = rv[b0 + t];
-        cnt = (int)(v & 31u);
-        ebase = v >> 5;
-      }
-      int etot;
-      const int eoff = block_excl_scan(cnt, s_warp, &etot);  // its barriers also close the mask zeroing
-      if (etot > kLightEntries) {
-        passes = true;
-      } else {
-        for_record_entries(c.entries + ebase, cnt, [&](int k, uint2 x) {
-          s_d[eoff + k] = __uint_as_float(x.x);
-          s_l[eoff + k] = (unsigned short)x.y;
-          if (x.y != kBadLocal) {
-            atomicOr(&s_mask[t >> 5][x.y], 1u << (t & 31));
-            ++n_upd;
-          }
-        });
-        __syncthreads();
-        unsigned nrv = 0u;
-        if (nb0 >= 0 && nb0 + t < nb1) nrv = rv[nb0 + t];
-        {
-          int a[4];
-          mask_counts(&s_mask[0][0], t, a);
-          int tot;
-          int ex = block_excl_scan(a[0] + a[1] + a[2] + a[3], s_warp, &tot);
-          s_off[4 * t] = ex;
-          s_off[4 * t + 1] = ex + a[0];
-          s_off[4 * t + 2] = ex + a[0] + a[1];
-          s_off[4 * t + 3] = ex + a[0] + a[1] + a[2];
-          if (t == 0) s_off[kVoxelsPerBlock] = tot;
-        }
-        __syncthreads();
-        // the owned voxels with updates, loaded now: the rank phase hides the latency
-        float2 ov[kVoxelsPerBlock / UPD_T];
-#pragma unroll
-        for (int j = 0; j < kVoxelsPerBlock / UPD_T; ++j) {
-          const int l = t + UPD_T * j;
-          ov[j] = s_off[l + 1] > s_off[l] ? gv2[l] : make_float2(0.f, 0.f);
-        }
-        if ((nrv & 31u) != 0u) {
-          const uint2* ne0 = c.entries + (nrv >> 5);
-          prefetch_l1(ne0);
-          prefetch_l1(ne0 + (nrv & 31u) - 1);
-        }
-        for (int k = 0; k < cnt; ++k) {
-          const int l = s_l[eoff + k];
-          if (l == (int)kBadLocal) continue;
-          int rank = __popc(s_mask[t >> 5][l] & lt_bits);
-          for (int w = 0; w < (t >> 5); ++w) rank += __popc(s_mask[w][l]);
-          s_bin[s_off[l] + rank] = (unsigned short)(eoff + k);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < kVoxelsPerBlock / UPD_T; ++j) {
-          const int l = t + UPD_T * j;
-          const int b = s_off[l], e = s_off[l + 1];
-          if (e == b) continue;
-          float sdf = ov[j].x, w = ov[j].y;
-          for (int a = b; a < e; ++a) update_voxel(&sdf, &w, s_d[s_bin[a]], maxw);
-          gv2[l] = make_float2(sdf, w);
-          nz_delta += (int)(w != 0.0f) - (int)(ov[j].y != 0.0f);
-          ++touched;
-        }
-        __syncthreads();
-      }
-    }
-    if (passes) {
+    {
       // ---- a heavy segment beyond the counting sort's capacity, or a light
       // one with more entries than the compacted arrays hold.  Pass 0:
       // per-voxel update counts over all records
@@ -2003,6 +1882,116 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
       stat_add(c.item_stats, item, ST_DVOX, b);
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
     }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Light segments (up to UPD_T routing records), one warp each.  A segment's
+// records are the rays through its block in ascending point order, and the
+// entries of one record are distinct voxels (a ray visits a voxel once), so
+// one record's updates go to the lanes at once and the records follow one
+// another: every voxel gets its updates in point order, the reference's rule
+// (tsdf_handler.cu:648-654) applied as the sequential loop would, with no
+// per-voxel ordering work.  The records go kUwChunk at a time: every lane
+// loads its entry of each of them into registers (one round of independent
+// loads), the lane that first marks a voxel in the segment's 512-bit map
+// loads it into the warp's copy of the block (a second round), and the
+// records are then applied in order from registers.  The touched voxels are
+// written back after the last record; the block's non-zero count moves by
+// the touched voxels whose weight left zero.  4.2 KB of shared memory per warp.
+constexpr int UW_T = 128;
+constexpr int kUwChunk = 16;
+
+__global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
+  __shared__ __align__(16) float2 s_vox[UW_T / 32][kVoxelsPerBlock];
+  __shared__ unsigned s_bits[UW_T / 32][kVoxelsPerBlock / 32];
+  __shared__ unsigned s_oldnz[UW_T / 32][kVoxelsPerBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float2* vox = s_vox[w];
+  unsigned* bits = s_bits[w];
+  unsigned* oldnz = s_oldnz[w];
+  const long long nseg = c.ctr->n_seg;
+  const unsigned* rv = c.rec_val[rec_sel];
+  long long next = 0;
+  if (lane == 0) next = (long long)atomicAdd(&c.ctr->q_update_warp, 1ull);
+  next = __shfl_sync(kFull, next, 0);
+  while (next < nseg) {
+    const long long sj = next;
+    // the segment after this one: claimed now, its descriptor fetched early
+    long long q = 0;
+    if (lane == 0) q = (long long)atomicAdd(&c.ctr->q_update_warp, 1ull);
+    next = __shfl_sync(kFull, q, 0);
+    if (next < nseg && lane == 0) prefetch_l1(c.seg_desc + next);
+    const int4 d = c.seg_desc[sj];
+    const int nrec = d.y - d.x;
+    if (nrec > UPD_T) continue;  // heavy: k_heavy_update, k_hot_chains or k_update's passes
+    const int item = c.seg_item[sj];
+    const float maxw = __int_as_float(d.w);
+    float2* gv2 = c.voxels + (long long)d.z * kVoxelsPerBlock;
+    if (lane < kVoxelsPerBlock / 32) bits[lane] = 0u, oldnz[lane] = 0u;
+    __syncwarp();
+    unsigned n_upd = 0;
+    for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
+      const int m = min(kUwChunk, nrec - c0);
+      const unsigned myrv = lane < m ? rv[d.x + c0 + lane] : 0u;
+      uint2 xs[kUwChunk];
+#pragma unroll
+      for (int j = 0; j < kUwChunk; ++j) {
+        const unsigned v = __shfl_sync(kFull, myrv, j);
+        xs[j] = lane < (int)(v & 31u) ? c.entries[(v >> 5) + lane] : make_uint2(0u, kBadLocal);
+      }
+      // voxels first touched in this chunk: loaded by the lane that marked them
+#pragma unroll
+      for (int j = 0; j < kUwChunk; ++j) {
+        const unsigned l = xs[j].y;
+        if (l != kBadLocal) {
+          ++n_upd;
+          const unsigned bit = 1u << (l & 31u);
+          if (!(atomicOr(&bits[l >> 5], bit) & bit)) {
+            const float2 v0 = gv2[l];
+            vox[l] = v0;
+            if (v0.y != 0.0f) atomicOr(&oldnz[l >> 5], bit);
+          }
+        }
+      }
+      __syncwarp();
+      // the chunk's records in point order; one record's entries update distinct voxels
+#pragma unroll
+      for (int j = 0; j < kUwChunk; ++j) {
+        if (j < m) {
+          const uint2 x = xs[j];
+          if (x.y != kBadLocal) {
+            float2 v = vox[x.y];
+            update_voxel(&v.x, &v.y, __uint_as_float(x.x), maxw);
+            vox[x.y] = v;
+          }
+          __syncwarp();
+        }
+      }
+    }
+    // write back the touched voxels
+    int nz_delta = 0, touched = 0;
+#pragma unroll 4
+    for (int j = 0; j < kVoxelsPerBlock / 32; ++j) {
+      const unsigned b = bits[j];
+      const bool t = (b >> lane) & 1u;
+      float2 v = make_float2(0.f, 0.f);
+      if (t) {
+        v = vox[32 * j + lane];
+        gv2[32 * j + lane] = v;
+      }
+      const unsigned nz = __ballot_sync(kFull, t && v.y != 0.0f);
+      nz_delta += __popc(nz) - __popc(oldnz[j]);
+      touched += __popc(b);
+    }
+    const unsigned upd = __reduce_add_sync(kFull, n_upd);
+    if (lane == 0) {
+      c.nnz[d.z] += nz_delta;
+      stat_add(c.item_stats, item, ST_UPD, (int)upd);
+      stat_add(c.item_stats, item, ST_DVOX, touched);
+      stat_add(c.item_stats, item, ST_BTOUCH, 1);
+    }
+    __syncwarp();
   }
 }
 
@@ -2680,12 +2669,13 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
   k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
-  k_update<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
+  k_update_warp<<<lc.sm_count * 8, UW_T, 0, s>>>(c, sel);
+  k_update<<<lc.sm_count * 2, UPD_T, 0, s>>>(c, sel);
   cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);
   cudaStreamWaitEvent(s, lc.ev_join2, 0);
   cudaStreamWaitEvent(s, lc.ev_join, 0);
-  *launches += 3;
+  *launches += 4;
 }
 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
