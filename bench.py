@@ -353,6 +353,7 @@ def run_ours(args, rank, world, local, pg):
         eng.flush_l2()
         batch_run(eng, a3)
     stage_acc = eng.stage_times()
+    branches = eng.update_branch_times()
     eng.set_stage_timing(0)
     t_dev = sum(dev_ms) / 1000.0
     t_dev = max_over_ranks(pg, t_dev)
@@ -368,7 +369,7 @@ def run_ours(args, rank, world, local, pg):
     # ---- e2e: pinned host buffers through the C-ABI, wall clock
     if args.no_e2e:
         return dict(value=value, ms_per_step=ms_per_step, e2e=None, plain=None, served=None, stats=mstats,
-                    stages=stage_acc,
+                    stages=stage_acc, branches=branches,
                     clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans, timed_pts=timed_pts,
                     dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
     eng2 = new_engine()
@@ -471,7 +472,7 @@ def run_ours(args, rank, world, local, pg):
                   "path": "tsdf_submit + tsdf_wait, the 32 maps' scans of a step queued at once, pinned host in/out"}
 
     return dict(value=value, ms_per_step=ms_per_step, e2e=e2e, plain=plain, served=served, stats=mstats,
-                stages=stage_acc, clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans,
+                stages=stage_acc, branches=branches, clocks=clocks, gpu_launches=gpu_launches, specs=specs, scans=scans,
                 timed_pts=timed_pts, dev_ms=dev_ms, wall_ms=wall_ms, stats_all=stats_all)
 
 
@@ -720,6 +721,8 @@ def result_line(args, r: dict, world: int, tuned, peak: float, peak_kind: str) -
                      "traffic_over_algorithmic": (traffic / dom_bytes) if traffic and dom_bytes else None,
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / peak},
         "stage_ms_per_step": stage_ms,
+        "update_branch_ms": ({k: v for k, v in r["branches"].items() if k != "steps"}
+                             if r.get("branches") else None),
         "algorithmic_bytes_per_step": ab,
         "per_step": {k: r["stats"][k] for k in ("n_points", "voxel_updates", "distinct_voxels", "blocks_touched",
                                                 "new_blocks", "alloc_blocks_before", "published",

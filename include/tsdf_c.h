@@ -334,6 +334,11 @@ tsdf_status tsdf_step_times(tsdf_engine* eng, double* ms, int64_t* steps);
 /* Stage names and accumulated milliseconds / launch counts since the last
  * reset.  names may be NULL.  *n in: capacity, out: number of stages. */
 tsdf_status tsdf_stage_times(tsdf_engine* eng, const char** names, double* ms, int64_t* launches, int* n);
+/* The update stage's three concurrent branches in stage-timed steps (on = 1):
+ * accumulated milliseconds from the stage's start to the end of ms[0] the hot
+ * chains, ms[1] the binned heavy blocks, ms[2] the light blocks, and the
+ * number of steps summed.  Reset with the stage times. */
+tsdf_status tsdf_update_branch_times(tsdf_engine* eng, double* ms, int64_t* steps);
 tsdf_status tsdf_reset_stage_times(tsdf_engine* eng);
 /* Write a buffer larger than L2 on the engine's stream (between timed steps). */
 tsdf_status tsdf_flush_l2(tsdf_engine* eng);

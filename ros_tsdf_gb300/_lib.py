@@ -120,6 +120,7 @@ SIGNATURES = [
     ("tsdf_set_stage_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("tsdf_stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    ("tsdf_update_branch_times", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("tsdf_reset_stage_times", C.c_int, [C.c_void_p]),
     ("tsdf_step_times", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("tsdf_flush_l2", C.c_int, [C.c_void_p]),

@@ -162,6 +162,7 @@ struct Lane {
   std::map<int, cudaGraphExec_t> graphs;
   std::map<int, long long> graph_launches;
   cudaEvent_t ev_stage[STAGE_COUNT + 1] = {};
+  cudaEvent_t ev_branch[3] = {};  // update-stage branch ends (stage-timed steps)
   cudaEvent_t ev_step[2] = {};  // around the whole step, outside the graph
   cudaEvent_t ev_done = nullptr;
   // the batch currently in flight (served mode)
@@ -210,6 +211,8 @@ struct tsdf_engine {
   bool stage_timing = false;
   double stage_ms[STAGE_COUNT] = {};
   long long stage_launches[STAGE_COUNT] = {};
+  double branch_ms[3] = {};
+  long long branch_steps = 0;
   double step_ms = 0;
   long long step_count = 0;
   std::atomic<long long> launches{0};
@@ -270,6 +273,7 @@ LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_p
   lc.ev_fork = L.ev_fork;
   lc.ev_join = L.ev_join;
   lc.ev_join2 = L.ev_join2;
+  for (int i = 0; i < 3; ++i) lc.ev_branch[i] = nullptr;
   return lc;
 }
 
@@ -282,6 +286,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   CK(cudaEventCreateWithFlags(&L.ev_join, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&L.ev_join2, cudaEventDisableTiming));
   for (int i = 0; i <= STAGE_COUNT; ++i) CK(cudaEventCreate(&L.ev_stage[i]));
+  for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&L.ev_branch[i]));
   for (int i = 0; i < 2; ++i) CK(cudaEventCreate(&L.ev_step[i]));
   CK(cudaEventCreateWithFlags(&L.ev_done, cudaEventDisableTiming));
   const long long npts = c.max_batch_points;
@@ -378,6 +383,8 @@ void lane_free(Lane& L) {
   if (L.h_mctr) cudaFreeHost(L.h_mctr);
   for (int i = 0; i <= STAGE_COUNT; ++i)
     if (L.ev_stage[i]) cudaEventDestroy(L.ev_stage[i]);
+  for (int i = 0; i < 3; ++i)
+    if (L.ev_branch[i]) cudaEventDestroy(L.ev_branch[i]);
   for (int i = 0; i < 2; ++i)
     if (L.ev_step[i]) cudaEventDestroy(L.ev_step[i]);
   if (L.ev_done) cudaEventDestroy(L.ev_done);
@@ -395,6 +402,8 @@ void lane_free(Lane& L) {
 long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
                            bool timed) {
   LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout);
+  if (timed)
+    for (int i = 0; i < 3; ++i) lc.ev_branch[i] = L.ev_branch[i];
   long long n = 0;
   using Fn = void (*)(const Ctx&, const LaunchCfg&, cudaStream_t, long long*);
   const Fn stages[STAGE_COUNT] = {stage_init,       stage_ray_blocks,  stage_alloc_order,
@@ -652,6 +661,14 @@ tsdf_status finish_batch(tsdf_engine* eng, Lane& L, int n, tsdf_scan_result* res
         eng->stage_ms[i] += ms;
         eng->stage_launches[i] += 1;
       }
+    }
+    float bms[3];
+    bool ok = true;
+    for (int i = 0; i < 3; ++i)
+      ok = ok && cudaEventElapsedTime(&bms[i], L.ev_stage[STAGE_UPDATE], L.ev_branch[i]) == cudaSuccess;
+    if (ok) {
+      for (int i = 0; i < 3; ++i) eng->branch_ms[i] += bms[i];
+      eng->branch_steps += 1;
     }
     cudaGetLastError();
   }
@@ -1574,10 +1591,20 @@ tsdf_status tsdf_stage_times(tsdf_engine* eng, const char** names, double* ms, i
   return TSDF_OK;
 }
 
+tsdf_status tsdf_update_branch_times(tsdf_engine* eng, double* ms, int64_t* steps) {
+  if (!eng || !ms || !steps) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  for (int i = 0; i < 3; ++i) ms[i] = eng->branch_ms[i];
+  *steps = eng->branch_steps;
+  return TSDF_OK;
+}
+
 tsdf_status tsdf_reset_stage_times(tsdf_engine* eng) {
   if (!eng) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   for (int i = 0; i < STAGE_COUNT; ++i) eng->stage_ms[i] = 0, eng->stage_launches[i] = 0;
+  for (int i = 0; i < 3; ++i) eng->branch_ms[i] = 0;
+  eng->branch_steps = 0;
   eng->step_ms = 0;
   eng->step_count = 0;
   return TSDF_OK;

@@ -242,6 +242,9 @@ struct LaunchCfg {
   cudaEvent_t ev_fork;   // and join it back (timing disabled; usable in graph capture)
   cudaEvent_t ev_join;
   cudaEvent_t ev_join2;
+  // stage-timed steps only (null otherwise): the end of each update-stage
+  // branch, recorded on its own stream (hot chains, heavy bins, light warps)
+  cudaEvent_t ev_branch[3];
 };
 
 cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice

@@ -1605,73 +1605,81 @@ __device__ __forceinline__ void warp_compose(float& a, float& b, int lane) {
 // A voxel's chain as one composition of affine maps (engine sdf_mode 1).  The
 // update rule (tsdf_handler.cu:648-654) is, in exact arithmetic,
 //   sdf' = a sdf + b,  a = W / W',  b = RN(w d) / W',  W' = RN(W + w),
-// and composing maps is associative.  The weights stay exact: while the voxel
-// is below max_weight the chain goes 32 updates at a time, lane 0 running the
+// and composing maps is associative.  The chain streams through this warp's
+// shared memory in chunks of 256 bins (8 coalesced float4 loads per lane, the
+// next chunk in flight in registers while the current one is composed).  The
+// weights stay exact: while the voxel is below max_weight lane 0 runs the
 // reference's serial float weight chain (W' = RN(W + w), W = min(W', max))
-// over the batch from shared memory, every lane then taking its update's map
-// and a warp reduction composing the batch.  From max_weight on every
-// W = max and W' = RN(max + w), which k_heavy_place precomputed, so the 32
-// lanes each compose a contiguous part of the rest and one reduction composes
-// them.  The composition is in float (GB300's FP64 rate made a double
-// composition slower than the serial chain): every map is contractive
-// (0 <= a < 1), so its rounding stays of the order of the serial chain's own;
-// on 13,400-update chains the two differ by 3e-7 T, and the tests assert
-// 1e-5 T on every workload.  tile: 32 float2 of this warp's shared memory.
-// Returns {sdf, W}, valid in lane 0.
+// over the chunk in shared memory; from max_weight on every W = max and
+// W' = RN(max + w), which k_heavy_place precomputed, so the chunk needs no
+// serial step.  Each lane then composes the maps of 8 consecutive bins and
+// one ordered warp reduction composes the chunk.  The composition is in float
+// (GB300's FP64 rate made a double composition slower than the serial chain):
+// every map is contractive (0 <= a < 1), so its rounding stays of the order
+// of the serial chain's own; on 13,400-update chains the two differ by
+// 3e-7 T, and the tests assert 1e-5 T on every workload.  tile: this warp's
+// kScanTile float4 of shared memory.  Returns {sdf, W}, valid in lane 0.
+constexpr int kScanChunk = 256;                            // bins per chunk, 8 per lane
+constexpr int kScanTile = kScanChunk + kScanChunk / 8;     // one pad float4 per 8 bins
+__device__ __forceinline__ int scan_slot(int k) { return k + (k >> 3); }
+
 __device__ __forceinline__ float2 warp_chain_scan(float sdf0, float W0, const float4* bins, int n, float maxw,
-                                                  int lane, float2* tile) {
+                                                  int lane, float4* tile) {
+  const float4 pad = make_float4(0.f, 1.f, 1.f, 0.f);
   float A = 1.0f, B = 0.0f;  // the composition so far (lane 0)
   float W = W0;              // the weight chain (lane 0)
-  int base = 0;
-  bool sat = W0 == maxw;
-  while (!sat && base < n) {
-    const int m = min(32, n - base);
-    const float4 x = lane < m ? bins[base + lane] : make_float4(0.f, 1.f, 1.f, 0.f);
-    tile[lane].x = x.w;
+  bool sat = W0 == maxw;     // uniform across the warp
+  float4 nxt[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int i = 32 * k + lane;
+    nxt[k] = i < n ? bins[i] : pad;
+  }
+  for (int base = 0; base < n; base += kScanChunk) {
+    const int m = min(kScanChunk, n - base);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) tile[scan_slot(32 * k + lane)] = nxt[k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int i = base + kScanChunk + 32 * k + lane;
+      nxt[k] = i < n ? bins[i] : pad;
+    }
     __syncwarp();
-    if (lane == 0) {
-      for (int k = 0; k < m; ++k) {
-        const float nw = fadd(W, tile[k].x);
-        tile[k] = make_float2(W, nw);
-        W = fminf(nw, maxw);
+    const bool chunk_sat = sat;
+    if (!chunk_sat) {
+      // the serial weight chain: .w <- W before the update, .y <- W'
+      if (lane == 0) {
+        for (int k = 0; k < m; ++k) {
+          float4* x = &tile[scan_slot(k)];
+          const float nw = fadd(W, x->w);
+          x->w = W;
+          x->y = nw;
+          W = fminf(nw, maxw);
+        }
+      }
+      sat = __shfl_sync(kFull, W == maxw, 0);
+      __syncwarp();
+    }
+    float a = 1.0f, b = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = 8 * lane + j;
+      if (k < m) {
+        const float4 x = tile[scan_slot(k)];
+        const float r = __frcp_rn(x.y);
+        const float ai = __fmul_rn(chunk_sat ? maxw : x.w, r);
+        b = __fmaf_rn(ai, b, __fmul_rn(x.x, r));
+        a = __fmul_rn(ai, a);
       }
     }
-    __syncwarp();
-    float a = 1.0f, b = 0.0f;
-    if (lane < m) {
-      const float2 ww = tile[lane];
-      const float r = __frcp_rn(ww.y);
-      a = __fmul_rn(ww.x, r);
-      b = __fmul_rn(x.x, r);
-    }
     warp_compose(a, b, lane);
     if (lane == 0) {
       B = __fmaf_rn(a, B, b);
       A = __fmul_rn(a, A);
     }
-    sat = __shfl_sync(kFull, W == maxw, 0);
-    base += m;
     __syncwarp();
   }
-  if (base < n) {
-    const int rest = n - base;
-    const int chunk = (rest + 31) >> 5;
-    const int lo = base + min(rest, lane * chunk), hi = min(n, lo + chunk);
-    float a = 1.0f, b = 0.0f;
-    for (int i = lo; i < hi; ++i) {
-      const float4 x = bins[i];
-      const float r = __frcp_rn(x.y);
-      const float ai = __fmul_rn(maxw, r);
-      b = __fmaf_rn(ai, b, __fmul_rn(x.x, r));
-      a = __fmul_rn(ai, a);
-    }
-    warp_compose(a, b, lane);
-    if (lane == 0) {
-      B = __fmaf_rn(a, B, b);
-      A = __fmul_rn(a, A);
-      W = maxw;
-    }
-  }
+  if (sat) W = maxw;
   return make_float2(__fmaf_rn(A, sdf0, B), W);
 }
 
@@ -1695,8 +1703,7 @@ __device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32],
     float2* v = c.voxels + (long long)hc.phys * kVoxelsPerBlock + hc.local;
     const float2 v0 = *v;
     if (c.sdf_scan) {
-      const float2 r = warp_chain_scan(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, lane,
-                                       reinterpret_cast<float2*>(tile[0]));
+      const float2 r = warp_chain_scan(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, lane, tile[0]);
       if (lane == 0) *v = r;
       continue;
     }
@@ -1732,11 +1739,13 @@ __device__ __forceinline__ void for_record_entries(const uint2* e, int cnt, F f)
 // issue contention on its sub-partition).  Each warp takes chains until the
 // list is empty; a CTA that finds it empty exits and frees its SM.
 constexpr int kHotSmem = 64 * 1024;
+constexpr int kHotWarpTile = kHotSmem / 16 / 4;  // float4 per warp: 2 x 32 (serial chain) or kScanTile
+static_assert(kHotWarpTile >= kScanTile && kHotWarpTile >= 64, "hot-chain tile");
 
 __global__ void __launch_bounds__(128) k_hot_chains(Ctx c) {
   extern __shared__ __align__(16) float4 s_hot_tile[];
   const int t = threadIdx.x;
-  float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(s_hot_tile) + 2 * (t >> 5);
+  float4 (*tile)[32] = reinterpret_cast<float4 (*)[32]>(s_hot_tile + (t >> 5) * kHotWarpTile);
   run_hot_chains(c, tile, t & 31);
 }
 
@@ -1902,7 +1911,7 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
 constexpr int UW_T = 128;
 constexpr int kUwChunk = 16;
 
-__global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(UW_T, 7) k_update_warp(Ctx c, int rec_sel) {
   __shared__ __align__(16) float2 s_vox[UW_T / 32][kVoxelsPerBlock];
   __shared__ unsigned s_bits[UW_T / 32][kVoxelsPerBlock / 32];
   __shared__ unsigned s_oldnz[UW_T / 32][kVoxelsPerBlock / 32];
@@ -1937,14 +1946,17 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
       uint2 xs[kUwChunk];
 #pragma unroll
       for (int j = 0; j < kUwChunk; ++j) {
-        const unsigned v = __shfl_sync(kFull, myrv, j);
-        xs[j] = lane < (int)(v & 31u) ? c.entries[(v >> 5) + lane] : make_uint2(0u, kBadLocal);
+        xs[j] = make_uint2(0u, kBadLocal);
+        if (j < m) {  // uniform: a short last chunk skips the rest
+          const unsigned v = __shfl_sync(kFull, myrv, j);
+          if (lane < (int)(v & 31u)) xs[j] = c.entries[(v >> 5) + lane];
+        }
       }
       // voxels first touched in this chunk: loaded by the lane that marked them
 #pragma unroll
       for (int j = 0; j < kUwChunk; ++j) {
         const unsigned l = xs[j].y;
-        if (l != kBadLocal) {
+        if (j < m && l != kBadLocal) {
           ++n_upd;
           const unsigned bit = 1u << (l & 31u);
           if (!(atomicOr(&bits[l >> 5], bit) & bit)) {
@@ -2668,8 +2680,11 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   cudaStreamWaitEvent(lc.side2, lc.ev_fork, 0);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
+  if (lc.ev_branch[0]) cudaEventRecordWithFlags(lc.ev_branch[0], lc.side2, cudaEventRecordExternal);
   k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
+  if (lc.ev_branch[1]) cudaEventRecordWithFlags(lc.ev_branch[1], lc.side, cudaEventRecordExternal);
   k_update_warp<<<lc.sm_count * 8, UW_T, 0, s>>>(c, sel);
+  if (lc.ev_branch[2]) cudaEventRecordWithFlags(lc.ev_branch[2], s, cudaEventRecordExternal);
   k_update<<<lc.sm_count * 2, UPD_T, 0, s>>>(c, sel);
   cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);

@@ -338,6 +338,15 @@ class Engine:
         self._check(self.lib.tsdf_stage_times(self.h, names, ms, cnt, C.byref(n)), "tsdf_stage_times")
         return {names[i].decode(): (ms[i], int(cnt[i])) for i in range(n.value)}
 
+    def update_branch_times(self) -> dict:
+        """Per stage-timed step, milliseconds from the update stage's start to
+        the end of each of its concurrent branches."""
+        ms = (C.c_double * 3)()
+        n = C.c_int64()
+        self._check(self.lib.tsdf_update_branch_times(self.h, ms, C.byref(n)), "tsdf_update_branch_times")
+        k = max(int(n.value), 1)
+        return {"hot_chains": ms[0] / k, "heavy": ms[1] / k, "light": ms[2] / k, "steps": int(n.value)}
+
     def reset_stage_times(self):
         self.lib.tsdf_reset_stage_times(self.h)
 
