@@ -1901,24 +1901,42 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
 // one record's updates go to the lanes at once and the records follow one
 // another: every voxel gets its updates in point order, the reference's rule
 // (tsdf_handler.cu:648-654) applied as the sequential loop would, with no
-// per-voxel ordering work.  The records go kUwChunk at a time: every lane
-// loads its entry of each of them into registers (one round of independent
-// loads), the lane that first marks a voxel in the segment's 512-bit map
-// loads it into the warp's copy of the block (a second round), and the
-// records are then applied in order from registers.  The touched voxels are
+// per-voxel ordering work.  Three phases, each with its global loads issued
+// together: (A) the segment's record values (four per lane), then its
+// entries kUwChunk records at a time, marking every touched voxel in the
+// warp's 512-bit map; (B) the touched voxels loaded into the warp's copy of
+// the block, 32 consecutive voxels per instruction, eight words in flight;
+// (C) the records applied in order from registers (a segment of more than
+// kUwChunk records loads its entries again, from L1).  The touched voxels are
 // written back after the last record; the block's non-zero count moves by
 // the touched voxels whose weight left zero.  4.2 KB of shared memory per warp.
 constexpr int UW_T = 128;
 constexpr int kUwChunk = 16;
 
-__global__ void __launch_bounds__(UW_T, 7) k_update_warp(Ctx c, int rec_sel) {
+// Record value i of the segment (lane i % 32 holds it in rv4[i / 32]).
+__device__ __forceinline__ unsigned pick_rv(const unsigned (&rv4)[UPD_T / 32], int k) {
+  return k == 0 ? rv4[0] : k == 1 ? rv4[1] : k == 2 ? rv4[2] : rv4[3];
+}
+
+// The entries of records c0 .. c0 + kUwChunk - 1 (lane l: entry l of each;
+// kBadLocal past a record's count or the segment's end).
+__device__ __forceinline__ void load_round(const Ctx& c, const unsigned (&rv4)[UPD_T / 32], int c0, int lane,
+                                           uint2 (&xs)[kUwChunk]) {
+  const unsigned src = pick_rv(rv4, c0 >> 5);
+#pragma unroll
+  for (int j = 0; j < kUwChunk; ++j) {
+    const unsigned v = __shfl_sync(kFull, src, (c0 & 31) + j);
+    xs[j] = lane < (int)(v & 31u) ? c.entries[(v >> 5) + lane] : make_uint2(0u, kBadLocal);
+  }
+}
+
+__global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
+  static_assert(UPD_T == 128 && kUwChunk == 16, "record layout of k_update_warp");
   __shared__ __align__(16) float2 s_vox[UW_T / 32][kVoxelsPerBlock];
   __shared__ unsigned s_bits[UW_T / 32][kVoxelsPerBlock / 32];
-  __shared__ unsigned s_oldnz[UW_T / 32][kVoxelsPerBlock / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float2* vox = s_vox[w];
   unsigned* bits = s_bits[w];
-  unsigned* oldnz = s_oldnz[w];
   const long long nseg = c.ctr->n_seg;
   const unsigned* rv = c.rec_val[rec_sel];
   long long next = 0;
@@ -1937,37 +1955,51 @@ __global__ void __launch_bounds__(UW_T, 7) k_update_warp(Ctx c, int rec_sel) {
     const int item = c.seg_item[sj];
     const float maxw = __int_as_float(d.w);
     float2* gv2 = c.voxels + (long long)d.z * kVoxelsPerBlock;
-    if (lane < kVoxelsPerBlock / 32) bits[lane] = 0u, oldnz[lane] = 0u;
+    if (lane < kVoxelsPerBlock / 32) bits[lane] = 0u;
+    unsigned rv4[UPD_T / 32];
+#pragma unroll
+    for (int k = 0; k < UPD_T / 32; ++k) {
+      const int i = 32 * k + lane;
+      rv4[k] = i < nrec ? rv[d.x + i] : 0u;
+    }
     __syncwarp();
+    // (A) entries and the touched-voxel map
+    uint2 xs[kUwChunk];
     unsigned n_upd = 0;
     for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
-      const int m = min(kUwChunk, nrec - c0);
-      const unsigned myrv = lane < m ? rv[d.x + c0 + lane] : 0u;
-      uint2 xs[kUwChunk];
-#pragma unroll
-      for (int j = 0; j < kUwChunk; ++j) {
-        xs[j] = make_uint2(0u, kBadLocal);
-        if (j < m) {  // uniform: a short last chunk skips the rest
-          const unsigned v = __shfl_sync(kFull, myrv, j);
-          if (lane < (int)(v & 31u)) xs[j] = c.entries[(v >> 5) + lane];
-        }
-      }
-      // voxels first touched in this chunk: loaded by the lane that marked them
+      load_round(c, rv4, c0, lane, xs);
 #pragma unroll
       for (int j = 0; j < kUwChunk; ++j) {
         const unsigned l = xs[j].y;
-        if (j < m && l != kBadLocal) {
+        if (l != kBadLocal) {
           ++n_upd;
-          const unsigned bit = 1u << (l & 31u);
-          if (!(atomicOr(&bits[l >> 5], bit) & bit)) {
-            const float2 v0 = gv2[l];
-            vox[l] = v0;
-            if (v0.y != 0.0f) atomicOr(&oldnz[l >> 5], bit);
-          }
+          atomicOr(&bits[l >> 5], 1u << (l & 31u));
         }
       }
-      __syncwarp();
-      // the chunk's records in point order; one record's entries update distinct voxels
+    }
+    __syncwarp();
+    // (B) the touched voxels into the block copy; their non-zero count before
+    int nz_old = 0;
+#pragma unroll
+    for (int j0 = 0; j0 < kVoxelsPerBlock / 32; j0 += 8) {
+      float2 v[8];
+      bool t[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        t[k] = (bits[j0 + k] >> lane) & 1u;
+        v[k] = t[k] ? gv2[32 * (j0 + k) + lane] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (t[k]) vox[32 * (j0 + k) + lane] = v[k];
+        nz_old += __popc(__ballot_sync(kFull, t[k] && v[k].y != 0.0f));
+      }
+    }
+    __syncwarp();
+    // (C) the records in point order; one record's entries update distinct voxels
+    for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
+      if (nrec > kUwChunk) load_round(c, rv4, c0, lane, xs);
+      const int m = min(kUwChunk, nrec - c0);
 #pragma unroll
       for (int j = 0; j < kUwChunk; ++j) {
         if (j < m) {
@@ -1982,7 +2014,7 @@ __global__ void __launch_bounds__(UW_T, 7) k_update_warp(Ctx c, int rec_sel) {
       }
     }
     // write back the touched voxels
-    int nz_delta = 0, touched = 0;
+    int nz_new = 0, touched = 0;
 #pragma unroll 4
     for (int j = 0; j < kVoxelsPerBlock / 32; ++j) {
       const unsigned b = bits[j];
@@ -1992,13 +2024,12 @@ __global__ void __launch_bounds__(UW_T, 7) k_update_warp(Ctx c, int rec_sel) {
         v = vox[32 * j + lane];
         gv2[32 * j + lane] = v;
       }
-      const unsigned nz = __ballot_sync(kFull, t && v.y != 0.0f);
-      nz_delta += __popc(nz) - __popc(oldnz[j]);
+      nz_new += __popc(__ballot_sync(kFull, t && v.y != 0.0f));
       touched += __popc(b);
     }
     const unsigned upd = __reduce_add_sync(kFull, n_upd);
     if (lane == 0) {
-      c.nnz[d.z] += nz_delta;
+      c.nnz[d.z] += nz_new - nz_old;
       stat_add(c.item_stats, item, ST_UPD, (int)upd);
       stat_add(c.item_stats, item, ST_DVOX, touched);
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
