@@ -1896,47 +1896,62 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
 
 // ----------------------------------------------------------------------------
 // Light segments (up to UPD_T routing records), one warp each.  A segment's
-// records are the rays through its block in ascending point order, and the
-// entries of one record are distinct voxels (a ray visits a voxel once), so
-// one record's updates go to the lanes at once and the records follow one
-// another: every voxel gets its updates in point order, the reference's rule
-// (tsdf_handler.cu:648-654) applied as the sequential loop would, with no
-// per-voxel ordering work.  Three phases, each with its global loads issued
-// together: (A) the segment's record values (four per lane), then its
-// entries kUwChunk records at a time, marking every touched voxel in the
-// warp's 512-bit map; (B) the touched voxels loaded into the warp's copy of
-// the block, 32 consecutive voxels per instruction, eight words in flight;
-// (C) the records applied in order from registers (a segment of more than
-// kUwChunk records loads its entries again, from L1).  The touched voxels are
-// written back after the last record; the block's non-zero count moves by
-// the touched voxels whose weight left zero.  4.2 KB of shared memory per warp.
+// records are the rays through its block in ascending point order; the
+// entries of one record are distinct voxels (a ray visits a voxel once).  An
+// entry's depth is the number of the segment's earlier entries (in point
+// order) that update its voxel, so the entries of one depth update distinct
+// voxels and the depths taken in ascending order give every voxel its
+// updates in point order: the reference's rule (tsdf_handler.cu:648-654)
+// applied as the sequential loop would.  A segment of at most kUwCap entries:
+//   (A) the record values (four per lane) and an exclusive scan of their
+//       entry counts; every entry loaded flat, 32 per instruction, 16 in
+//       flight per lane; depths from a match over each 32 entries plus the
+//       voxel's running count, and each entry's place within its depth
+//       (a match over the depths plus the depth's running count);
+//   (B) an exclusive scan over the depths, the entries written depth-major
+//       into shared memory; depth 0 holds every touched voxel once, whose
+//       voxels are loaded into the warp's block copy;
+//   (C) the depths in order, each one's entries 32 at a time with no wait
+//       between them (their voxels are distinct).
+// On this workload that is a quarter of the warp steps of one record at a
+// time.  A longer segment marks its touched voxels, loads them 32
+// consecutive per instruction and applies its records one at a time, 16
+// records' entries held in registers.  The touched voxels are written back
+// at the end; the block's non-zero count moves by the touched voxels whose
+// weight left zero.  9 KB of shared memory per warp.
 constexpr int UW_T = 128;
-constexpr int kUwChunk = 16;
+constexpr int kUwChunk = 16;  // records per register round (long segments)
+constexpr int kUwCap = 512;   // entries of a segment on the depth path (16 per lane)
+constexpr unsigned kUwNone = 0xFFFFFFFFu;
 
-// Record value i of the segment (lane i % 32 holds it in rv4[i / 32]).
-__device__ __forceinline__ unsigned pick_rv(const unsigned (&rv4)[UPD_T / 32], int k) {
-  return k == 0 ? rv4[0] : k == 1 ? rv4[1] : k == 2 ? rv4[2] : rv4[3];
-}
+struct __align__(16) UwWarp {
+  float2 vox[kVoxelsPerBlock];       // the block's touched voxels
+  uint2 sorted[kUwCap];              // entries by depth {d, local}; first the records' entry bases and positions
+  int lvl[UPD_T];                    // per depth: running count, then its first entry
+  unsigned char cnt[kVoxelsPerBlock];  // per voxel: updates so far (zero between segments)
+};
 
-// The entries of records c0 .. c0 + kUwChunk - 1 (lane l: entry l of each;
-// kBadLocal past a record's count or the segment's end).
+// The entries of records c0 .. c0 + kUwChunk - 1 (record i is rv4[i % 4] of
+// lane i / 4; lane l takes entry l of each, kBadLocal past its count).
 __device__ __forceinline__ void load_round(const Ctx& c, const unsigned (&rv4)[UPD_T / 32], int c0, int lane,
                                            uint2 (&xs)[kUwChunk]) {
-  const unsigned src = pick_rv(rv4, c0 >> 5);
 #pragma unroll
   for (int j = 0; j < kUwChunk; ++j) {
-    const unsigned v = __shfl_sync(kFull, src, (c0 & 31) + j);
+    const unsigned v = __shfl_sync(kFull, rv4[j & 3], (c0 + j) >> 2);
     xs[j] = lane < (int)(v & 31u) ? c.entries[(v >> 5) + lane] : make_uint2(0u, kBadLocal);
   }
 }
 
 __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
-  static_assert(UPD_T == 128 && kUwChunk == 16, "record layout of k_update_warp");
-  __shared__ __align__(16) float2 s_vox[UW_T / 32][kVoxelsPerBlock];
-  __shared__ unsigned s_bits[UW_T / 32][kVoxelsPerBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float2* vox = s_vox[w];
-  unsigned* bits = s_bits[w];
+  static_assert(UPD_T == 128 && kUwChunk == 16 && kUwCap == 512, "record and entry layout of k_update_warp");
+  __shared__ UwWarp s_warp[UW_T / 32];
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  UwWarp& sm = s_warp[threadIdx.x >> 5];
+  reinterpret_cast<uint4*>(sm.cnt)[lane] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+  for (int k = 0; k < UPD_T / 32; ++k) sm.lvl[32 * k + lane] = 0;
+  __syncwarp();
   const long long nseg = c.ctr->n_seg;
   const unsigned* rv = c.rec_val[rec_sel];
   long long next = 0;
@@ -1955,83 +1970,191 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
     const int item = c.seg_item[sj];
     const float maxw = __int_as_float(d.w);
     float2* gv2 = c.voxels + (long long)d.z * kVoxelsPerBlock;
-    if (lane < kVoxelsPerBlock / 32) bits[lane] = 0u;
     unsigned rv4[UPD_T / 32];
+    int pre[UPD_T / 32];
+    int lsum = 0;
 #pragma unroll
     for (int k = 0; k < UPD_T / 32; ++k) {
-      const int i = 32 * k + lane;
+      const int i = 4 * lane + k;
       rv4[k] = i < nrec ? rv[d.x + i] : 0u;
+      pre[k] = lsum;
+      lsum += (int)(rv4[k] & 31u);
     }
-    __syncwarp();
-    // (A) entries and the touched-voxel map
-    uint2 xs[kUwChunk];
-    unsigned n_upd = 0;
-    for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
-      load_round(c, rv4, c0, lane, xs);
+    int incl = lsum;
 #pragma unroll
-      for (int j = 0; j < kUwChunk; ++j) {
-        const unsigned l = xs[j].y;
-        if (l != kBadLocal) {
-          ++n_upd;
-          atomicOr(&bits[l >> 5], 1u << (l & 31u));
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int n_ent = __shfl_sync(kFull, incl, 31);
+    int n_upd = 0, nz_old = 0, nz_new = 0, touched = 0;
+    if (n_ent <= kUwCap) {
+      // ---- (A) entries flat, depths and places within depth
+      unsigned* ebase = reinterpret_cast<unsigned*>(sm.sorted);          // [UPD_T]
+      int* rpos = reinterpret_cast<int*>(sm.sorted) + UPD_T;             // [UPD_T]
+#pragma unroll
+      for (int k = 0; k < UPD_T / 32; ++k) {
+        ebase[4 * lane + k] = rv4[k] >> 5;
+        rpos[4 * lane + k] = incl - lsum + pre[k];
+      }
+      __syncwarp();
+      uint2 xs[kUwCap / 32];
+#pragma unroll
+      for (int i = 0; i < kUwCap / 32; ++i) {
+        const int f = 32 * i + lane;
+        xs[i] = make_uint2(0u, kBadLocal);
+        if (f < n_ent) {
+          int j = 0;
+#pragma unroll
+          for (int st = UPD_T / 2; st >= 1; st >>= 1)
+            if (j + st < nrec && rpos[j + st] <= f) j += st;
+          xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
         }
       }
-    }
-    __syncwarp();
-    // (B) the touched voxels into the block copy; their non-zero count before
-    int nz_old = 0;
+      int maxdep = 0;
 #pragma unroll
-    for (int j0 = 0; j0 < kVoxelsPerBlock / 32; j0 += 8) {
-      float2 v[8];
-      bool t[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        t[k] = (bits[j0 + k] >> lane) & 1u;
-        v[k] = t[k] ? gv2[32 * (j0 + k) + lane] : make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        if (t[k]) vox[32 * (j0 + k) + lane] = v[k];
-        nz_old += __popc(__ballot_sync(kFull, t[k] && v[k].y != 0.0f));
-      }
-    }
-    __syncwarp();
-    // (C) the records in point order; one record's entries update distinct voxels
-    for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
-      if (nrec > kUwChunk) load_round(c, rv4, c0, lane, xs);
-      const int m = min(kUwChunk, nrec - c0);
-#pragma unroll
-      for (int j = 0; j < kUwChunk; ++j) {
-        if (j < m) {
-          const uint2 x = xs[j];
-          if (x.y != kBadLocal) {
-            float2 v = vox[x.y];
-            update_voxel(&v.x, &v.y, __uint_as_float(x.x), maxw);
-            vox[x.y] = v;
-          }
+      for (int i = 0; i < kUwCap / 32; ++i) {
+        if (32 * i < n_ent) {  // uniform
+          const unsigned l = xs[i].y;
+          const bool ok = l != kBadLocal;
+          const unsigned pv = __match_any_sync(kFull, ok ? l : (0x10000u | lane));
+          int dep = 0;
+          if (ok) dep = (int)sm.cnt[l] + __popc(pv & lt);
+          const unsigned pd = __match_any_sync(kFull, ok ? (unsigned)dep : (0x10000u | lane));
+          int pil = 0;
+          // dep < nrec <= 128: a record updates a voxel at most once (the
+          // mask only keeps the index inside the array)
+          if (ok) pil = sm.lvl[dep & 127] + __popc(pd & lt);
           __syncwarp();
+          if (ok && (pv >> lane) == 1u) sm.cnt[l] = (unsigned char)(dep + 1);
+          if (ok && (pd >> lane) == 1u) sm.lvl[dep & 127] = pil + 1;
+          __syncwarp();
+          if (ok) ++n_upd, maxdep = max(maxdep, dep);
+          xs[i].y = ok ? (l | ((unsigned)dep << 9) | ((unsigned)pil << 16)) : kUwNone;
+        }
+      }
+      const int n_dep = __reduce_max_sync(kFull, (unsigned)maxdep) + 1;
+      // ---- (B) depth bases, entries depth-major, touched voxels loaded
+      int c4[UPD_T / 32], dsum = 0;
+#pragma unroll
+      for (int k = 0; k < UPD_T / 32; ++k) c4[k] = sm.lvl[4 * lane + k], dsum += c4[k];
+      int dincl = dsum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, dincl, o);
+        if (lane >= o) dincl += y;
+      }
+      const int n_valid = __shfl_sync(kFull, dincl, 31);
+      __syncwarp();
+      {
+        int run = dincl - dsum;
+#pragma unroll
+        for (int k = 0; k < UPD_T / 32; ++k) sm.lvl[4 * lane + k] = run, run += c4[k];
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < kUwCap / 32; ++i) {
+        const uint2 x = xs[i];
+        if (32 * i < n_ent && x.y != kUwNone)  // packed by the depth pass
+          sm.sorted[sm.lvl[(x.y >> 9) & 127u] + (int)(x.y >> 16)] = make_uint2(x.x, x.y & 511u);
+      }
+      __syncwarp();
+      const int n0 = n_dep > 1 ? sm.lvl[1] : n_valid;  // depth 0: every touched voxel once
+      for (int k0 = 0; k0 < n0; k0 += 64) {
+        const int ka = k0 + lane, kb = k0 + 32 + lane;
+        const unsigned la = ka < n0 ? sm.sorted[ka].y : 0u;
+        const unsigned lb = kb < n0 ? sm.sorted[kb].y : 0u;
+        float2 va = make_float2(0.f, 0.f), vb = make_float2(0.f, 0.f);
+        if (ka < n0) va = gv2[la];
+        if (kb < n0) vb = gv2[lb];
+        if (ka < n0) sm.vox[la] = va, nz_old += va.y != 0.0f;
+        if (kb < n0) sm.vox[lb] = vb, nz_old += vb.y != 0.0f;
+      }
+      __syncwarp();
+      // ---- (C) the depths in order
+      for (int dd = 0; dd < n_dep; ++dd) {
+        const int e0 = sm.lvl[dd];
+        const int e1 = dd + 1 < n_dep ? sm.lvl[dd + 1] : n_valid;
+        for (int k = e0 + lane; k < e1; k += 32) {
+          const uint2 x = sm.sorted[k];
+          float2 v = sm.vox[x.y];
+          update_voxel(&v.x, &v.y, __uint_as_float(x.x), maxw);
+          sm.vox[x.y] = v;
+        }
+        __syncwarp();
+      }
+      // write back the touched voxels; counters back to zero
+      for (int k = lane; k < n0; k += 32) {
+        const unsigned l = sm.sorted[k].y;
+        const float2 v = sm.vox[l];
+        gv2[l] = v;
+        nz_new += v.y != 0.0f;
+        ++touched;
+        sm.cnt[l] = 0;
+      }
+#pragma unroll
+      for (int k = 0; k < UPD_T / 32; ++k) sm.lvl[32 * k + lane] = 0;
+    } else {
+      // ---- long segment: mark, load the touched voxels, one record at a time
+      uint2 xs[kUwChunk];
+      for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
+        load_round(c, rv4, c0, lane, xs);
+#pragma unroll
+        for (int j = 0; j < kUwChunk; ++j) {
+          const unsigned l = xs[j].y;
+          if (l != kBadLocal) ++n_upd, sm.cnt[l] = 1;
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j0 = 0; j0 < kVoxelsPerBlock / 32; j0 += 8) {
+        float2 v[8];
+        bool t[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          t[k] = sm.cnt[32 * (j0 + k) + lane] != 0;
+          v[k] = t[k] ? gv2[32 * (j0 + k) + lane] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (t[k]) sm.vox[32 * (j0 + k) + lane] = v[k], nz_old += v[k].y != 0.0f;
+      }
+      __syncwarp();
+      for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
+        load_round(c, rv4, c0, lane, xs);
+        const int m = min(kUwChunk, nrec - c0);
+#pragma unroll
+        for (int j = 0; j < kUwChunk; ++j) {
+          if (j < m) {
+            const uint2 x = xs[j];
+            if (x.y != kBadLocal) {
+              float2 v = sm.vox[x.y];
+              update_voxel(&v.x, &v.y, __uint_as_float(x.x), maxw);
+              sm.vox[x.y] = v;
+            }
+            __syncwarp();
+          }
+        }
+      }
+#pragma unroll 4
+      for (int j = 0; j < kVoxelsPerBlock / 32; ++j) {
+        const int l = 32 * j + lane;
+        if (sm.cnt[l]) {
+          const float2 v = sm.vox[l];
+          gv2[l] = v;
+          nz_new += v.y != 0.0f;
+          ++touched;
+          sm.cnt[l] = 0;
         }
       }
     }
-    // write back the touched voxels
-    int nz_new = 0, touched = 0;
-#pragma unroll 4
-    for (int j = 0; j < kVoxelsPerBlock / 32; ++j) {
-      const unsigned b = bits[j];
-      const bool t = (b >> lane) & 1u;
-      float2 v = make_float2(0.f, 0.f);
-      if (t) {
-        v = vox[32 * j + lane];
-        gv2[32 * j + lane] = v;
-      }
-      nz_new += __popc(__ballot_sync(kFull, t && v.y != 0.0f));
-      touched += __popc(b);
-    }
-    const unsigned upd = __reduce_add_sync(kFull, n_upd);
+    const int nz_delta = __reduce_add_sync(kFull, nz_new - nz_old);
+    const unsigned upd = __reduce_add_sync(kFull, (unsigned)n_upd);
+    const unsigned tch = __reduce_add_sync(kFull, (unsigned)touched);
     if (lane == 0) {
-      c.nnz[d.z] += nz_new - nz_old;
+      c.nnz[d.z] += nz_delta;
       stat_add(c.item_stats, item, ST_UPD, (int)upd);
-      stat_add(c.item_stats, item, ST_DVOX, touched);
+      stat_add(c.item_stats, item, ST_DVOX, (int)tch);
       stat_add(c.item_stats, item, ST_BTOUCH, 1);
     }
     __syncwarp();
