@@ -1065,8 +1065,10 @@ struct SegHeadOut {
   }
 };
 
-// segments with more records than one update chunk go to the heavy list
+// segments with more records than one update chunk, or more voxel updates
+// than k_update_warp's shared-memory sort holds, go to the heavy list
 constexpr int UPD_T = 128;
+constexpr int kUwCap = 512;
 constexpr int kHotChain = 128;    // longer voxel chains of a heavy segment run as a warp each
 constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
@@ -1101,7 +1103,13 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
     // what the update kernels need first, in one 16-byte load
     c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
                               __float_as_int(c.maps[c.items[item].map].maxw));
-    if (b1 - b0 > UPD_T) {
+    bool heavy = b1 - b0 > UPD_T;
+    if (!heavy && (b1 - b0) * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates
+      int e = 0;
+      for (long long r = b0; r < b1; ++r) e += (int)(rv[r] & 31u);
+      heavy = e > kUwCap;
+    }
+    if (heavy) {
       unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_heavy), 1ull);
       c.heavy[k] = (int)j;
     }
@@ -1895,14 +1903,15 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
 }
 
 // ----------------------------------------------------------------------------
-// Light segments (up to UPD_T routing records), one warp each.  A segment's
-// records are the rays through its block in ascending point order; the
-// entries of one record are distinct voxels (a ray visits a voxel once).  An
-// entry's depth is the number of the segment's earlier entries (in point
-// order) that update its voxel, so the entries of one depth update distinct
-// voxels and the depths taken in ascending order give every voxel its
-// updates in point order: the reference's rule (tsdf_handler.cu:648-654)
-// applied as the sequential loop would.  A segment of at most kUwCap entries:
+// Light segments (up to UPD_T routing records and kUwCap voxel updates; the
+// others are on the heavy list), one warp each.  A segment's records are the
+// rays through its block in ascending point order; the entries of one record
+// are distinct voxels (a ray visits a voxel once).  An entry's depth is the
+// number of the segment's earlier entries (in point order) that update its
+// voxel, so the entries of one depth update distinct voxels and the depths
+// taken in ascending order give every voxel its updates in point order: the
+// reference's rule (tsdf_handler.cu:648-654) applied as the sequential loop
+// would.
 //   (A) the record values (four per lane) and an exclusive scan of their
 //       entry counts; every entry loaded flat, 32 per instruction, 16 in
 //       flight per lane; depths from a match over each 32 entries plus the
@@ -1914,14 +1923,10 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
 //   (C) the depths in order, each one's entries 32 at a time with no wait
 //       between them (their voxels are distinct).
 // On this workload that is a quarter of the warp steps of one record at a
-// time.  A longer segment marks its touched voxels, loads them 32
-// consecutive per instruction and applies its records one at a time, 16
-// records' entries held in registers.  The touched voxels are written back
-// at the end; the block's non-zero count moves by the touched voxels whose
-// weight left zero.  9 KB of shared memory per warp.
+// time.  The touched voxels are written back at the end; the block's
+// non-zero count moves by the touched voxels whose weight left zero.  9 KB
+// of shared memory per warp.
 constexpr int UW_T = 128;
-constexpr int kUwChunk = 16;  // records per register round (long segments)
-constexpr int kUwCap = 512;   // entries of a segment on the depth path (16 per lane)
 constexpr unsigned kUwNone = 0xFFFFFFFFu;
 
 struct __align__(16) UwWarp {
@@ -1931,19 +1936,8 @@ struct __align__(16) UwWarp {
   unsigned char cnt[kVoxelsPerBlock];  // per voxel: updates so far (zero between segments)
 };
 
-// The entries of records c0 .. c0 + kUwChunk - 1 (record i is rv4[i % 4] of
-// lane i / 4; lane l takes entry l of each, kBadLocal past its count).
-__device__ __forceinline__ void load_round(const Ctx& c, const unsigned (&rv4)[UPD_T / 32], int c0, int lane,
-                                           uint2 (&xs)[kUwChunk]) {
-#pragma unroll
-  for (int j = 0; j < kUwChunk; ++j) {
-    const unsigned v = __shfl_sync(kFull, rv4[j & 3], (c0 + j) >> 2);
-    xs[j] = lane < (int)(v & 31u) ? c.entries[(v >> 5) + lane] : make_uint2(0u, kBadLocal);
-  }
-}
-
 __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
-  static_assert(UPD_T == 128 && kUwChunk == 16 && kUwCap == 512, "record and entry layout of k_update_warp");
+  static_assert(UPD_T == 128 && kUwCap == 512, "record and entry layout of k_update_warp");
   __shared__ UwWarp s_warp[UW_T / 32];
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -1987,8 +1981,9 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
       if (lane >= o) incl += y;
     }
     const int n_ent = __shfl_sync(kFull, incl, 31);
+    if (n_ent > kUwCap) continue;  // on the heavy list (k_seg_classify counts the same way)
     int n_upd = 0, nz_old = 0, nz_new = 0, touched = 0;
-    if (n_ent <= kUwCap) {
+    {
       // ---- (A) entries flat, depths and places within depth
       unsigned* ebase = reinterpret_cast<unsigned*>(sm.sorted);          // [UPD_T]
       int* rpos = reinterpret_cast<int*>(sm.sorted) + UPD_T;             // [UPD_T]
@@ -2005,7 +2000,7 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
         xs[i] = make_uint2(0u, kBadLocal);
         if (f < n_ent) {
           int j = 0;
-#pragma unroll
+#pragma unroll 1
           for (int st = UPD_T / 2; st >= 1; st >>= 1)
             if (j + st < nrec && rpos[j + st] <= f) j += st;
           xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
@@ -2094,59 +2089,6 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
       }
 #pragma unroll
       for (int k = 0; k < UPD_T / 32; ++k) sm.lvl[32 * k + lane] = 0;
-    } else {
-      // ---- long segment: mark, load the touched voxels, one record at a time
-      uint2 xs[kUwChunk];
-      for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
-        load_round(c, rv4, c0, lane, xs);
-#pragma unroll
-        for (int j = 0; j < kUwChunk; ++j) {
-          const unsigned l = xs[j].y;
-          if (l != kBadLocal) ++n_upd, sm.cnt[l] = 1;
-        }
-      }
-      __syncwarp();
-#pragma unroll
-      for (int j0 = 0; j0 < kVoxelsPerBlock / 32; j0 += 8) {
-        float2 v[8];
-        bool t[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          t[k] = sm.cnt[32 * (j0 + k) + lane] != 0;
-          v[k] = t[k] ? gv2[32 * (j0 + k) + lane] : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (t[k]) sm.vox[32 * (j0 + k) + lane] = v[k], nz_old += v[k].y != 0.0f;
-      }
-      __syncwarp();
-      for (int c0 = 0; c0 < nrec; c0 += kUwChunk) {
-        load_round(c, rv4, c0, lane, xs);
-        const int m = min(kUwChunk, nrec - c0);
-#pragma unroll
-        for (int j = 0; j < kUwChunk; ++j) {
-          if (j < m) {
-            const uint2 x = xs[j];
-            if (x.y != kBadLocal) {
-              float2 v = sm.vox[x.y];
-              update_voxel(&v.x, &v.y, __uint_as_float(x.x), maxw);
-              sm.vox[x.y] = v;
-            }
-            __syncwarp();
-          }
-        }
-      }
-#pragma unroll 4
-      for (int j = 0; j < kVoxelsPerBlock / 32; ++j) {
-        const int l = 32 * j + lane;
-        if (sm.cnt[l]) {
-          const float2 v = sm.vox[l];
-          gv2[l] = v;
-          nz_new += v.y != 0.0f;
-          ++touched;
-          sm.cnt[l] = 0;
-        }
-      }
     }
     const int nz_delta = __reduce_add_sync(kFull, nz_new - nz_old);
     const unsigned upd = __reduce_add_sync(kFull, (unsigned)n_upd);
