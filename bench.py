@@ -598,7 +598,7 @@ def traffic_from_profiles(kernel: str, workload: str):
 
 # stage -> (kernels, unit counter in the per-step stats) for the roofline line
 STAGE_KERNELS = {
-    "update": (["k_hot_chains", "k_heavy_update", "k_update"], "blocks_touched"),
+    "update": (["k_hot_chains", "k_heavy_update", "k_update_warp"], "blocks_touched"),
     "publish": (["k_pub_write"], "published_blocks"),
     "ray_voxels": (["k_ray_voxels"], "n_points"),
     "ray_blocks": (["k_ray_blocks"], "n_points"),

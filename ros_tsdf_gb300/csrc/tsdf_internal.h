@@ -113,6 +113,8 @@ struct LaneCounters {
   unsigned long long q_voxels;
   unsigned long long q_update;
   unsigned long long q_update_warp;  // work queue of the light-segment warps
+  unsigned long long n_bcta;  // heavy segments updated by one CTA in shared memory
+  unsigned long long q_bcta;  // their work queue
   unsigned long long q_pubwrite;
   unsigned long long q_hot;      // work queue of the hot-chain kernel
   long long n_new;        // new keys appended
@@ -197,7 +199,8 @@ struct Ctx {
   int* enum_gc;                  // gc flags per enumerated slot
   int* pub_prefix;
   int* gc_prefix;
-  int* heavy;                    // segment ids of heavy segments
+  int* heavy;                    // segment ids of heavy segments (binned grid-wide)
+  int* bcta;                     // segment ids of heavy segments updated by one CTA
   float* bin_d;                  // heavy-segment bins (entry_cap floats)
   int* hchunk_base;              // [heavy] first chunk of each planned heavy segment
   int* hcnt;                     // [hchunk_cap][512] per-chunk voxel counts, then offsets

@@ -1069,6 +1069,11 @@ struct SegHeadOut {
 // than k_update_warp's shared-memory sort holds, go to the heavy list
 constexpr int UPD_T = 128;
 constexpr int kUwCap = 512;
+// heavy segments of at most kBcRec records and kBcCap voxel updates are
+// updated by one CTA in shared memory (k_update_warp's first phase); longer
+// ones are binned grid-wide (heavy_bins) and go to k_heavy_update / k_hot_chains
+constexpr int kBcRec = 1024;
+constexpr int kBcCap = 4096;
 constexpr int kHotChain = 128;    // longer voxel chains of a heavy segment run as a warp each
 constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
@@ -1081,38 +1086,66 @@ __device__ __forceinline__ void zero_masks(unsigned* m, int t) {
 
 
 
+__device__ __forceinline__ void push_heavy(const Ctx& c, long long j) {
+  const unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_heavy), 1ull);
+  c.heavy[k] = (int)j;
+}
+
 // Per segment: its batch item (the scan of the entry of its first record) and,
 // for segments longer than one update chunk, a place on the heavy list.
 __device__ void heavy_plan_cta(const Ctx& c);
 
 __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
   __shared__ long long s_pb[kMaxItems];
+  __shared__ int s_list[256];  // this round's segments whose update count is needed
+  __shared__ int s_nlist;
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
-  __syncthreads();
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned* rk = c.rec_key[rec_sel];
-  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nseg;
-       j += (long long)gridDim.x * blockDim.x) {
-    const long long b0 = c.seg_start[j];
-    const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
-    const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
-    c.seg_item[j] = item;
-    // what the update kernels need first, in one 16-byte load
-    c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
-                              __float_as_int(c.maps[c.items[item].map].maxw));
-    bool heavy = b1 - b0 > UPD_T;
-    if (!heavy && (b1 - b0) * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates
+  const int lane = threadIdx.x & 31;
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < nseg; base += (long long)gridDim.x * blockDim.x) {
+    if (threadIdx.x == 0) s_nlist = 0;
+    __syncthreads();
+    const long long j = base + threadIdx.x;
+    if (j < nseg) {
+      const long long b0 = c.seg_start[j];
+      const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+      const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+      c.seg_item[j] = item;
+      // what the update kernels need first, in one 16-byte load
+      c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
+                                __float_as_int(c.maps[c.items[item].map].maxw));
+      const long long n = b1 - b0;
+      if (n > kBcRec) {
+        push_heavy(c, j);
+      } else if (n * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates: count them below
+        s_list[atomicAdd(&s_nlist, 1)] = (int)j;
+      }
+    }
+    __syncthreads();
+    // one warp per listed segment: its update count from the record counts
+    for (int k = threadIdx.x >> 5; k < s_nlist; k += blockDim.x >> 5) {
+      const int sj = s_list[k];
+      const long long b0 = c.seg_start[sj];
+      const long long b1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
       int e = 0;
-      for (long long r = b0; r < b1; ++r) e += (int)(rv[r] & 31u);
-      heavy = e > kUwCap;
+      for (long long r = b0 + lane; r < b1; r += 32) e += (int)(rv[r] & 31u);
+      e = __reduce_add_sync(kFull, e);
+      if (lane == 0) {
+        if (b1 - b0 > UPD_T || e > kUwCap) {
+          if (e > kBcCap) {
+            push_heavy(c, sj);
+          } else {
+            const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
+            c.bcta[q] = sj;
+          }
+        }
+      }
     }
-    if (heavy) {
-      unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_heavy), 1ull);
-      c.heavy[k] = (int)j;
-    }
+    __syncthreads();
   }
   if (last_cta(&c.ctr->done_classify)) heavy_plan_cta(c);
 }
@@ -1936,12 +1969,174 @@ struct __align__(16) UwWarp {
   unsigned char cnt[kVoxelsPerBlock];  // per voxel: updates so far (zero between segments)
 };
 
+// Heavy segments of up to kBcRec records and kBcCap updates (k_seg_classify
+// lists them), one CTA each, before the CTA's warps turn to light segments.
+// The segment's updates are counted per voxel, the counts scanned into bin
+// offsets, and the updates placed into their voxel's bins in point order:
+// 128 updates per round in point order, a warp's rank from a match over its
+// 32 updates, the earlier warps' counts of the same voxel in the round, and
+// the voxel's running cursor.  Then one thread per voxel runs its chain
+// (the reference's rule, tsdf_handler.cu:648-654, in point order) from the
+// bins, reading and writing only the touched voxels.  30.8 KB of shared
+// memory, inside the light phase's 36 KB.
+struct BcSmem {
+  int rpos[kBcRec];                              // first flat update of each record
+  unsigned ebase[kBcRec];                        // entry offset of each record
+  float bins[kBcCap];                            // distances by voxel, point order within a voxel
+  int off[kVoxelsPerBlock + 1];                  // per voxel: first bin
+  int run[kVoxelsPerBlock];                      // per voxel: count, then placement cursor
+  unsigned char cw[UW_T / 32][kVoxelsPerBlock];  // per warp: its updates of a voxel in the round
+  int scan[32];
+  int red[3][UW_T / 32];
+  long long seg;
+};
+
+__device__ __forceinline__ int bc_record(const int* rpos, int nrec, int f) {
+  int j = 0;
+#pragma unroll 1
+  for (int st = kBcRec / 2; st >= 1; st >>= 1)
+    if (j + st < nrec && rpos[j + st] <= f) j += st;
+  return j;
+}
+
+__device__ __forceinline__ uint2 bc_entry(const Ctx& c, const BcSmem& sm, int nrec, int n_ent, int f) {
+  if (f >= n_ent) return make_uint2(0u, kBadLocal);
+  const int j = bc_record(sm.rpos, nrec, f);
+  return c.entries[sm.ebase[j] + (unsigned)(f - sm.rpos[j])];
+}
+
+__device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
+  constexpr int RPT = kBcRec / UW_T;  // records per thread
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const unsigned* rv = c.rec_val[rec_sel];
+  const long long nb = c.ctr->n_bcta;
+  for (;;) {
+    __syncthreads();
+    if (t == 0) sm.seg = (long long)atomicAdd(&c.ctr->q_bcta, 1ull);
+    __syncthreads();
+    const long long q = sm.seg;
+    if (q >= nb) break;
+    const int sj = c.bcta[q];
+    const int4 d = c.seg_desc[sj];
+    const int nrec = d.y - d.x;
+    const int item = c.seg_item[sj];
+    const float maxw = __int_as_float(d.w);
+    float2* gv2 = c.voxels + (long long)d.z * kVoxelsPerBlock;
+    // records RPT t .. RPT t + RPT - 1: entry bases and first flat updates
+    unsigned r8[RPT];
+    int pre[RPT], lsum = 0;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int i = RPT * t + k;
+      r8[k] = i < nrec ? rv[d.x + i] : 0u;
+      pre[k] = lsum;
+      lsum += (int)(r8[k] & 31u);
+    }
+    int n_ent;
+    const int ex = block_excl_scan(lsum, sm.scan, &n_ent);
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int i = RPT * t + k;
+      if (i < nrec) sm.rpos[i] = ex + pre[k], sm.ebase[i] = r8[k] >> 5;
+    }
+    for (int l = t; l < kVoxelsPerBlock; l += UW_T) sm.run[l] = 0;
+    reinterpret_cast<uint4*>(&sm.cw[0][0])[t] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    // per-voxel counts, four updates per thread in flight
+    for (int f0 = 0; f0 < n_ent; f0 += 4 * UW_T) {
+      uint2 x[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x[k] = bc_entry(c, sm, nrec, n_ent, f0 + k * UW_T + t);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (x[k].y != kBadLocal) atomicAdd(&sm.run[x[k].y], 1);
+    }
+    __syncthreads();
+    {
+      const int a0 = sm.run[4 * t], a1 = sm.run[4 * t + 1], a2 = sm.run[4 * t + 2], a3 = sm.run[4 * t + 3];
+      int tot;
+      const int e0 = block_excl_scan(a0 + a1 + a2 + a3, sm.scan, &tot);
+      sm.off[4 * t] = e0;
+      sm.off[4 * t + 1] = e0 + a0;
+      sm.off[4 * t + 2] = e0 + a0 + a1;
+      sm.off[4 * t + 3] = e0 + a0 + a1 + a2;
+      sm.run[4 * t] = e0;
+      sm.run[4 * t + 1] = e0 + a0;
+      sm.run[4 * t + 2] = e0 + a0 + a1;
+      sm.run[4 * t + 3] = e0 + a0 + a1 + a2;
+      if (t == 0) sm.off[kVoxelsPerBlock] = tot;
+    }
+    __syncthreads();
+    // placement in point order, UW_T updates per round, the next round's in flight
+    uint2 x = bc_entry(c, sm, nrec, n_ent, t);
+    for (int f0 = 0; f0 < n_ent; f0 += UW_T) {
+      const uint2 nx = bc_entry(c, sm, nrec, n_ent, f0 + UW_T + t);
+      const bool ok = x.y != kBadLocal;
+      const unsigned pv = __match_any_sync(kFull, ok ? x.y : (0x10000u | lane));
+      const bool lead = ok && (pv >> lane) == 1u;  // its voxel's last update in this warp
+      if (lead) sm.cw[w][x.y] = (unsigned char)__popc(pv);
+      __syncthreads();
+      if (ok) {
+        int pos = sm.run[x.y] + __popc(pv & lt);
+        for (int w2 = 0; w2 < w; ++w2) pos += sm.cw[w2][x.y];
+        sm.bins[pos] = __uint_as_float(x.x);
+      }
+      __syncthreads();
+      if (lead) {
+        atomicAdd(&sm.run[x.y], __popc(pv));
+        sm.cw[w][x.y] = 0;
+      }
+      x = nx;
+    }
+    __syncthreads();
+    // one thread per voxel: its chain from the bins
+    int nz = 0, touched = 0, upd = 0;
+    float2 v0[kVoxelsPerBlock / UW_T];
+#pragma unroll
+    for (int k = 0; k < kVoxelsPerBlock / UW_T; ++k) {
+      const int l = t + k * UW_T;
+      v0[k] = sm.off[l + 1] > sm.off[l] ? gv2[l] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < kVoxelsPerBlock / UW_T; ++k) {
+      const int l = t + k * UW_T;
+      const int b = sm.off[l], e = sm.off[l + 1];
+      if (e > b) {
+        float sdf = v0[k].x;
+        const float wv = apply_chain(&sdf, v0[k].y, sm.bins + b, e - b, maxw);
+        gv2[l] = make_float2(sdf, wv);
+        nz += (int)(wv != 0.0f) - (int)(v0[k].y != 0.0f);
+        ++touched;
+        upd += e - b;
+      }
+    }
+    nz = __reduce_add_sync(kFull, (unsigned)nz);
+    touched = __reduce_add_sync(kFull, (unsigned)touched);
+    upd = __reduce_add_sync(kFull, (unsigned)upd);
+    if (lane == 0) sm.red[0][w] = nz, sm.red[1][w] = touched, sm.red[2][w] = upd;
+    __syncthreads();
+    if (t == 0) {
+      int a = 0, b = 0, u = 0;
+      for (int k = 0; k < UW_T / 32; ++k) a += sm.red[0][k], b += sm.red[1][k], u += sm.red[2][k];
+      c.nnz[d.z] += a;
+      stat_add(c.item_stats, item, ST_UPD, u);
+      stat_add(c.item_stats, item, ST_DVOX, b);
+      stat_add(c.item_stats, item, ST_BTOUCH, 1);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
   static_assert(UPD_T == 128 && kUwCap == 512, "record and entry layout of k_update_warp");
-  __shared__ UwWarp s_warp[UW_T / 32];
+  static_assert(sizeof(BcSmem) <= sizeof(UwWarp) * (UW_T / 32), "the CTA phase fits the light phase's shared memory");
+  static_assert(kBcRec % UW_T == 0 && UW_T * 4 == kVoxelsPerBlock, "CTA phase layout");
+  __shared__ __align__(16) unsigned char s_raw[sizeof(UwWarp) * (UW_T / 32)];
+  block_update_cta(c, rec_sel, *reinterpret_cast<BcSmem*>(s_raw));
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  UwWarp& sm = s_warp[threadIdx.x >> 5];
+  UwWarp& sm = reinterpret_cast<UwWarp*>(s_raw)[threadIdx.x >> 5];
   reinterpret_cast<uint4*>(sm.cnt)[lane] = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
   for (int k = 0; k < UPD_T / 32; ++k) sm.lvl[32 * k + lane] = 0;

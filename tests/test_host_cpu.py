@@ -248,7 +248,7 @@ def test_bench_result_line_contract():
     rf = line["roofline"]
     for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
         assert k in rf, k
-    assert rf["stage"] == "update" and rf["kernel"] == "k_hot_chains+k_heavy_update+k_update"
+    assert rf["stage"] == "update" and rf["kernel"] == "k_hot_chains+k_heavy_update+k_update_warp"
     # the update stage's algorithmic bytes: 16 B per distinct voxel (read +
     # write) and 16 B per touched block's entry
     assert abs(rf["achieved"] - (16 * 1000 + 16 * 1000) / 0.18e-3 / 1e9) < 1e-9
