@@ -48,6 +48,7 @@
 // Float arithmetic uses explicit round-to-nearest intrinsics (no FMA
 // contraction) so every value matches the sequential CPU restatement bit for
 // bit.  Every loop that waits on another thread's progress is bounded.
+#include <cstddef>
 #include <cstdio>
 
 #include "tsdf_internal.h"
@@ -1985,7 +1986,7 @@ struct BcSmem {
   float bins[kBcCap];                            // distances by voxel, point order within a voxel
   int off[kVoxelsPerBlock + 1];                  // per voxel: first bin
   int run[kVoxelsPerBlock];                      // per voxel: count, then placement cursor
-  unsigned char cw[UW_T / 32][kVoxelsPerBlock];  // per warp: its updates of a voxel in the round
+  alignas(16) unsigned char cw[UW_T / 32][kVoxelsPerBlock];  // per warp: its updates of a voxel in the round (zeroed 16 B per thread)
   int scan[32];
   int red[3][UW_T / 32];
   long long seg;
@@ -2131,6 +2132,8 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
   static_assert(UPD_T == 128 && kUwCap == 512, "record and entry layout of k_update_warp");
   static_assert(sizeof(BcSmem) <= sizeof(UwWarp) * (UW_T / 32), "the CTA phase fits the light phase's shared memory");
   static_assert(kBcRec % UW_T == 0 && UW_T * 4 == kVoxelsPerBlock, "CTA phase layout");
+  static_assert(offsetof(BcSmem, cw) % 16 == 0 && offsetof(UwWarp, cnt) % 16 == 0 && sizeof(UwWarp) % 16 == 0,
+                "16-byte zeroing stores");
   __shared__ __align__(16) unsigned char s_raw[sizeof(UwWarp) * (UW_T / 32)];
   block_update_cta(c, rec_sel, *reinterpret_cast<BcSmem*>(s_raw));
   __syncthreads();
