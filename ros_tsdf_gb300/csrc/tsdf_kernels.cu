@@ -1075,6 +1075,7 @@ constexpr int kUwCap = 512;
 // ones are binned grid-wide (heavy_bins) and go to k_heavy_update / k_hot_chains
 constexpr int kBcRec = 1024;
 constexpr int kBcCap = 4096;
+constexpr int kBcBuckets = 13;  // chain lengths 1 .. kBcCap in log2 buckets
 constexpr int kHotChain = 128;    // longer voxel chains of a heavy segment run as a warp each
 constexpr int kLongChain = 2048;  // hot chains this long are dequeued first
 
@@ -1098,55 +1099,55 @@ __device__ void heavy_plan_cta(const Ctx& c);
 
 __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
   __shared__ long long s_pb[kMaxItems];
-  __shared__ int s_list[256];  // this round's segments whose update count is needed
-  __shared__ int s_nlist;
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
   const long long nseg = c.ctr->n_seg;
   const long long nrec = c.ctr->n_rec_live;
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned* rk = c.rec_key[rec_sel];
   const int lane = threadIdx.x & 31;
-  for (long long base = blockIdx.x * (long long)blockDim.x; base < nseg; base += (long long)gridDim.x * blockDim.x) {
-    if (threadIdx.x == 0) s_nlist = 0;
-    __syncthreads();
-    const long long j = base + threadIdx.x;
-    if (j < nseg) {
-      const long long b0 = c.seg_start[j];
-      const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
-      const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
-      c.seg_item[j] = item;
-      // what the update kernels need first, in one 16-byte load
-      c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
-                                __float_as_int(c.maps[c.items[item].map].maxw));
-      const long long n = b1 - b0;
-      if (n > kBcRec) {
-        push_heavy(c, j);
-      } else if (n * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates: count them below
-        s_list[atomicAdd(&s_nlist, 1)] = (int)j;
-      }
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per segment; 32 segments' bounds read at once
+  for (long long j0 = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; j0 < nseg; j0 += nwarps * 32) {
+    const long long jl = j0 + lane;
+    long long mb0 = 0, mb1 = 0;
+    if (jl < nseg) {
+      mb0 = c.seg_start[jl];
+      mb1 = (jl + 1 < nseg) ? c.seg_start[jl + 1] : nrec;
     }
-    __syncthreads();
-    // one warp per listed segment: its update count from the record counts
-    for (int k = threadIdx.x >> 5; k < s_nlist; k += blockDim.x >> 5) {
-      const int sj = s_list[k];
-      const long long b0 = c.seg_start[sj];
-      const long long b1 = (sj + 1 < nseg) ? c.seg_start[sj + 1] : nrec;
+    const int m = (int)min(32ll, nseg - j0);
+    for (int k = 0; k < m; ++k) {
+      const long long j = j0 + k;
+      const long long b0 = __shfl_sync(kFull, mb0, k);
+      const long long b1 = __shfl_sync(kFull, mb1, k);
+      const long long n = b1 - b0;
+      // the update count of a segment that may hold more than kUwCap updates
       int e = 0;
-      for (long long r = b0 + lane; r < b1; r += 32) e += (int)(rv[r] & 31u);
-      e = __reduce_add_sync(kFull, e);
-      if (lane == 0) {
-        if (b1 - b0 > UPD_T || e > kUwCap) {
-          if (e > kBcCap) {
-            push_heavy(c, sj);
-          } else {
-            const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
-            c.bcta[q] = sj;
-          }
+      if (n <= kBcRec && n * kUpdEntries > kUwCap) {
+        for (long long r = b0 + lane; r < b1; r += 256) {  // eight loads per lane in flight
+          unsigned v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = r + 32 * u < b1 ? rv[r + 32 * u] : 0u;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) e += (int)(v[u] & 31u);
+        }
+        e = __reduce_add_sync(kFull, e);
+      }
+      if (lane == k) {
+        const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+        c.seg_item[j] = item;
+        // what the update kernels need first, in one 16-byte load
+        c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
+                                  __float_as_int(c.maps[c.items[item].map].maxw));
+        if (n > kBcRec || e > kBcCap) {
+          push_heavy(c, j);
+        } else if (n > UPD_T || e > kUwCap) {
+          const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
+          c.bcta[q] = (int)j;
         }
       }
     }
-    __syncthreads();
   }
   if (last_cta(&c.ctr->done_classify)) heavy_plan_cta(c);
 }
@@ -1989,6 +1990,8 @@ struct BcSmem {
   alignas(16) unsigned char cw[UW_T / 32][kVoxelsPerBlock];  // per warp: its updates of a voxel in the round (zeroed 16 B per thread)
   int scan[32];
   int red[3][UW_T / 32];
+  int bk[kBcBuckets + 1];                        // chain-length buckets: counts, then cursors
+  unsigned short order[kVoxelsPerBlock];         // touched voxels, longest chains first
   long long seg;
 };
 
@@ -2091,19 +2094,51 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
       x = nx;
     }
     __syncthreads();
-    // one thread per voxel: its chain from the bins
-    int nz = 0, touched = 0, upd = 0;
-    float2 v0[kVoxelsPerBlock / UW_T];
+    // one thread per touched voxel: its chain from the bins.  The touched
+    // voxels are taken longest chains first (buckets of equal log2 length,
+    // then in any order), so that the lanes of a warp run chains of similar
+    // length
+    constexpr int VPT = kVoxelsPerBlock / UW_T;  // voxels per thread
+    if (t < kBcBuckets) sm.bk[t] = 0;
+    __syncthreads();
+    int bkt[VPT];
 #pragma unroll
-    for (int k = 0; k < kVoxelsPerBlock / UW_T; ++k) {
+    for (int k = 0; k < VPT; ++k) {
       const int l = t + k * UW_T;
-      v0[k] = sm.off[l + 1] > sm.off[l] ? gv2[l] : make_float2(0.f, 0.f);
+      const int n = sm.off[l + 1] - sm.off[l];
+      bkt[k] = n > 0 ? kBcBuckets - 1 - min(31 - __clz(n), kBcBuckets - 1) : -1;  // 0 = longest
+      if (n > 0) atomicAdd(&sm.bk[bkt[k]], 1);
+    }
+    __syncthreads();
+    if (t == 0) {
+      int run = 0;
+      for (int b = 0; b < kBcBuckets; ++b) {
+        const int v = sm.bk[b];
+        sm.bk[b] = run;
+        run += v;
+      }
+      sm.bk[kBcBuckets] = run;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < VPT; ++k)
+      if (bkt[k] >= 0) sm.order[atomicAdd(&sm.bk[bkt[k]], 1)] = (unsigned short)(t + k * UW_T);
+    __syncthreads();
+    const int n_touched = sm.bk[kBcBuckets];
+    int nz = 0, touched = 0, upd = 0;
+    int lv[VPT];
+    float2 v0[VPT];
+#pragma unroll
+    for (int k = 0; k < VPT; ++k) {
+      const int i = t + k * UW_T;
+      lv[k] = i < n_touched ? (int)sm.order[i] : -1;
+      v0[k] = lv[k] >= 0 ? gv2[lv[k]] : make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int k = 0; k < kVoxelsPerBlock / UW_T; ++k) {
-      const int l = t + k * UW_T;
-      const int b = sm.off[l], e = sm.off[l + 1];
-      if (e > b) {
+    for (int k = 0; k < VPT; ++k) {
+      const int l = lv[k];
+      if (l >= 0) {
+        const int b = sm.off[l], e = sm.off[l + 1];
         float sdf = v0[k].x;
         const float wv = apply_chain(&sdf, v0[k].y, sm.bins + b, e - b, maxw);
         gv2[l] = make_float2(sdf, wv);
