@@ -325,6 +325,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   TRY(dalloc(eng, &x.bin_d, entry_cap, tr));
   TRY(dalloc(eng, &x.heavy, rec_cap, tr));
   TRY(dalloc(eng, &x.bcta, rec_cap, tr));
+  TRY(dalloc(eng, &x.cand, rec_cap, tr));
   // heavy-block counting sort: every routing record can sit in a planned
   // heavy segment (dense scans at small voxel sizes put most blocks there)
   x.hchunk_cap = (int)std::min<long long>(rec_cap / 128 + 64, 1 << 30);

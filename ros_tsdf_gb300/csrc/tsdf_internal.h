@@ -114,6 +114,7 @@ struct LaneCounters {
   unsigned long long q_update;
   unsigned long long q_update_warp;  // work queue of the light-segment warps
   unsigned long long n_bcta;  // heavy segments updated by one CTA in shared memory
+  unsigned long long n_cand;  // segments whose update count k_seg_count sums
   unsigned long long q_bcta;  // their work queue
   unsigned long long q_pubwrite;
   unsigned long long q_hot;      // work queue of the hot-chain kernel
@@ -201,6 +202,7 @@ struct Ctx {
   int* gc_prefix;
   int* heavy;                    // segment ids of heavy segments (binned grid-wide)
   int* bcta;                     // segment ids of heavy segments updated by one CTA
+  int* cand;                     // segment ids whose update count decides their class
   float* bin_d;                  // heavy-segment bins (entry_cap floats)
   int* hchunk_base;              // [heavy] first chunk of each planned heavy segment
   int* hcnt;                     // [hchunk_cap][512] per-chunk voxel counts, then offsets

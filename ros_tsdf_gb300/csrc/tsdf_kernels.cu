@@ -1093,8 +1093,8 @@ __device__ __forceinline__ void push_heavy(const Ctx& c, long long j) {
   c.heavy[k] = (int)j;
 }
 
-// Per segment: its batch item (the scan of the entry of its first record) and,
-// for segments longer than one update chunk, a place on the heavy list.
+// Per segment: its batch item (the scan of the entry of its first record),
+// its descriptor and, where its record count decides, its class.
 __device__ void heavy_plan_cta(const Ctx& c);
 
 __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
@@ -1106,46 +1106,52 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
   const long long nrec = c.ctr->n_rec_live;
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned* rk = c.rec_key[rec_sel];
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nseg;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long b0 = c.seg_start[j];
+    const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+    const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+    c.seg_item[j] = item;
+    // what the update kernels need first, in one 16-byte load
+    c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
+                              __float_as_int(c.maps[c.items[item].map].maxw));
+    const long long n = b1 - b0;
+    if (n > kBcRec) {
+      push_heavy(c, j);
+    } else if (n * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates: k_seg_count counts them
+      const unsigned long long q = atomicAdd(&c.ctr->n_cand, 1ull);
+      c.cand[q] = (int)j;
+    }
+  }
+}
+
+// The segments k_seg_classify could not class by their record count alone:
+// one warp each sums their records' update counts (eight loads per lane in
+// flight) and lists them as CTA-heavy or grid-heavy (or leaves them light).
+// Its last CTA plans the grid-heavy segments' chunks.
+__global__ void __launch_bounds__(256) k_seg_count(Ctx c, int rec_sel) {
+  const long long ncand = c.ctr->n_cand;
+  const unsigned* rv = c.rec_val[rec_sel];
   const int lane = threadIdx.x & 31;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  // one warp per segment; 32 segments' bounds read at once
-  for (long long j0 = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; j0 < nseg; j0 += nwarps * 32) {
-    const long long jl = j0 + lane;
-    long long mb0 = 0, mb1 = 0;
-    if (jl < nseg) {
-      mb0 = c.seg_start[jl];
-      mb1 = (jl + 1 < nseg) ? c.seg_start[jl + 1] : nrec;
+  for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; k < ncand; k += nwarps) {
+    const int sj = c.cand[k];
+    const int4 d = c.seg_desc[sj];
+    int e = 0;
+    for (int r = d.x + lane; r < d.y; r += 256) {
+      unsigned v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = r + 32 * u < d.y ? rv[r + 32 * u] : 0u;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) e += (int)(v[u] & 31u);
     }
-    const int m = (int)min(32ll, nseg - j0);
-    for (int k = 0; k < m; ++k) {
-      const long long j = j0 + k;
-      const long long b0 = __shfl_sync(kFull, mb0, k);
-      const long long b1 = __shfl_sync(kFull, mb1, k);
-      const long long n = b1 - b0;
-      // the update count of a segment that may hold more than kUwCap updates
-      int e = 0;
-      if (n <= kBcRec && n * kUpdEntries > kUwCap) {
-        for (long long r = b0 + lane; r < b1; r += 256) {  // eight loads per lane in flight
-          unsigned v[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) v[u] = r + 32 * u < b1 ? rv[r + 32 * u] : 0u;
-#pragma unroll
-          for (int u = 0; u < 8; ++u) e += (int)(v[u] & 31u);
-        }
-        e = __reduce_add_sync(kFull, e);
-      }
-      if (lane == k) {
-        const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
-        c.seg_item[j] = item;
-        // what the update kernels need first, in one 16-byte load
-        c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
-                                  __float_as_int(c.maps[c.items[item].map].maxw));
-        if (n > kBcRec || e > kBcCap) {
-          push_heavy(c, j);
-        } else if (n > UPD_T || e > kUwCap) {
-          const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
-          c.bcta[q] = (int)j;
-        }
+    e = __reduce_add_sync(kFull, e);
+    if (lane == 0) {
+      if (e > kBcCap) {
+        push_heavy(c, sj);
+      } else if (d.y - d.x > UPD_T || e > kUwCap) {
+        const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
+        c.bcta[q] = sj;
       }
     }
   }
@@ -1158,8 +1164,8 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
 // bins, ordered by point index.  plan -> per-chunk voxel counts -> per-voxel
 // scan over chunks -> ordered placement.  Segments whose chunks exceed the
 // scratch capacity fall back to the single-CTA passes in k_update.  The plan
-// runs in the last CTA of k_seg_classify, which lists the heavy segments (it
-// reads the list through L2).
+// runs in the last CTA of k_seg_count; k_seg_classify and k_seg_count list
+// the heavy segments (the plan reads the list through L2).
 __device__ void heavy_plan_cta(const Ctx& c) {
   __shared__ int s_warp[32];
   const long long nh = __ldcg(&c.ctr->n_heavy);
@@ -1971,7 +1977,7 @@ struct __align__(16) UwWarp {
   unsigned char cnt[kVoxelsPerBlock];  // per voxel: updates so far (zero between segments)
 };
 
-// Heavy segments of up to kBcRec records and kBcCap updates (k_seg_classify
+// Heavy segments of up to kBcRec records and kBcCap updates (k_seg_count
 // lists them), one CTA each, before the CTA's warps turn to light segments.
 // The segment's updates are counted per voxel, the counts scanned into bin
 // offsets, and the updates placed into their voxel's bins in point order:
@@ -2214,7 +2220,7 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
       if (lane >= o) incl += y;
     }
     const int n_ent = __shfl_sync(kFull, incl, 31);
-    if (n_ent > kUwCap) continue;  // on the heavy list (k_seg_classify counts the same way)
+    if (n_ent > kUwCap) continue;  // a heavy segment (k_seg_count counts the same way)
     int n_upd = 0, nz_old = 0, nz_new = 0, touched = 0;
     {
       // ---- (A) entries flat, depths and places within depth
@@ -2986,7 +2992,8 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums, &c.ctr->n_seg, &c.ctr->done_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
   k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c, sel);
-  *launches += 4;
+  k_seg_count<<<lc.sm_count * 4, 256, 0, s>>>(c, sel);
+  *launches += 5;
 }
 
 void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
