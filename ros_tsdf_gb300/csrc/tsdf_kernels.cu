@@ -1994,6 +1994,8 @@ struct BcSmem {
   int off[kVoxelsPerBlock + 1];                  // per voxel: first bin
   int run[kVoxelsPerBlock];                      // per voxel: count, then placement cursor
   alignas(16) unsigned char cw[UW_T / 32][kVoxelsPerBlock];  // per warp: its updates of a voxel in the round (zeroed 16 B per thread)
+  unsigned wmask[kBcCap / 32];                   // per 32 flat updates: the records that start there
+  int wbase[kBcCap / 32];                        // per 32 flat updates: records starting before them
   int scan[32];
   int red[3][UW_T / 32];
   int bk[kBcBuckets + 1];                        // chain-length buckets: counts, then cursors
@@ -2001,17 +2003,12 @@ struct BcSmem {
   long long seg;
 };
 
-__device__ __forceinline__ int bc_record(const int* rpos, int nrec, int f) {
-  int j = 0;
-#pragma unroll 1
-  for (int st = kBcRec / 2; st >= 1; st >>= 1)
-    if (j + st < nrec && rpos[j + st] <= f) j += st;
-  return j;
-}
-
-__device__ __forceinline__ uint2 bc_entry(const Ctx& c, const BcSmem& sm, int nrec, int n_ent, int f) {
+// The update at flat index f of a segment: its record is the last one that
+// starts at or before f, found from the 32-bit start mask of f's window of 32
+// and the number of records starting before that window.
+__device__ __forceinline__ uint2 bc_entry(const Ctx& c, const BcSmem& sm, int n_ent, int f) {
   if (f >= n_ent) return make_uint2(0u, kBadLocal);
-  const int j = bc_record(sm.rpos, nrec, f);
+  const int j = sm.wbase[f >> 5] + __popc(sm.wmask[f >> 5] << (31 - (f & 31))) - 1;
   return c.entries[sm.ebase[j] + (unsigned)(f - sm.rpos[j])];
 }
 
@@ -2045,19 +2042,32 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
     }
     int n_ent;
     const int ex = block_excl_scan(lsum, sm.scan, &n_ent);
+    static_assert(kBcCap / 32 == UW_T, "one start-mask window per thread");
+    sm.wmask[t] = 0u;
+    __syncthreads();
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
       const int i = RPT * t + k;
-      if (i < nrec) sm.rpos[i] = ex + pre[k], sm.ebase[i] = r8[k] >> 5;
+      if (i < nrec) {  // every record holds at least one update, so its start is its own
+        const int f = ex + pre[k];
+        sm.rpos[i] = f;
+        sm.ebase[i] = r8[k] >> 5;
+        atomicOr(&sm.wmask[f >> 5], 1u << (f & 31));
+      }
     }
     for (int l = t; l < kVoxelsPerBlock; l += UW_T) sm.run[l] = 0;
     reinterpret_cast<uint4*>(&sm.cw[0][0])[t] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    {
+      int nstarts;
+      sm.wbase[t] = block_excl_scan(__popc(sm.wmask[t]), sm.scan, &nstarts);
+    }
     __syncthreads();
     // per-voxel counts, four updates per thread in flight
     for (int f0 = 0; f0 < n_ent; f0 += 4 * UW_T) {
       uint2 x[4];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) x[k] = bc_entry(c, sm, nrec, n_ent, f0 + k * UW_T + t);
+      for (int k = 0; k < 4; ++k) x[k] = bc_entry(c, sm, n_ent, f0 + k * UW_T + t);
 #pragma unroll
       for (int k = 0; k < 4; ++k)
         if (x[k].y != kBadLocal) atomicAdd(&sm.run[x[k].y], 1);
@@ -2079,9 +2089,9 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
     }
     __syncthreads();
     // placement in point order, UW_T updates per round, the next round's in flight
-    uint2 x = bc_entry(c, sm, nrec, n_ent, t);
+    uint2 x = bc_entry(c, sm, n_ent, t);
     for (int f0 = 0; f0 < n_ent; f0 += UW_T) {
-      const uint2 nx = bc_entry(c, sm, nrec, n_ent, f0 + UW_T + t);
+      const uint2 nx = bc_entry(c, sm, n_ent, f0 + UW_T + t);
       const bool ok = x.y != kBadLocal;
       const unsigned pv = __match_any_sync(kFull, ok ? x.y : (0x10000u | lane));
       const bool lead = ok && (pv >> lane) == 1u;  // its voxel's last update in this warp
@@ -2224,24 +2234,41 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
     int n_upd = 0, nz_old = 0, nz_new = 0, touched = 0;
     {
       // ---- (A) entries flat, depths and places within depth
+      // a flat update's record: the last one starting at or before it, from
+      // the start mask of its window of 32 and the records starting before
       unsigned* ebase = reinterpret_cast<unsigned*>(sm.sorted);          // [UPD_T]
       int* rpos = reinterpret_cast<int*>(sm.sorted) + UPD_T;             // [UPD_T]
+      unsigned* wmask = reinterpret_cast<unsigned*>(sm.vox);             // [kUwCap / 32]
+      if (lane < kUwCap / 32) wmask[lane] = 0u;
+      __syncwarp();
 #pragma unroll
       for (int k = 0; k < UPD_T / 32; ++k) {
-        ebase[4 * lane + k] = rv4[k] >> 5;
-        rpos[4 * lane + k] = incl - lsum + pre[k];
+        const int i = 4 * lane + k;
+        if (i < nrec) {  // every record holds at least one update
+          const int f = incl - lsum + pre[k];
+          ebase[i] = rv4[k] >> 5;
+          rpos[i] = f;
+          atomicOr(&wmask[f >> 5], 1u << (f & 31));
+        }
       }
       __syncwarp();
+      const unsigned my_mask = lane < kUwCap / 32 ? wmask[lane] : 0u;
+      int wb = __popc(my_mask);
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, wb, o);
+        if (lane >= o) wb += y;
+      }
+      wb -= __popc(my_mask);  // records starting before window `lane`
       uint2 xs[kUwCap / 32];
 #pragma unroll
       for (int i = 0; i < kUwCap / 32; ++i) {
         const int f = 32 * i + lane;
+        const unsigned wm = __shfl_sync(kFull, my_mask, i);
+        const int wbi = __shfl_sync(kFull, wb, i);
         xs[i] = make_uint2(0u, kBadLocal);
         if (f < n_ent) {
-          int j = 0;
-#pragma unroll 1
-          for (int st = UPD_T / 2; st >= 1; st >>= 1)
-            if (j + st < nrec && rpos[j + st] <= f) j += st;
+          const int j = wbi + __popc(wm << (31 - lane)) - 1;
           xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
         }
       }
