@@ -144,6 +144,7 @@ struct PtrInfo {
 struct Lane {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr, side2 = nullptr;
+  cudaStream_t cond_stream = nullptr;  // conditional-node bodies are captured here
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
   Ctx ctx{};
   // device scratch
@@ -274,6 +275,8 @@ LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_p
   lc.ev_join = L.ev_join;
   lc.ev_join2 = L.ev_join2;
   for (int i = 0; i < 3; ++i) lc.ev_branch[i] = nullptr;
+  lc.capturing = 0;
+  lc.cond_stream = L.cond_stream;
   return lc;
 }
 
@@ -282,6 +285,7 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   CK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&L.side2, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&L.cond_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&L.ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&L.ev_join, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&L.ev_join2, cudaEventDisableTiming));
@@ -395,6 +399,7 @@ void lane_free(Lane& L) {
   if (L.ev_join2) cudaEventDestroy(L.ev_join2);
   if (L.side) cudaStreamDestroy(L.side);
   if (L.side2) cudaStreamDestroy(L.side2);
+  if (L.cond_stream) cudaStreamDestroy(L.cond_stream);
   if (L.stream) cudaStreamDestroy(L.stream);
   L = Lane();
 }
@@ -402,8 +407,9 @@ void lane_free(Lane& L) {
 // Enqueue the pipeline of one step on the lane's stream (used directly or
 // inside a graph capture).  Returns the number of kernel launches.
 long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
-                           bool timed) {
+                           bool timed, bool capturing) {
   LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout);
+  lc.capturing = capturing ? 1 : 0;
   if (timed)
     for (int i = 0; i < 3; ++i) lc.ev_branch[i] = L.ev_branch[i];
   long long n = 0;
@@ -424,7 +430,7 @@ tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_
   const bool timed = eng->stage_timing;
   L.timed = timed;
   if (eng->cfg.no_graphs) {
-    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed);
+    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed, false);
     CK(cudaGetLastError());
     return TSDF_OK;
   }
@@ -434,7 +440,7 @@ tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_
   if (it == L.graphs.end()) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
-    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed);
+    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed, true);
     cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     cudaGraphExec_t ex = nullptr;
@@ -676,6 +682,8 @@ tsdf_status finish_batch(tsdf_engine* eng, Lane& L, int n, tsdf_scan_result* res
   }
   for (int m : L.maps) eng->maps[m].in_flight = false;
   L.busy = false;
+  // kernels a conditional node of the step's graph did not launch
+  if (!eng->cfg.no_graphs) eng->launches -= L.h_ctr->skipped_launches;
   tsdf_status worst = TSDF_OK;
   if (L.h_ctr->error) {
     std::string what;

@@ -144,6 +144,8 @@ struct LaneCounters {
   unsigned done_classify;
   unsigned done_gcapply;
   int error;              // bit flags, see ERR_*
+  int rank_small;         // the new keys were sorted by k_gather_ranks' last CTA: the rank passes do nothing
+  int skipped_launches;   // kernels of the step's graph that a conditional node did not launch
   int pad;
 };
 
@@ -250,6 +252,10 @@ struct LaunchCfg {
   // stage-timed steps only (null otherwise): the end of each update-stage
   // branch, recorded on its own stream (hot chains, heavy bins, light warps)
   cudaEvent_t ev_branch[3];
+  // set while the step is captured into a graph: stages may add conditional
+  // nodes, whose bodies are captured on cond_stream
+  int capturing;
+  cudaStream_t cond_stream;
 };
 
 cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice

@@ -677,8 +677,10 @@ constexpr int RS_IPT = 8;
 constexpr int RS_TILE = RS_T * RS_IPT;
 
 __global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* keys, const long long* n_ptr, long long cap,
-                                                  int shift, unsigned key_limit, int* hist, int max_tiles) {
+                                                  int shift, unsigned key_limit, int* hist, int max_tiles,
+                                                  const int* skip) {
   __shared__ int s_h[256];
+  if (skip && *skip) return;
   const long long n = min(*n_ptr, cap);
   const long long ntiles = (n + RS_TILE - 1) / RS_TILE;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -699,7 +701,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* keys, const lo
 
 // One CTA per digit: exclusive scan of the digit's row over tiles.
 __global__ void __launch_bounds__(1024) k_rs_scan_digits(int* hist, const long long* n_ptr, long long cap,
-                                                         int max_tiles, int* digit_tot) {
+                                                         int max_tiles, int* digit_tot, const int* skip) {
+  if (skip && *skip) return;
   __shared__ int s_warp[32];
   const long long n = min(*n_ptr, cap);
   const long long ntiles = (n + RS_TILE - 1) / RS_TILE;
@@ -726,7 +729,8 @@ __global__ void __launch_bounds__(1024) k_rs_scan_digits(int* hist, const long l
 __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* kin, const unsigned* vin, unsigned* kout,
                                                      unsigned* vout, const long long* n_ptr, long long cap,
                                                      int shift, unsigned key_limit, const int* hist,
-                                                     int max_tiles, const int* digit_tot, long long* n_out) {
+                                                     int max_tiles, const int* digit_tot, long long* n_out, const int* skip) {
+  if (skip && *skip) return;
   __shared__ int s_base[256];
   __shared__ __align__(16) unsigned short s_cell[RS_IPT][RS_T / 32][256];
   __shared__ int s_warp[32];
@@ -797,7 +801,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* kin, const 
 
 void radix_sort(const Ctx& c, unsigned* const* keys, unsigned* const* vals, const long long* n_first,
                 unsigned key_limit, long long* n_live, long long cap, int passes, int max_tiles, int sm_count,
-                cudaStream_t s, long long* launches) {
+                cudaStream_t s, long long* launches, const int* skip = nullptr) {
   const int grid = sm_count * 4;
   for (int p = 0; p < passes; ++p) {
     const unsigned* kin = keys[p & 1];
@@ -806,10 +810,10 @@ void radix_sort(const Ctx& c, unsigned* const* keys, unsigned* const* vals, cons
     unsigned* vout = vals[(p + 1) & 1];
     const long long* np = p == 0 ? n_first : n_live;
     const unsigned lim = p == 0 ? key_limit : 0xFFFFFFFFu;
-    k_rs_hist<<<grid, RS_T, 0, s>>>(kin, np, cap, p * kRadixBits, lim, c.hist, max_tiles);
-    k_rs_scan_digits<<<256, 1024, 0, s>>>(c.hist, np, cap, max_tiles, c.digit_tot);
+    k_rs_hist<<<grid, RS_T, 0, s>>>(kin, np, cap, p * kRadixBits, lim, c.hist, max_tiles, skip);
+    k_rs_scan_digits<<<256, 1024, 0, s>>>(c.hist, np, cap, max_tiles, c.digit_tot, skip);
     k_rs_scatter<<<grid, RS_T, 0, s>>>(kin, vin, kout, vout, np, cap, p * kRadixBits, lim, c.hist, max_tiles,
-                                       c.digit_tot, p == 0 ? n_live : nullptr);
+                                       c.digit_tot, p == 0 ? n_live : nullptr, skip);
     *launches += 3;
   }
 }
@@ -819,8 +823,16 @@ void radix_sort(const Ctx& c, unsigned* const* keys, unsigned* const* vals, cons
 // The new keys' (first-touch rank, hash entry) pairs for the rank sort; the
 // CTA that finishes last also writes every item's first index among the new
 // keys (exclusive prefix of the per-item new-key counts).
-__global__ void __launch_bounds__(256) k_gather_ranks(Ctx c) {
+// Up to this many new keys are sorted by rank in k_gather_ranks' last CTA
+// (bitonic, in shared memory); the radix passes then do nothing, and inside a
+// graph a conditional node does not launch them.
+constexpr int kSmallRank = 2048;
+
+__global__ void __launch_bounds__(256) k_gather_ranks(Ctx c, cudaGraphConditionalHandle cond, int use_cond,
+                                                      int rank_sel, int pass_launches) {
   __shared__ int s_warp[32];
+  __shared__ unsigned s_k[kSmallRank];
+  __shared__ unsigned s_v[kSmallRank];
   const long long n = min(c.ctr->n_new, c.rank_cap);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     unsigned e = c.newlist[i];
@@ -837,6 +849,42 @@ __global__ void __launch_bounds__(256) k_gather_ranks(Ctx c) {
     const int ex = block_excl_scan(v, s_warp, &tot);
     if (i < ni) c.item_i[i * II_COUNT + II_NEW_BASE] = (int)(carry + ex);
     carry += tot;
+  }
+  const bool small = n <= kSmallRank;
+  if (small) {
+    // ranks are distinct (one per point route), below 0xFFFFFFFF, which pads
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      s_k[i] = i < n ? __ldcg(&c.rank_key[0][i]) : 0xFFFFFFFFu;
+      s_v[i] = i < n ? __ldcg(&c.rank_val[0][i]) : 0u;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const unsigned a = s_k[i], b2 = s_k[ixj];
+            if ((a > b2) == ((i & k) == 0)) {
+              s_k[i] = b2, s_k[ixj] = a;
+              const unsigned t = s_v[i];
+              s_v[i] = s_v[ixj], s_v[ixj] = t;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) c.rank_key[rank_sel][i] = s_k[i], c.rank_val[rank_sel][i] = s_v[i];
+  }
+  if (threadIdx.x == 0) {
+    c.ctr->rank_small = small ? 1 : 0;
+    c.ctr->n_rank_live = n;
+    if (use_cond) {
+      cudaGraphSetConditional(cond, small ? 0u : 1u);
+      if (small) c.ctr->skipped_launches += pass_launches;
+    }
   }
 }
 
@@ -2986,10 +3034,42 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c);
+  const int sel = lc.rank_passes & 1;
+  const int pass_launches = 3 * lc.rank_passes;
+  if (!lc.capturing) {
+    // eager: the passes see rank_small and return at once when the small sort ran
+    k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c, cudaGraphConditionalHandle{}, 0, sel, pass_launches);
+    *launches += 1;
+    radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
+               lc.rank_passes, c.max_tiles_rank, lc.sm_count, s, launches, &c.ctr->rank_small);
+    return;
+  }
+  // in a graph: the passes are the body of a conditional node that the last
+  // CTA of k_gather_ranks switches off when it sorted the keys itself
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr);
+  cudaGraphConditionalHandle cond{};
+  cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault);
+  k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c, cond, 1, sel, pass_launches);
   *launches += 1;
+  cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  cudaStreamBeginCaptureToGraph(lc.cond_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
-             lc.rank_passes, c.max_tiles_rank, lc.sm_count, s, launches);
+             lc.rank_passes, c.max_tiles_rank, lc.sm_count, lc.cond_stream, launches, &c.ctr->rank_small);
+  cudaGraph_t captured = nullptr;
+  cudaStreamEndCapture(lc.cond_stream, &captured);
+  cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
