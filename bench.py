@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--serving-s", type=float, default=2.0,
                     help="seconds of the serving64 Poisson trace replayed served and plain (0: skip)")
     ap.add_argument("--serving-only", action="store_true", help="run only the serving64 replay and print it")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch every kernel directly (no CUDA graph): for ncu, which cannot profile the kernels "
+                         "of a graph with conditional nodes")
     ap.add_argument("--sdf-mode", type=int, default=0, choices=[0, 1],
                     help="0: every update applied in point order (bit-exact); 1: voxels with more than 128 updates "
                          "in a step as one affine-map composition (weights exact, sdf within 1e-5 T)")
@@ -280,7 +283,7 @@ def run_ours(args, rank, world, local, pg):
         return Engine(device=local, max_maps=max(64, len(specs)), pool_blocks=pool, max_batch_points=max_pts,
                       max_publish=cap * len(specs), bucket_size=args.bucket_size, ray_chunk=args.ray_chunk,
                       ray_threads=args.ray_threads, max_routes=max(8, max(s.params.routes() for s in specs)),
-                      sdf_mode=args.sdf_mode, **kw)
+                      sdf_mode=args.sdf_mode, graphs=not args.no_graphs, **kw)
 
     # ---- value: device-resident inputs and outputs, CUDA-event device time
     eng = new_engine()
@@ -702,7 +705,8 @@ def result_line(args, r: dict, world: int, tuned, peak: float, peak_kind: str) -
         "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded lidar scans; stand-in for the reference's private AirSim data)",
         "config": workload_config(args.workload, r["specs"], r["timed_pts"] / n),
-        "method": {"l2": "flushed (512 MiB write) between timed steps", "graph": "one CUDA graph per step",
+        "method": {"l2": "flushed (512 MiB write) between timed steps", "graph": ("kernels launched directly (--no-graphs)" if getattr(args, "no_graphs", False)
+                           else "one CUDA graph per step (the rank sort's passes in a conditional node)"),
                    "sdf_mode": args.sdf_mode,
                    "parity_bar": ("block/publish sets, counters and weights exact; sdf bit-exact" if args.sdf_mode == 0
                                   else "block/publish sets, counters and weights exact; sdf within 1e-5 T"),

@@ -1019,7 +1019,6 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
       const long long ebase = g * (long long)VS;
       unsigned long long cur = kEmptyKey;
       int run = -1, run_slot = -1, run_start = 0, run_cnt = 0, j = 0;
-      float blx = 0.f, bly = 0.f, blz = 0.f;
       unsigned route_ovf = 0, missing = 0, bad = 0;
       while (true) {
         float x, y, z;
@@ -1028,10 +1027,22 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
         if (!__ballot_sync(kFull, has)) break;
         unsigned long long bkey = 0;
         float fbx = 0.f, fby = 0.f, fbz = 0.f;
+        // Below 2^20 cells from the origin on every axis, the float
+        // arithmetic of the block and in-block index of a voxel centre
+        // (cell k: centre (k + 1/2) vs, relative error 2^-23) is exact to
+        // the cell, so the block is k >> 3 and the index in the block k & 7;
+        // farther out the reference's float path runs as written.
+        const bool exact = has && abs(kx) < (1 << 20) && abs(ky) < (1 << 20) && abs(kz) < (1 << 20);
         if (has) {
-          fbx = floorf(fmul(x, scale_b));
-          fby = floorf(fmul(y, scale_b));
-          fbz = floorf(fmul(z, scale_b));
+          if (exact) {
+            fbx = (float)(kx >> 3);
+            fby = (float)(ky >> 3);
+            fbz = (float)(kz >> 3);
+          } else {
+            fbx = floorf(fmul(x, scale_b));
+            fby = floorf(fmul(y, scale_b));
+            fbz = floorf(fmul(z, scale_b));
+          }
           bkey = pack_key((int)fbx, (int)fby, (int)fbz);
         }
         const bool newrun = has && bkey != cur;
@@ -1045,10 +1056,6 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
           run_slot = -1;
           run_start = j;
           run_cnt = 0;
-          // block centre and bottom-left corner (tsdf_handler.cu:612-624)
-          blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
-          bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
-          blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
         }
         const bool need = newrun && run < rmax;
         const unsigned nm = __ballot_sync(kFull, need);
@@ -1071,14 +1078,22 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
             ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
           } else {
             // getLocalVoxelIndex (tsdf_handler.cu:507-512)
-            float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
-            float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
-            float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
             unsigned local = kBadLocal;
-            if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
-              local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
-            else
-              ++bad;
+            if (exact) {
+              local = (unsigned)((kx & 7) + (ky & 7) * 8 + (kz & 7) * 64);
+            } else {
+              // block centre and bottom-left corner (tsdf_handler.cu:612-624)
+              const float blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
+              const float bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
+              const float blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
+              float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
+              float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
+              float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
+              if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
+                local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
+              else
+                ++bad;
+            }
             const float d = distance_update(x, y, z, px, py, pz, ox, oy, oz);
             ent[ebase + j] = make_uint2(__float_as_uint(d), local);
             ++run_cnt;
