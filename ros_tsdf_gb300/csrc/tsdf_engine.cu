@@ -418,10 +418,10 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
                                   stage_alloc,      stage_ray_voxels,  stage_route_sort,  stage_heavy_bins,
                                   stage_update,     stage_publish,     stage_gc};
   for (int i = 0; i < STAGE_COUNT; ++i) {
-    if (timed) cudaEventRecordWithFlags(L.ev_stage[i], L.stream, cudaEventRecordExternal);
+    if (timed) record_timing_event(L.ev_stage[i], L.stream, capturing);
     stages[i](L.ctx, lc, L.stream, &n);
   }
-  if (timed) cudaEventRecordWithFlags(L.ev_stage[STAGE_COUNT], L.stream, cudaEventRecordExternal);
+  if (timed) record_timing_event(L.ev_stage[STAGE_COUNT], L.stream, capturing);
   return n;
 }
 

@@ -258,6 +258,13 @@ struct LaunchCfg {
   cudaStream_t cond_stream;
 };
 
+// An event for device timing: inside a graph capture it must be an external
+// record node (a plain record would only order the capture); outside one a
+// plain record.
+inline cudaError_t record_timing_event(cudaEvent_t ev, cudaStream_t s, bool capturing) {
+  return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal) : cudaEventRecord(ev, s);
+}
+
 cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice
 void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);
 void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);

@@ -3138,11 +3138,11 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   cudaStreamWaitEvent(lc.side2, lc.ev_fork, 0);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
-  if (lc.ev_branch[0]) cudaEventRecordWithFlags(lc.ev_branch[0], lc.side2, cudaEventRecordExternal);
+  if (lc.ev_branch[0]) record_timing_event(lc.ev_branch[0], lc.side2, lc.capturing);
   k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
-  if (lc.ev_branch[1]) cudaEventRecordWithFlags(lc.ev_branch[1], lc.side, cudaEventRecordExternal);
+  if (lc.ev_branch[1]) record_timing_event(lc.ev_branch[1], lc.side, lc.capturing);
   k_update_warp<<<lc.sm_count * 8, UW_T, 0, s>>>(c, sel);
-  if (lc.ev_branch[2]) cudaEventRecordWithFlags(lc.ev_branch[2], s, cudaEventRecordExternal);
+  if (lc.ev_branch[2]) record_timing_event(lc.ev_branch[2], s, lc.capturing);
   k_update<<<lc.sm_count * 2, UPD_T, 0, s>>>(c, sel);
   cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);

@@ -539,9 +539,12 @@ def test_pinned_inputs_staged_by_kernel_match_oracle(built):
             assert_state_equal(eng, mids[i], orcs[i], specs[i].heap_blocks, voxels=(i < 2))
 
 
-def test_step_timing_modes(built):
+@pytest.mark.parametrize("graphs", [True, False])
+def test_step_timing_modes(built, graphs):
     """Timing mode 2 records one device interval per step (no events inside
-    the graph); mode 1 also fills the per-stage times; results are the same."""
+    the graph); mode 1 also fills the per-stage times and the update stage's
+    branch times; results are the same.  With kernels launched directly too
+    (the timing events are then plain records)."""
     from ros_tsdf_gb300 import Engine, workloads as W
 
     spec = W.plain_small(seed=5, heap_blocks=1 << 12)
@@ -549,7 +552,7 @@ def test_step_timing_modes(built):
     scans = [src.scan(k) for k in range(4)]
     outs = []
     for mode in (2, 1):
-        with Engine(max_maps=2, pool_blocks=1 << 12, max_batch_points=1 << 14) as eng:
+        with Engine(max_maps=2, pool_blocks=1 << 12, max_batch_points=1 << 14, graphs=graphs) as eng:
             mid = eng.create_map(spec.params, spec.heap_blocks)
             eng.set_stage_timing(mode)
             res = [eng.integrate(mid, *sc, pub_cap=1 << 16) for sc in scans]
@@ -560,6 +563,8 @@ def test_step_timing_modes(built):
                 assert all(v == (0.0, 0) for v in st.values())
             else:
                 assert all(v[1] == 4 for v in st.values()) and sum(v[0] for v in st.values()) > 0
+                br = eng.update_branch_times()
+                assert br["steps"] == 4 and min(br["hot_chains"], br["heavy"], br["light"]) > 0
             eng.reset_stage_times()
             assert eng.step_times() == (0.0, 0)
             outs.append([(r.count, r.pos.copy(), r.data.copy()) for r in res])
