@@ -410,6 +410,16 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
                            bool timed, bool capturing) {
   LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout);
   lc.capturing = capturing ? 1 : 0;
+  lc.cond_rank = cudaGraphConditionalHandle{};
+  lc.cond_rec = cudaGraphConditionalHandle{};
+  if (capturing) {
+    // conditional handles of the graph being captured, default 1 (run) at every launch
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &g, nullptr, nullptr, nullptr);
+    cudaGraphConditionalHandleCreate(&lc.cond_rank, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphConditionalHandleCreate(&lc.cond_rec, g, 1, cudaGraphCondAssignDefault);
+  }
   if (timed)
     for (int i = 0; i < 3; ++i) lc.ev_branch[i] = L.ev_branch[i];
   long long n = 0;
@@ -501,7 +511,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   ItemDev* items = reinterpret_cast<ItemDev*>(L.h_desc + sizeof(BatchHdr));
   std::memset(hdr, 0, sizeof(BatchHdr));
   long long total = 0, bytes = 0, pub_staged = 0;
-  long long lo = -1, hi = 0;
+  long long slot_total = 0;  // record keys are slot numbers below the batch's heap capacities
   int rank_stride = 1, rec_stride = 1, vox_stride = 1;
   L.staged.clear();
   L.maps.clear();
@@ -529,8 +539,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     rank_stride = std::max(rank_stride, m.dev.amax);
     rec_stride = std::max(rec_stride, m.dev.rmax);
     vox_stride = std::max(vox_stride, m.dev.vmax);
-    lo = lo < 0 ? m.dev.heap_base : std::min(lo, m.dev.heap_base);
-    hi = std::max(hi, m.dev.heap_base + m.dev.heap_cap);
+    slot_total += m.dev.heap_cap;
   }
   if (total > c.max_batch_points)
     return fail(eng, TSDF_ERR_CAPACITY, "batch has " + std::to_string(total) + " points; capacity " +
@@ -624,13 +633,14 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
     return fail(eng, TSDF_ERR_CAPACITY, "voxel-update entries exceed capacity");
   hdr->total_points = total;
   hdr->rec_total = total * rec_stride;
-  hdr->key_lo = lo;
   hdr->rec_key_limit = kRecSentinel;
   hdr->stage_chunks = chunks;
   const unsigned long long rank_range = (unsigned long long)std::max<long long>(total, 1) * rank_stride;
   if (rank_range >= 0xFFFFFFFFull) return fail(eng, TSDF_ERR_CAPACITY, "rank range exceeds 32 bits");
   const int rank_passes = std::max(1, (bits_for(rank_range) + kRadixBits - 1) / kRadixBits);
-  const int rec_passes = std::max(1, (bits_for((unsigned long long)(hi - lo)) + kRadixBits - 1) / kRadixBits);
+  // passes for the largest possible slot number; k_alloc skips the last one
+  // when the maps' high waters leave its digit empty
+  const int rec_passes = std::max(1, (bits_for((unsigned long long)slot_total) + kRadixBits - 1) / kRadixBits);
   L.step_timed = eng->timing != 0;
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[0], L.stream));
   CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr), cudaMemcpyHostToDevice, L.stream));

@@ -101,7 +101,6 @@ struct BatchHdr {
   int vox_stride;      // max voxel-DDA cap over items (entry = g * stride + j)
   long long total_points;
   long long rec_total;        // total_points * rec_stride
-  long long key_lo;           // record key = physical slot - key_lo
   unsigned rec_key_limit;     // record keys >= this are empty routes
   int pad1;
   long long stage_chunks;     // staging chunks of pinned host inputs (k_stage_points)
@@ -146,7 +145,9 @@ struct LaneCounters {
   int error;              // bit flags, see ERR_*
   int rank_small;         // the new keys were sorted by k_gather_ranks' last CTA: the rank passes do nothing
   int skipped_launches;   // kernels of the step's graph that a conditional node did not launch
-  int pad;
+  int rec_skip_last;      // the record sort's last pass has nothing to do (k_alloc)
+  int rec_sel;            // which record buffer holds the sorted records (k_alloc)
+  int pad[3];
 };
 
 enum { ERR_HASH_FULL = 1, ERR_SPIN = 2, ERR_CAPACITY = 4 };
@@ -256,6 +257,8 @@ struct LaunchCfg {
   // nodes, whose bodies are captured on cond_stream
   int capturing;
   cudaStream_t cond_stream;
+  cudaGraphConditionalHandle cond_rank;  // the rank sort's passes run (k_gather_ranks sets it)
+  cudaGraphConditionalHandle cond_rec;   // the record sort's last pass runs (k_alloc sets it)
 };
 
 // An event for device timing: inside a graph capture it must be an external

@@ -799,23 +799,53 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* kin, const 
   }
 }
 
+void radix_pass(const Ctx& c, unsigned* const* keys, unsigned* const* vals, const long long* n_first,
+                unsigned key_limit, long long* n_live, long long cap, int p, int max_tiles, int sm_count,
+                cudaStream_t s, long long* launches, const int* skip) {
+  const int grid = sm_count * 4;
+  const unsigned* kin = keys[p & 1];
+  const unsigned* vin = vals[p & 1];
+  unsigned* kout = keys[(p + 1) & 1];
+  unsigned* vout = vals[(p + 1) & 1];
+  const long long* np = p == 0 ? n_first : n_live;
+  const unsigned lim = p == 0 ? key_limit : 0xFFFFFFFFu;
+  k_rs_hist<<<grid, RS_T, 0, s>>>(kin, np, cap, p * kRadixBits, lim, c.hist, max_tiles, skip);
+  k_rs_scan_digits<<<256, 1024, 0, s>>>(c.hist, np, cap, max_tiles, c.digit_tot, skip);
+  k_rs_scatter<<<grid, RS_T, 0, s>>>(kin, vin, kout, vout, np, cap, p * kRadixBits, lim, c.hist, max_tiles,
+                                     c.digit_tot, p == 0 ? n_live : nullptr, skip);
+  *launches += 3;
+}
+
 void radix_sort(const Ctx& c, unsigned* const* keys, unsigned* const* vals, const long long* n_first,
                 unsigned key_limit, long long* n_live, long long cap, int passes, int max_tiles, int sm_count,
                 cudaStream_t s, long long* launches, const int* skip = nullptr) {
-  const int grid = sm_count * 4;
-  for (int p = 0; p < passes; ++p) {
-    const unsigned* kin = keys[p & 1];
-    const unsigned* vin = vals[p & 1];
-    unsigned* kout = keys[(p + 1) & 1];
-    unsigned* vout = vals[(p + 1) & 1];
-    const long long* np = p == 0 ? n_first : n_live;
-    const unsigned lim = p == 0 ? key_limit : 0xFFFFFFFFu;
-    k_rs_hist<<<grid, RS_T, 0, s>>>(kin, np, cap, p * kRadixBits, lim, c.hist, max_tiles, skip);
-    k_rs_scan_digits<<<256, 1024, 0, s>>>(c.hist, np, cap, max_tiles, c.digit_tot, skip);
-    k_rs_scatter<<<grid, RS_T, 0, s>>>(kin, vin, kout, vout, np, cap, p * kRadixBits, lim, c.hist, max_tiles,
-                                       c.digit_tot, p == 0 ? n_live : nullptr, skip);
-    *launches += 3;
-  }
+  for (int p = 0; p < passes; ++p)
+    radix_pass(c, keys, vals, n_first, key_limit, n_live, cap, p, max_tiles, sm_count, s, launches, skip);
+}
+
+// Inside a graph capture on s: an IF node on cond after the work captured so
+// far, its body captured from body(stream) on lc.cond_stream; s's later work
+// follows the node.
+template <class F>
+void capture_if(const LaunchCfg& lc, cudaStream_t s, cudaGraphConditionalHandle cond, F body) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+  cudaStreamBeginCaptureToGraph(lc.cond_stream, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                cudaStreamCaptureModeThreadLocal);
+  body(lc.cond_stream);
+  cudaGraph_t captured = nullptr;
+  cudaStreamEndCapture(lc.cond_stream, &captured);
+  cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
 }
 
 // ----------------------------------------------------------------------------
@@ -890,7 +920,8 @@ __global__ void __launch_bounds__(256) k_gather_ranks(Ctx c, cudaGraphConditiona
 
 // One warp per new block, in first-touch order: pop the free list, resolve
 // the pending entry, zero the 4 KiB block (the reference's new VoxelBlock()).
-__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel) {
+__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, cudaGraphConditionalHandle cond, int use_cond,
+                                               int rec_passes) {
   __shared__ long long s_pb[kMaxItems];
   __shared__ int s_warp[32];
   const BatchHdr h = *c.hdr;
@@ -958,7 +989,18 @@ __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel) {
     }
     carry += tot;
   }
-  if (threadIdx.x == 0) c.ctr->n_enum = carry;
+  if (threadIdx.x == 0) {
+    c.ctr->n_enum = carry;
+    // record keys are slot numbers below carry: the sort's last 8-bit pass
+    // is needed only when some key reaches its digit
+    const bool last = rec_passes > 1 && carry > (1ll << (kRadixBits * (rec_passes - 1)));
+    c.ctr->rec_skip_last = rec_passes > 1 && !last ? 1 : 0;
+    c.ctr->rec_sel = (rec_passes - (c.ctr->rec_skip_last ? 1 : 0)) & 1;
+    if (use_cond) {
+      cudaGraphSetConditional(cond, last ? 1u : 0u);
+      if (!last && rec_passes > 1) c.ctr->skipped_launches += 3;
+    }
+  }
 }
 
 // ----------------------------------------------------------------------------
@@ -1009,7 +1051,7 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
       if (valid) dda.init(seg, m.vs, m.scale_v, m.rs_v, m.half_vs, m.vmax);
       const HEntry* tab = c.hash + m.hash_base;
       const unsigned mask = m.hash_mask;
-      const long long kbase = m.heap_base - h.key_lo;
+      const long long kbase = c.item_i[item * II_COUNT + II_SLOT_BASE];  // the item's first slot number
       // per-map constants and the origin in registers: the loop's stores
       // could alias the map and item records as far as the compiler knows
       const float scale_b = m.scale_b, rs_b = m.rs_b, half_bs = m.half_bs, vs = m.vs, r_vs = m.r_vs;
@@ -1019,6 +1061,7 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
       const long long ebase = g * (long long)VS;
       unsigned long long cur = kEmptyKey;
       int run = -1, run_slot = -1, run_start = 0, run_cnt = 0, j = 0;
+      float blx = 0.f, bly = 0.f, blz = 0.f;
       unsigned route_ovf = 0, missing = 0, bad = 0;
       while (true) {
         float x, y, z;
@@ -1027,22 +1070,10 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
         if (!__ballot_sync(kFull, has)) break;
         unsigned long long bkey = 0;
         float fbx = 0.f, fby = 0.f, fbz = 0.f;
-        // Below 2^20 cells from the origin on every axis, the float
-        // arithmetic of the block and in-block index of a voxel centre
-        // (cell k: centre (k + 1/2) vs, relative error 2^-23) is exact to
-        // the cell, so the block is k >> 3 and the index in the block k & 7;
-        // farther out the reference's float path runs as written.
-        const bool exact = has && abs(kx) < (1 << 20) && abs(ky) < (1 << 20) && abs(kz) < (1 << 20);
         if (has) {
-          if (exact) {
-            fbx = (float)(kx >> 3);
-            fby = (float)(ky >> 3);
-            fbz = (float)(kz >> 3);
-          } else {
-            fbx = floorf(fmul(x, scale_b));
-            fby = floorf(fmul(y, scale_b));
-            fbz = floorf(fmul(z, scale_b));
-          }
+          fbx = floorf(fmul(x, scale_b));
+          fby = floorf(fmul(y, scale_b));
+          fbz = floorf(fmul(z, scale_b));
           bkey = pack_key((int)fbx, (int)fby, (int)fbz);
         }
         const bool newrun = has && bkey != cur;
@@ -1056,6 +1087,10 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
           run_slot = -1;
           run_start = j;
           run_cnt = 0;
+          // block centre and bottom-left corner (tsdf_handler.cu:612-624)
+          blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
+          bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
+          blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
         }
         const bool need = newrun && run < rmax;
         const unsigned nm = __ballot_sync(kFull, need);
@@ -1078,22 +1113,14 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
             ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
           } else {
             // getLocalVoxelIndex (tsdf_handler.cu:507-512)
+            float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
+            float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
+            float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
             unsigned local = kBadLocal;
-            if (exact) {
-              local = (unsigned)((kx & 7) + (ky & 7) * 8 + (kz & 7) * 64);
-            } else {
-              // block centre and bottom-left corner (tsdf_handler.cu:612-624)
-              const float blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
-              const float bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
-              const float blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
-              float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
-              float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
-              float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
-              if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
-                local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
-              else
-                ++bad;
-            }
+            if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
+              local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
+            else
+              ++bad;
             const float d = distance_update(x, y, z, px, py, pz, ox, oy, oz);
             ent[ebase + j] = make_uint2(__float_as_uint(d), local);
             ++run_cnt;
@@ -1119,8 +1146,13 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
 
 // segment heads of the sorted records
 struct SegHeadIn {
-  const unsigned* k;
-  __device__ int operator()(long long i) const { return (i == 0 || k[i] != k[i - 1]) ? 1 : 0; }
+  const unsigned* k0;
+  const unsigned* k1;
+  const int* sel;  // which of the two holds the sorted keys (k_alloc sets it)
+  __device__ int operator()(long long i) const {
+    const unsigned* k = *sel ? k1 : k0;
+    return (i == 0 || k[i] != k[i - 1]) ? 1 : 0;
+  }
 };
 struct SegHeadOut {
   int* seg_start;
@@ -1160,7 +1192,8 @@ __device__ __forceinline__ void push_heavy(const Ctx& c, long long j) {
 // its descriptor and, where its record count decides, its class.
 __device__ void heavy_plan_cta(const Ctx& c);
 
-__global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(256) k_seg_classify(Ctx c) {
+  const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   __shared__ long long s_pb[kMaxItems];
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
@@ -1176,8 +1209,11 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
     const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
     c.seg_item[j] = item;
     // what the update kernels need first, in one 16-byte load
-    c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)(h.key_lo + rk[b0]),
-                              __float_as_int(c.maps[c.items[item].map].maxw));
+    // record keys number the batch's slots (each map's below its high water,
+    // after the maps before it): back to the physical slot
+    const MapDev& m = c.maps[c.items[item].map];
+    const long long phys = m.heap_base + (long long)rk[b0] - c.item_i[item * II_COUNT + II_SLOT_BASE];
+    c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)phys, __float_as_int(m.maxw));
     const long long n = b1 - b0;
     if (n > kBcRec) {
       push_heavy(c, j);
@@ -1192,7 +1228,8 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c, int rec_sel) {
 // one warp each sums their records' update counts (eight loads per lane in
 // flight) and lists them as CTA-heavy or grid-heavy (or leaves them light).
 // Its last CTA plans the grid-heavy segments' chunks.
-__global__ void __launch_bounds__(256) k_seg_count(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(256) k_seg_count(Ctx c) {
+  const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   const long long ncand = c.ctr->n_cand;
   const unsigned* rv = c.rec_val[rec_sel];
   const int lane = threadIdx.x & 31;
@@ -1300,7 +1337,8 @@ __device__ __forceinline__ int load_chunk_entries(const Ctx& c, const unsigned* 
   return ne;
 }
 
-__global__ void __launch_bounds__(UPD_T) k_heavy_count(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(UPD_T) k_heavy_count(Ctx c) {
+  const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   __shared__ float s_d[UPD_T * kUpdEntries];
   __shared__ unsigned short s_l[UPD_T * kUpdEntries];
   __shared__ int s_cnt[kVoxelsPerBlock];
@@ -1337,7 +1375,7 @@ __global__ void __launch_bounds__(UPD_T) k_heavy_count(Ctx c, int rec_sel) {
 constexpr int HS_T = 256;
 constexpr int kScanWarpChunks = 16;  // longer segments: k_heavy_scan_large
 
-__global__ void __launch_bounds__(HS_T) k_heavy_scan(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(HS_T) k_heavy_scan(Ctx c) {
   const int lane = threadIdx.x & 31;
   const int np = (int)c.ctr->n_hplanned;
   const long long nch = c.ctr->n_hchunks;
@@ -1393,7 +1431,6 @@ __global__ void __launch_bounds__(HS_T) k_heavy_scan(Ctx c, int rec_sel) {
     int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
     int ex = incl - lsum;
     unsigned hot_bits = 0;  // bit i: voxel V*lane+i went on the hot list
-    long long b0 = -1;
 #pragma unroll
     for (int i = 0; i < V; ++i) {
       vo[V * lane + i] = ex;
@@ -1401,12 +1438,11 @@ __global__ void __launch_bounds__(HS_T) k_heavy_scan(Ctx c, int rec_sel) {
         const bool lng = run[i] >= kLongChain;
         const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
         if (idx < half) {
-          if (b0 < 0) b0 = c.seg_start[c.heavy[h]];
           const int item = c.seg_item[c.heavy[h]];
           HotChain hc;
           hc.bin = base + (unsigned long long)ex;
           hc.n = run[i];
-          hc.phys = (int)(c.hdr->key_lo + c.rec_key[rec_sel][b0]);
+          hc.phys = c.seg_desc[c.heavy[h]].z;
           hc.local = V * lane + i;
           hc.maxw = c.maps[c.items[item].map].maxw;
           c.hot[(lng ? 0 : half) + idx] = hc;
@@ -1424,7 +1460,7 @@ __global__ void __launch_bounds__(HS_T) k_heavy_scan(Ctx c, int rec_sel) {
 
 // The same for segments of more than kScanWarpChunks chunks: one CTA of 512
 // threads per segment, one thread per voxel, eight chunk counts in flight.
-__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan_large(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan_large(Ctx c) {
   __shared__ int s_warp[32];
   __shared__ unsigned long long s_base;
   __shared__ int s_fit;
@@ -1474,12 +1510,11 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan_large(Ctx c, int
       const bool lng = run >= kLongChain;
       const long long idx = (long long)atomicAdd(lng ? &c.ctr->n_hot_long : &c.ctr->n_hot_short, 1ull);
       if (idx < half) {
-        const long long b0 = c.seg_start[c.heavy[h]];
         const int item = c.seg_item[c.heavy[h]];
         HotChain hc;
         hc.bin = s_base + (unsigned long long)ex;
         hc.n = run;
-        hc.phys = (int)(c.hdr->key_lo + c.rec_key[rec_sel][b0]);
+        hc.phys = c.seg_desc[c.heavy[h]].z;
         hc.local = l;
         hc.maxw = c.maps[c.items[item].map].maxw;
         c.hot[(lng ? 0 : half) + idx] = hc;
@@ -1492,7 +1527,8 @@ __global__ void __launch_bounds__(kVoxelsPerBlock) k_heavy_scan_large(Ctx c, int
   }
 }
 
-__global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(UPD_T) k_heavy_place(Ctx c) {
+  const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   __shared__ float s_d[UPD_T * kUpdEntries];
   __shared__ unsigned short s_l[UPD_T * kUpdEntries];
   __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];  // word-major, as in k_update
@@ -1869,7 +1905,8 @@ __global__ void __launch_bounds__(128) k_hot_chains(Ctx c) {
 // earlier chunks' counts); pass 2 runs one chain per voxel.  Only the touched
 // voxels are read and written, and the block's non-zero count moves by the
 // touched voxels whose weight left zero.
-__global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c) {
+  const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   // record bit masks per voxel, word-major (word w covers records 32w..32w+31)
   // so that 16-byte accesses of four consecutive voxels hit distinct banks
   __shared__ __align__(16) unsigned s_mask[UPD_T / 32][kVoxelsPerBlock];
@@ -2242,7 +2279,8 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
   }
 }
 
-__global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c) {
+  const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   static_assert(UPD_T == 128 && kUwCap == 512, "record and entry layout of k_update_warp");
   static_assert(sizeof(BcSmem) <= sizeof(UwWarp) * (UW_T / 32), "the CTA phase fits the light phase's shared memory");
   static_assert(kBcRec % UW_T == 0 && UW_T * 4 == kVoxelsPerBlock, "CTA phase layout");
@@ -2450,7 +2488,7 @@ constexpr int HU_T = kVoxelsPerBlock;
 constexpr int kRound = 8;
 constexpr int kHuSmem = (HU_T / 32) * kRound * 33 * (int)sizeof(float4);
 
-__global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c, int rec_sel) {
+__global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c) {
   extern __shared__ __align__(16) float4 s_dyn[];
   __shared__ short s_fb[kVoxelsPerBlock];
   __shared__ int s_nfb;
@@ -2458,13 +2496,10 @@ __global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c, int rec_sel) {
   const int l = threadIdx.x, lane = l & 31, warp = l >> 5;
   float4 (*tile)[33] = reinterpret_cast<float4 (*)[33]>(s_dyn + warp * kRound * 33);
   const int np = (int)c.ctr->n_hplanned;
-  const BatchHdr hd = *c.hdr;
-  const unsigned* rk = c.rec_key[rec_sel];
   for (int h = blockIdx.x; h < np; h += gridDim.x) {
     if (!c.hfit[h]) continue;  // k_update's fallback passes take it
     const int j = c.heavy[h];
-    const long long b0 = c.seg_start[j];
-    const long long phys = hd.key_lo + rk[b0];
+    const long long phys = c.seg_desc[j].z;
     const int item = c.seg_item[j];
     const float maxw = c.maps[c.items[item].map].maxw;
     const int* vo = c.hvoff + (long long)h * (kVoxelsPerBlock + 1);
@@ -3051,44 +3086,23 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int sel = lc.rank_passes & 1;
   const int pass_launches = 3 * lc.rank_passes;
-  if (!lc.capturing) {
-    // eager: the passes see rank_small and return at once when the small sort ran
-    k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c, cudaGraphConditionalHandle{}, 0, sel, pass_launches);
-    *launches += 1;
-    radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
-               lc.rank_passes, c.max_tiles_rank, lc.sm_count, s, launches, &c.ctr->rank_small);
-    return;
-  }
-  // in a graph: the passes are the body of a conditional node that the last
-  // CTA of k_gather_ranks switches off when it sorted the keys itself
-  cudaStreamCaptureStatus st;
-  cudaGraph_t g = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t nd = 0;
-  cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr);
-  cudaGraphConditionalHandle cond{};
-  cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault);
-  k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c, cond, 1, sel, pass_launches);
+  k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing, sel, pass_launches);
   *launches += 1;
-  cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd);
-  cudaGraphNodeParams np = {};
-  np.type = cudaGraphNodeTypeConditional;
-  np.conditional.handle = cond;
-  np.conditional.type = cudaGraphCondTypeIf;
-  np.conditional.size = 1;
-  cudaGraphNode_t node = nullptr;
-  cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
-  cudaGraph_t body = np.conditional.phGraph_out[0];
-  cudaStreamBeginCaptureToGraph(lc.cond_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-  radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
-             lc.rank_passes, c.max_tiles_rank, lc.sm_count, lc.cond_stream, launches, &c.ctr->rank_small);
-  cudaGraph_t captured = nullptr;
-  cudaStreamEndCapture(lc.cond_stream, &captured);
-  cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  auto passes = [&](cudaStream_t st) {
+    radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
+               lc.rank_passes, c.max_tiles_rank, lc.sm_count, st, launches, &c.ctr->rank_small);
+  };
+  // in a graph the passes are the body of a conditional node that the last
+  // CTA of k_gather_ranks switches off when it sorted the keys itself;
+  // launched directly they see rank_small and return at once
+  if (lc.capturing)
+    capture_if(lc, s, lc.cond_rank, passes);
+  else
+    passes(s);
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1);
+  k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.cond_rec, lc.capturing, lc.rec_passes);
   *launches += 1;
 }
 
@@ -3105,25 +3119,35 @@ void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  radix_sort(c, c.rec_key, c.rec_val, &c.hdr->rec_total, kRecSentinel, &c.ctr->n_rec_live, c.rec_cap,
-             lc.rec_passes, c.max_tiles_rec, lc.sm_count, s, launches);
-  const int sel = lc.rec_passes & 1;
-  SegHeadIn fin{c.rec_key[sel]};
+  // record keys number the batch's slots (k_alloc counts them): every pass
+  // but the last, then the last only when a key reaches its digit
+  const int P = lc.rec_passes;
+  auto pass = [&](int p, cudaStream_t st, const int* skip) {
+    radix_pass(c, c.rec_key, c.rec_val, &c.hdr->rec_total, kRecSentinel, &c.ctr->n_rec_live, c.rec_cap, p,
+               c.max_tiles_rec, lc.sm_count, st, launches, skip);
+  };
+  for (int p = 0; p + 1 < P; ++p) pass(p, s, nullptr);
+  if (P == 1)
+    pass(0, s, nullptr);
+  else if (lc.capturing)
+    capture_if(lc, s, lc.cond_rec, [&](cudaStream_t st) { pass(P - 1, st, &c.ctr->rec_skip_last); });
+  else
+    pass(P - 1, s, &c.ctr->rec_skip_last);
+  SegHeadIn fin{c.rec_key[0], c.rec_key[1], &c.ctr->rec_sel};
   SegHeadOut fout{c.seg_start};
   const int grid = lc.sm_count * 2;
   k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums, &c.ctr->n_seg, &c.ctr->done_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
-  k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c, sel);
-  k_seg_count<<<lc.sm_count * 4, 256, 0, s>>>(c, sel);
+  k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c);
+  k_seg_count<<<lc.sm_count * 4, 256, 0, s>>>(c);
   *launches += 5;
 }
 
 void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  const int sel = lc.rec_passes & 1;
-  k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c, sel);
-  k_heavy_scan<<<lc.sm_count * 8, HS_T, 0, s>>>(c, sel);
-  k_heavy_scan_large<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c, sel);
-  k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c, sel);
+  k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c);
+  k_heavy_scan<<<lc.sm_count * 8, HS_T, 0, s>>>(c);
+  k_heavy_scan_large<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c);
+  k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c);
   *launches += 4;
 }
 
@@ -3133,17 +3157,16 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   // sort's capacity) touch disjoint voxels: the first two are forked onto
   // the lane's side streams, launched before k_update so the chains start at
   // once, and all three join before the publish stage
-  const int sel = lc.rec_passes & 1;
   cudaEventRecord(lc.ev_fork, s);
   cudaStreamWaitEvent(lc.side2, lc.ev_fork, 0);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
   if (lc.ev_branch[0]) record_timing_event(lc.ev_branch[0], lc.side2, lc.capturing);
-  k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c, sel);
+  k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c);
   if (lc.ev_branch[1]) record_timing_event(lc.ev_branch[1], lc.side, lc.capturing);
-  k_update_warp<<<lc.sm_count * 8, UW_T, 0, s>>>(c, sel);
+  k_update_warp<<<lc.sm_count * 8, UW_T, 0, s>>>(c);
   if (lc.ev_branch[2]) record_timing_event(lc.ev_branch[2], s, lc.capturing);
-  k_update<<<lc.sm_count * 2, UPD_T, 0, s>>>(c, sel);
+  k_update<<<lc.sm_count * 2, UPD_T, 0, s>>>(c);
   cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);
   cudaStreamWaitEvent(s, lc.ev_join2, 0);
