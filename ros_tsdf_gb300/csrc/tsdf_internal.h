@@ -147,7 +147,8 @@ struct LaneCounters {
   int skipped_launches;   // kernels of the step's graph that a conditional node did not launch
   int rec_skip_last;      // the record sort's last pass has nothing to do (k_alloc)
   int rec_sel;            // which record buffer holds the sorted records (k_alloc)
-  int pad[3];
+  int gc_skip;            // no block to collect this step (k_enum_flags)
+  int pad[2];
 };
 
 enum { ERR_HASH_FULL = 1, ERR_SPIN = 2, ERR_CAPACITY = 4 };
@@ -259,6 +260,7 @@ struct LaunchCfg {
   cudaStream_t cond_stream;
   cudaGraphConditionalHandle cond_rank;  // the rank sort's passes run (k_gather_ranks sets it)
   cudaGraphConditionalHandle cond_rec;   // the record sort's last pass runs (k_alloc sets it)
+  cudaGraphConditionalHandle cond_gc;    // the collect passes run (k_enum_flags sets it)
 };
 
 // An event for device timing: inside a graph capture it must be an external

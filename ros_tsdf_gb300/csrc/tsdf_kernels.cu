@@ -631,9 +631,10 @@ __device__ __forceinline__ long long scan_tile_sums(int* tile_sums, long long nt
 // Tile sums, then (in the CTA that finishes last) their exclusive scan and
 // the total: the reduce and top levels of the scan in one launch.
 template <class F>
-__global__ void __launch_bounds__(SC_T) k_scan_reduce(F f, const long long* n_ptr, int* tile_sums,
+__global__ void __launch_bounds__(SC_T) k_scan_reduce(F f_in, const long long* n_ptr, int* tile_sums,
                                                       long long* total_out, unsigned* done) {
   __shared__ int s_warp[32];
+  const F f = f_in.bind();
   const long long n = *n_ptr;
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -653,8 +654,9 @@ __global__ void __launch_bounds__(SC_T) k_scan_reduce(F f, const long long* n_pt
 }
 
 template <class F, class O>
-__global__ void __launch_bounds__(SC_T) k_scan_apply(F f, O o, const long long* n_ptr, const int* tile_offs) {
+__global__ void __launch_bounds__(SC_T) k_scan_apply(F f_in, O o, const long long* n_ptr, const int* tile_offs) {
   __shared__ int s_warp[32];
+  const F f = f_in.bind();
   const long long n = *n_ptr;
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -1149,10 +1151,14 @@ struct SegHeadIn {
   const unsigned* k0;
   const unsigned* k1;
   const int* sel;  // which of the two holds the sorted keys (k_alloc sets it)
-  __device__ int operator()(long long i) const {
-    const unsigned* k = *sel ? k1 : k0;
-    return (i == 0 || k[i] != k[i - 1]) ? 1 : 0;
+  const unsigned* k = nullptr;
+  // the kernels bind once, before their loops: the buffer is read once
+  __device__ SegHeadIn bind() const {
+    SegHeadIn b = *this;
+    b.k = *sel ? k1 : k0;
+    return b;
   }
+  __device__ int operator()(long long i) const { return (i == 0 || k[i] != k[i - 1]) ? 1 : 0; }
 };
 struct SegHeadOut {
   int* seg_start;
@@ -2628,7 +2634,7 @@ __device__ __forceinline__ int find_item_i(const int* base, int n, long long e) 
 // voxels to publish, tile_sums3: blocks to collect; zeroed at step start),
 // and the CTA that finishes last scans both: the reduce and top levels of the
 // publish and gc scans in this one launch.
-__global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
+__global__ void __launch_bounds__(256) k_enum_flags(Ctx c, cudaGraphConditionalHandle cond_gc, int use_cond) {
   __shared__ int s_sb[kMaxItems];
   __shared__ int s_warp[32];
   const BatchHdr h = *c.hdr;
@@ -2676,7 +2682,18 @@ __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
     if (threadIdx.x == 0) {
       c.ctr->scan_total = tp;
       c.ctr->scan_total2 = tg;
+      // no block left the collect radius: the collect passes have nothing to
+      // do (a conditional node does not launch them; launched directly they
+      // return at once), and the block counts stand
+      c.ctr->gc_skip = tg == 0 ? 1 : 0;
+      if (use_cond) {
+        cudaGraphSetConditional(cond_gc, tg == 0 ? 0u : 1u);
+        if (tg == 0) c.ctr->skipped_launches += 2;
+      }
     }
+    if (tg == 0)
+      for (int i = threadIdx.x; i < c.hdr->n_items; i += blockDim.x)
+        c.item_stats[i * ST_COUNT + ST_BC] = c.mctr[c.items[i].map].block_count;
   }
 }
 
@@ -2687,8 +2704,10 @@ __device__ void copyout_plan_cta(const Ctx& c, int* s_warp);
 
 __global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, const int* flags, int* prefix, const int* tile_offs,
                                                      const long long* total, int base_field, int count_field,
-                                                     int stat_field, unsigned* done, int plan_copyout) {
+                                                     int stat_field, unsigned* done, int plan_copyout,
+                                                     const int* skip) {
   __shared__ int s_warp[32];
+  if (skip && *skip) return;
   const long long n = c.ctr->n_enum;
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -2915,6 +2934,7 @@ __global__ void __launch_bounds__(256) k_pub_copyout(Ctx c, int part) {
 // gc apply: free_list push in ascending slot order, entry tombstoned
 __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
   __shared__ int s_sb[kMaxItems];
+  if (c.ctr->gc_skip) return;  // k_enum_flags found nothing to collect
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
@@ -3176,9 +3196,9 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
-  k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c);
+  k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.cond_gc, lc.capturing);
   k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_cnt, c.pub_prefix, c.tile_sums2, &c.ctr->scan_total, II_PUB_BASE, -1,
-                                     ST_PUB, &c.ctr->done_pub, lc.copyout);
+                                     ST_PUB, &c.ctr->done_pub, lc.copyout, nullptr);
   *launches += 2;
   if (!lc.copyout) {
     k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c, -1);
@@ -3204,10 +3224,16 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
 
 void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
-  k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_gc, c.gc_prefix, c.tile_sums3, &c.ctr->scan_total2, II_GC_BASE, II_GC_N,
-                                     -1, &c.ctr->done_gc, 0);
-  k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
-  *launches += 2;
+  auto collect = [&](cudaStream_t st) {
+    k_enum_apply<<<grid, SC_T, 0, st>>>(c, c.enum_gc, c.gc_prefix, c.tile_sums3, &c.ctr->scan_total2, II_GC_BASE,
+                                        II_GC_N, -1, &c.ctr->done_gc, 0, &c.ctr->gc_skip);
+    k_gc_apply<<<lc.sm_count * 4, 256, 0, st>>>(c, lc.bucket_size);
+    *launches += 2;
+  };
+  if (lc.capturing)
+    capture_if(lc, s, lc.cond_gc, collect);
+  else
+    collect(s);
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
   k_step_report<<<1, 256, 0, s>>>(c);
   *launches += 1;
