@@ -411,16 +411,12 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
   LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout);
   lc.capturing = capturing ? 1 : 0;
   lc.cond_rank = cudaGraphConditionalHandle{};
-  lc.cond_rec = cudaGraphConditionalHandle{};
-  lc.cond_gc = cudaGraphConditionalHandle{};
   if (capturing) {
-    // conditional handles of the graph being captured, default 1 (run) at every launch
+    // the conditional handle of the graph being captured, default 1 (run) at every launch
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
     cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &g, nullptr, nullptr, nullptr);
     cudaGraphConditionalHandleCreate(&lc.cond_rank, g, 1, cudaGraphCondAssignDefault);
-    cudaGraphConditionalHandleCreate(&lc.cond_rec, g, 1, cudaGraphCondAssignDefault);
-    cudaGraphConditionalHandleCreate(&lc.cond_gc, g, 1, cudaGraphCondAssignDefault);
   }
   if (timed)
     for (int i = 0; i < 3; ++i) lc.ev_branch[i] = L.ev_branch[i];

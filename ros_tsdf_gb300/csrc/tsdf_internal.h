@@ -259,8 +259,6 @@ struct LaunchCfg {
   int capturing;
   cudaStream_t cond_stream;
   cudaGraphConditionalHandle cond_rank;  // the rank sort's passes run (k_gather_ranks sets it)
-  cudaGraphConditionalHandle cond_rec;   // the record sort's last pass runs (k_alloc sets it)
-  cudaGraphConditionalHandle cond_gc;    // the collect passes run (k_enum_flags sets it)
 };
 
 // An event for device timing: inside a graph capture it must be an external

@@ -922,8 +922,7 @@ __global__ void __launch_bounds__(256) k_gather_ranks(Ctx c, cudaGraphConditiona
 
 // One warp per new block, in first-touch order: pop the free list, resolve
 // the pending entry, zero the 4 KiB block (the reference's new VoxelBlock()).
-__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, cudaGraphConditionalHandle cond, int use_cond,
-                                               int rec_passes) {
+__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, int rec_passes) {
   __shared__ long long s_pb[kMaxItems];
   __shared__ int s_warp[32];
   const BatchHdr h = *c.hdr;
@@ -998,10 +997,6 @@ __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, cudaGraphCon
     const bool last = rec_passes > 1 && carry > (1ll << (kRadixBits * (rec_passes - 1)));
     c.ctr->rec_skip_last = rec_passes > 1 && !last ? 1 : 0;
     c.ctr->rec_sel = (rec_passes - (c.ctr->rec_skip_last ? 1 : 0)) & 1;
-    if (use_cond) {
-      cudaGraphSetConditional(cond, last ? 1u : 0u);
-      if (!last && rec_passes > 1) c.ctr->skipped_launches += 3;
-    }
   }
 }
 
@@ -2379,6 +2374,11 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c) {
           xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
         }
       }
+      // the next segment's record values into L1 while these loads are in flight
+      if (next < nseg && lane < UPD_T / 32) {
+        const int2 nb = *reinterpret_cast<const int2*>(c.seg_desc + next);
+        if (nb.y - nb.x <= UPD_T && nb.x + 32 * lane < nb.y) prefetch_l1(rv + nb.x + 32 * lane);
+      }
       int maxdep = 0;
 #pragma unroll
       for (int i = 0; i < kUwCap / 32; ++i) {
@@ -2634,7 +2634,7 @@ __device__ __forceinline__ int find_item_i(const int* base, int n, long long e) 
 // voxels to publish, tile_sums3: blocks to collect; zeroed at step start),
 // and the CTA that finishes last scans both: the reduce and top levels of the
 // publish and gc scans in this one launch.
-__global__ void __launch_bounds__(256) k_enum_flags(Ctx c, cudaGraphConditionalHandle cond_gc, int use_cond) {
+__global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
   __shared__ int s_sb[kMaxItems];
   __shared__ int s_warp[32];
   const BatchHdr h = *c.hdr;
@@ -2683,13 +2683,8 @@ __global__ void __launch_bounds__(256) k_enum_flags(Ctx c, cudaGraphConditionalH
       c.ctr->scan_total = tp;
       c.ctr->scan_total2 = tg;
       // no block left the collect radius: the collect passes have nothing to
-      // do (a conditional node does not launch them; launched directly they
-      // return at once), and the block counts stand
+      // do (they return at once), and the block counts stand
       c.ctr->gc_skip = tg == 0 ? 1 : 0;
-      if (use_cond) {
-        cudaGraphSetConditional(cond_gc, tg == 0 ? 0u : 1u);
-        if (tg == 0) c.ctr->skipped_launches += 2;
-      }
     }
     if (tg == 0)
       for (int i = threadIdx.x; i < c.hdr->n_items; i += blockDim.x)
@@ -3122,7 +3117,7 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.cond_rec, lc.capturing, lc.rec_passes);
+  k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_passes);
   *launches += 1;
 }
 
@@ -3146,13 +3141,10 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
     radix_pass(c, c.rec_key, c.rec_val, &c.hdr->rec_total, kRecSentinel, &c.ctr->n_rec_live, c.rec_cap, p,
                c.max_tiles_rec, lc.sm_count, st, launches, skip);
   };
+  // (the last pass's three kernels return at once when k_alloc found it
+  // empty: cheaper than a conditional node around them, measured)
   for (int p = 0; p + 1 < P; ++p) pass(p, s, nullptr);
-  if (P == 1)
-    pass(0, s, nullptr);
-  else if (lc.capturing)
-    capture_if(lc, s, lc.cond_rec, [&](cudaStream_t st) { pass(P - 1, st, &c.ctr->rec_skip_last); });
-  else
-    pass(P - 1, s, &c.ctr->rec_skip_last);
+  pass(P - 1, s, P > 1 ? &c.ctr->rec_skip_last : nullptr);
   SegHeadIn fin{c.rec_key[0], c.rec_key[1], &c.ctr->rec_sel};
   SegHeadOut fout{c.seg_start};
   const int grid = lc.sm_count * 2;
@@ -3196,7 +3188,7 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
-  k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.cond_gc, lc.capturing);
+  k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c);
   k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_cnt, c.pub_prefix, c.tile_sums2, &c.ctr->scan_total, II_PUB_BASE, -1,
                                      ST_PUB, &c.ctr->done_pub, lc.copyout, nullptr);
   *launches += 2;
@@ -3230,10 +3222,9 @@ void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* laun
     k_gc_apply<<<lc.sm_count * 4, 256, 0, st>>>(c, lc.bucket_size);
     *launches += 2;
   };
-  if (lc.capturing)
-    capture_if(lc, s, lc.cond_gc, collect);
-  else
-    collect(s);
+  // (they return at once when k_enum_flags found nothing to collect:
+  // cheaper than a conditional node around them, measured)
+  collect(s);
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
   k_step_report<<<1, 256, 0, s>>>(c);
   *launches += 1;
