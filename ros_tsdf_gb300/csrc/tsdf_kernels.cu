@@ -2280,7 +2280,7 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
   }
 }
 
-__global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c) {
+__global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
   const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   static_assert(UPD_T == 128 && kUwCap == 512, "record and entry layout of k_update_warp");
   static_assert(sizeof(BcSmem) <= sizeof(UwWarp) * (UW_T / 32), "the CTA phase fits the light phase's shared memory");
@@ -2366,12 +2366,14 @@ __global__ void __launch_bounds__(UW_T) k_update_warp(Ctx c) {
 #pragma unroll
       for (int i = 0; i < kUwCap / 32; ++i) {
         const int f = 32 * i + lane;
-        const unsigned wm = __shfl_sync(kFull, my_mask, i);
-        const int wbi = __shfl_sync(kFull, wb, i);
         xs[i] = make_uint2(0u, kBadLocal);
-        if (f < n_ent) {
-          const int j = wbi + __popc(wm << (31 - lane)) - 1;
-          xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
+        if (32 * i < n_ent) {  // uniform: the windows past the segment's updates cost nothing
+          const unsigned wm = __shfl_sync(kFull, my_mask, i);
+          const int wbi = __shfl_sync(kFull, wb, i);
+          if (f < n_ent) {
+            const int j = wbi + __popc(wm << (31 - lane)) - 1;
+            xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
+          }
         }
       }
       // the next segment's record values into L1 while these loads are in flight
