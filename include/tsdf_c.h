@@ -284,8 +284,7 @@ typedef struct tsdf_map_check_report {
   int64_t slot_mismatches;    /* found entries pointing at another slot        */
   int64_t stray_entries;      /* live entries without an allocated slot        */
   int64_t pending_entries;    /* entries left pending or ranked                */
-  int64_t nnz_mismatches;     /* blocks whose non-zero count or occupancy
-                                 words (the publish pass's voxel mask) are wrong */
+  int64_t nnz_mismatches;     /* blocks whose non-zero count is wrong          */
 } tsdf_map_check_report;
 tsdf_status tsdf_map_check(tsdf_engine* eng, int map_id, tsdf_map_check_report* out);
 

@@ -192,7 +192,6 @@ struct tsdf_engine {
   float2* voxels = nullptr;
   unsigned long long* slot_key = nullptr;
   int* nnz = nullptr;
-  unsigned* occ = nullptr;  // occupancy words, 16 per heap block
   int* free_list = nullptr;
   HEntry* hash = nullptr;
   MapDev* d_maps = nullptr;
@@ -307,7 +306,6 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   x.voxels = eng->voxels;
   x.slot_key = eng->slot_key;
   x.nnz = eng->nnz;
-  x.occ = eng->occ;
   x.free_list = eng->free_list;
   x.hash = eng->hash;
   x.maps = eng->d_maps;
@@ -939,7 +937,6 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   if (dalloc(eng, &eng->voxels, c.pool_blocks * kVoxelsPerBlock, nullptr) != TSDF_OK ||
       dalloc(eng, &eng->slot_key, c.pool_blocks, nullptr) != TSDF_OK ||
       dalloc(eng, &eng->nnz, c.pool_blocks, nullptr) != TSDF_OK ||
-      dalloc(eng, &eng->occ, c.pool_blocks * (kVoxelsPerBlock / 32), nullptr) != TSDF_OK ||
       dalloc(eng, &eng->free_list, c.pool_blocks, nullptr) != TSDF_OK ||
       dalloc(eng, &eng->hash, eng->hash_pool, nullptr) != TSDF_OK ||
       dalloc(eng, &eng->d_maps, c.max_maps, nullptr) != TSDF_OK ||
@@ -949,7 +946,6 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   }
   cudaMemset(eng->slot_key, 0xFF, sizeof(unsigned long long) * c.pool_blocks);
   cudaMemset(eng->nnz, 0, sizeof(int) * c.pool_blocks);
-  cudaMemset(eng->occ, 0, sizeof(unsigned) * (kVoxelsPerBlock / 32) * c.pool_blocks);
   cudaMemset(eng->hash, 0xFF, sizeof(HEntry) * eng->hash_pool);
   cudaMemset(eng->d_maps, 0, sizeof(MapDev) * c.max_maps);
   cudaMemset(eng->d_mctr, 0, sizeof(MapCounters) * c.max_maps);
@@ -987,7 +983,6 @@ tsdf_status tsdf_engine_destroy(tsdf_engine* eng) {
   cudaFree(eng->voxels);
   cudaFree(eng->slot_key);
   cudaFree(eng->nnz);
-  cudaFree(eng->occ);
   cudaFree(eng->free_list);
   cudaFree(eng->hash);
   cudaFree(eng->d_maps);
@@ -1201,7 +1196,6 @@ tsdf_status tsdf_map_restore(tsdf_engine* eng, const void* snapshot, int64_t byt
     CK(cudaMemcpyAsync(eng->nnz + m.dev.heap_base, in + lay.nnz_off, 4ll * hw, cudaMemcpyDefault, L.stream));
     CK(cudaMemcpyAsync(eng->voxels + m.dev.heap_base * kVoxelsPerBlock, in + lay.vox_off,
                        8ll * kVoxelsPerBlock * hw, cudaMemcpyDefault, L.stream));
-    launch_map_occ(L.ctx, m.dev.heap_base, hw, L.stream);
   }
   // hash table from the live keys (the same kernel that rebuilds a table
   // crowded with tombstones)
@@ -1488,10 +1482,7 @@ tsdf_status tsdf_map_check(tsdf_engine* eng, int map_id, tsdf_map_check_report* 
   std::vector<int> fl((size_t)cap), nnz((size_t)cap);
   std::vector<HEntry> tab((size_t)m.hash_entries);
   std::vector<float2> vox((size_t)hw * kVoxelsPerBlock);
-  std::vector<unsigned> occ((size_t)hw * (kVoxelsPerBlock / 32));
   if (hw > 0) {
-    CK(cudaMemcpy(occ.data(), eng->occ + base * (kVoxelsPerBlock / 32), 4 * (kVoxelsPerBlock / 32) * hw,
-                  cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(keys.data(), eng->slot_key + base, 8 * hw, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(vox.data(), eng->voxels + base * kVoxelsPerBlock, sizeof(float2) * kVoxelsPerBlock * hw,
                   cudaMemcpyDeviceToHost));
@@ -1545,20 +1536,11 @@ tsdf_status tsdf_map_check(tsdf_engine* eng, int map_id, tsdf_map_check_report* 
     auto it = slot_of.find(e.key);
     if (it == slot_of.end() || it->second != e.slot) ++r.stray_entries;
   }
-  // non-zero counts, and the occupancy words the publish pass reads (bit l
-  // of word w: voxel 32 w + l has a non-zero weight)
   for (long long s = 0; s < cap; ++s) {
     int want = 0;
-    bool occ_ok = true;
     if (s < hw && keys[s] != kEmptyKey)
-      for (int w = 0; w < kVoxelsPerBlock / 32; ++w) {
-        unsigned bits = 0;
-        for (int l = 0; l < 32; ++l)
-          if (vox[(size_t)s * kVoxelsPerBlock + 32 * w + l].y != 0.0f) bits |= 1u << l;
-        want += __builtin_popcount(bits);
-        occ_ok = occ_ok && occ[(size_t)s * (kVoxelsPerBlock / 32) + w] == bits;
-      }
-    if (nnz[(size_t)s] != want || !occ_ok) ++r.nnz_mismatches;
+      for (int l = 0; l < kVoxelsPerBlock; ++l) want += vox[(size_t)s * kVoxelsPerBlock + l].y != 0.0f;
+    if (nnz[(size_t)s] != want) ++r.nnz_mismatches;
   }
   if (out) *out = r;
   const bool ok = !r.duplicate_keys && !r.free_list_errors && !r.unfindable_keys && !r.slot_mismatches &&

@@ -170,7 +170,6 @@ struct Ctx {
   float2* voxels;                // pool_blocks * 512
   unsigned long long* slot_key;  // pool_blocks, kEmptyKey when free
   int* nnz;                      // non-zero-weight voxels per block
-  unsigned* occ;                 // per block 16 words: bit l of word w set iff voxel 32w+l has a non-zero weight
   int* free_list;                // pool_blocks (map range: logical slots)
   HEntry* hash;                  // all maps' tables
   const MapDev* maps;
@@ -268,9 +267,6 @@ struct LaunchCfg {
 inline cudaError_t record_timing_event(cudaEvent_t ev, cudaStream_t s, bool capturing) {
   return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal) : cudaEventRecord(ev, s);
 }
-
-// A restored map's occupancy words from its voxels (slots below hw).
-void launch_map_occ(const Ctx& c, long long heap_base, long long hw, cudaStream_t s);
 
 cudaError_t kernels_init();  // per-device kernel attributes; after cudaSetDevice
 void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches);

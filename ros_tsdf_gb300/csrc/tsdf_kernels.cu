@@ -286,13 +286,6 @@ __device__ __forceinline__ void update_voxel(float* sdf, float* w, float d, floa
   *w = fminf(nw, maxw);
 }
 
-// A voxel's weight left zero: its bit in the block's occupancy words (bit l
-// of word w is voxel 32 w + l; weights never return to zero, and a block's
-// words are cleared when it is allocated).
-__device__ __forceinline__ void occ_mark(const Ctx& c, long long phys, int l) {
-  atomicOr(&c.occ[phys * (kVoxelsPerBlock / 32) + (l >> 5)], 1u << (l & 31));
-}
-
 __device__ __forceinline__ int find_item(const long long* pb, int n, long long g) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
@@ -966,7 +959,6 @@ __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, int rec_pass
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int k = 0; k < kVoxelsPerBlock / 2 / 32; ++k) dst[k * 32 + lane] = z;
-      if (lane < kVoxelsPerBlock / 32) c.occ[phys * (kVoxelsPerBlock / 32) + lane] = 0u;
     } else if (lane == 0) {
       en->key = kTombKey;
       en->slot = -1;
@@ -1861,10 +1853,7 @@ __device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32],
     const float2 v0 = *v;
     if (c.sdf_scan) {
       const float2 r = warp_chain_scan(v0.x, v0.y, c.hbin + hc.bin, hc.n, hc.maxw, lane, tile[0]);
-      if (lane == 0) {
-        *v = r;
-        if (v0.y == 0.0f) occ_mark(c, hc.phys, hc.local);
-      }
+      if (lane == 0) *v = r;
       continue;
     }
     bool ok;
@@ -1875,7 +1864,6 @@ __device__ __forceinline__ void run_hot_chains(const Ctx& c, float4 (*tile)[32],
         chain_redo(&r.x, &r.y, c.hbin + hc.bin, hc.n, hc.maxw);
       }
       *v = r;
-      if (v0.y == 0.0f) occ_mark(c, hc.phys, hc.local);
     }
   }
 }
@@ -2024,7 +2012,6 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c) {
           const float w = apply_chain(&sdf, v0.y, c.bin_d + base + b, e - b, maxw);
           gv2[l] = make_float2(sdf, w);
           nz_delta += (int)(w != 0.0f) - (int)(v0.y != 0.0f);
-          if (v0.y == 0.0f) occ_mark(c, phys, l);
           ++touched;
         }
       }
@@ -2273,7 +2260,6 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
         const float wv = apply_chain(&sdf, v0[k].y, sm.bins + b, e - b, maxw);
         gv2[l] = make_float2(sdf, wv);
         nz += (int)(wv != 0.0f) - (int)(v0[k].y != 0.0f);
-        if (v0[k].y == 0.0f) occ_mark(c, d.z, l);
         ++touched;
         upd += e - b;
       }
@@ -2467,11 +2453,7 @@ __global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
         }
         __syncwarp();
       }
-      // write back the touched voxels; counters back to zero; the touched
-      // voxels' occupancy bits gathered per word (in lvl, free now) and
-      // or-ed into the block's words where new
-      if (lane < kVoxelsPerBlock / 32) sm.lvl[lane] = 0;
-      __syncwarp();
+      // write back the touched voxels; counters back to zero
       for (int k = lane; k < n0; k += 32) {
         const unsigned l = sm.sorted[k].y;
         const float2 v = sm.vox[l];
@@ -2479,15 +2461,7 @@ __global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
         nz_new += v.y != 0.0f;
         ++touched;
         sm.cnt[l] = 0;
-        if (v.y != 0.0f) atomicOr(reinterpret_cast<unsigned*>(&sm.lvl[l >> 5]), 1u << (l & 31));
       }
-      __syncwarp();
-      if (lane < kVoxelsPerBlock / 32) {
-        const unsigned bits = (unsigned)sm.lvl[lane];
-        unsigned* ow = c.occ + (long long)d.z * (kVoxelsPerBlock / 32) + lane;
-        if (bits & ~*ow) atomicOr(ow, bits);
-      }
-      __syncwarp();
 #pragma unroll
       for (int k = 0; k < UPD_T / 32; ++k) sm.lvl[32 * k + lane] = 0;
     }
@@ -2623,10 +2597,7 @@ __global__ void __launch_bounds__(HU_T) k_heavy_update(Ctx c) {
       }
     }
     // block totals: non-zero weights (a voxel with an update has a positive
-    // weight), touched voxels, applied updates; the warp's 32 voxels are one
-    // occupancy word
-    const unsigned occ_bits = __ballot_sync(kFull, (nfull > 0) | (v0.y != 0.0f));
-    if (lane == 0) c.occ[phys * (kVoxelsPerBlock / 32) + warp] = occ_bits;
+    // weight), touched voxels, applied updates
     const unsigned nz = __reduce_add_sync(kFull, (unsigned)((nfull > 0) | (v0.y != 0.0f)));
     const unsigned tv = __reduce_add_sync(kFull, (unsigned)(nfull > 0));
     const unsigned up = __reduce_add_sync(kFull, (unsigned)nfull);
@@ -2794,15 +2765,9 @@ __global__ void __launch_bounds__(256) k_pub_write(Ctx c, int part) {
     const MapDev& m = c.maps[it.map];
     const long long phys = m.heap_base + (e - s_sb[item]);
     const float2* vox = c.voxels + phys * kVoxelsPerBlock;
-    // only the voxels with a non-zero weight are read: occupancy word r
-    // holds voxels 32 r .. 32 r + 31 (lane r of the warp loads word r)
-    const unsigned occ_w = lane < kVoxelsPerBlock / 32 ? c.occ[phys * (kVoxelsPerBlock / 32) + lane] : 0u;
     float2 v[kVoxelsPerBlock / 32];
 #pragma unroll
-    for (int r = 0; r < kVoxelsPerBlock / 32; ++r) {
-      const unsigned w = __shfl_sync(kFull, occ_w, r);
-      v[r] = (w >> lane) & 1u ? vox[r * 32 + lane] : make_float2(0.f, 0.f);
-    }
+    for (int r = 0; r < kVoxelsPerBlock / 32; ++r) v[r] = vox[r * 32 + lane];
     int kx, ky, kz;
     unpack_key(c.slot_key[phys], &kx, &ky, &kz);
     const float blx = fsub(fadd(div_const((float)kx, m.scale_b, m.rs_b), m.half_bs), m.half_bs);
@@ -3273,23 +3238,6 @@ void launch_map_init(float2* voxels, unsigned long long* slot_key, int* nnz, int
   (void)voxels;
   k_map_init<<<256, 256, 0, s>>>(free_list, slot_key, nnz, heap_base, heap_cap);
   cudaMemsetAsync(hash + hash_base, 0xFF, (size_t)hash_entries * sizeof(HEntry), s);
-}
-
-// One warp per occupancy word of the slots below hw: the ballot of its 32
-// voxels' weights.
-__global__ void k_map_occ(Ctx c, long long heap_base, long long hw) {
-  const long long nwords = hw * (kVoxelsPerBlock / 32);
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < nwords; w += nwarps) {
-    const float2 v = c.voxels[heap_base * kVoxelsPerBlock + w * 32 + lane];
-    const unsigned bits = __ballot_sync(kFull, v.y != 0.0f);
-    if (lane == 0) c.occ[heap_base * (kVoxelsPerBlock / 32) + w] = bits;
-  }
-}
-
-void launch_map_occ(const Ctx& c, long long heap_base, long long hw, cudaStream_t s) {
-  if (hw > 0) k_map_occ<<<512, 256, 0, s>>>(c, heap_base, hw);
 }
 
 void launch_map_rehash(const Ctx& c, int map, int bucket_size, long long heap_base, long long heap_hw,
