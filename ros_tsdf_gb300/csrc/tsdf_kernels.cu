@@ -11,24 +11,29 @@
 //                (G-lane cooperative probes, G = bucket size); unallocated
 //                blocks enter as "pending" with the smallest first-touch rank.
 //                (tsdf_handler.cu:112-272, :282-500)
-//   alloc_order  pending entries sorted by first-touch rank (LSD radix sort)
+//   alloc_order  pending entries sorted by first-touch rank: up to 2048 by
+//                one CTA (bitonic), more by LSD radix passes that sit in a
+//                conditional graph node
 //   alloc        heap slot = free_list[block_count + rank within the map]
-//                (device free-list stack), block zeroed, entry resolved
+//                (device free-list stack), block zeroed, entry resolved; the
+//                batch's slots numbered (each map's after the maps before it)
 //   ray_voxels   voxel DDA per point; its voxels grouped into runs of one
 //                block; per voxel an entry {d, local index}, per run one
-//                routing record (block slot, entry range)
-//   route_sort   stable radix sort of the records by block slot; segment
-//                heads -> one segment per block touched; segment items and
-//                the list of heavy segments (more than 128 records)
-//   heavy_bins   heavy segments: counting sort of their updates into
+//                routing record (slot number, entry range)
+//   route_sort   stable radix sort of the records by slot number (the last
+//                pass returns at once when no number reaches its digit);
+//                segment heads -> one segment per block touched; segment
+//                classes: light (<= 128 records and <= 512 updates),
+//                CTA-heavy (<= 1024 records and <= 4096 updates), grid-heavy
+//   heavy_bins   grid-heavy segments: counting sort of their updates into
 //                per-voxel bins in point order (plan, count, scan, place);
 //                voxels with more than 128 updates go on the hot list
 //   update       three streams: k_hot_chains (one warp per voxel with more
-//                than 128 updates), k_heavy_update (binned heavy segments,
-//                one lane per voxel) and k_update_warp (light segments: one
-//                warp per block, its records in point order, a record's
-//                updates in parallel, one lane per voxel); k_update takes the
-//                heavy segments beyond the binning capacity in passes.
+//                than 128 updates), k_heavy_update (binned grid-heavy
+//                segments, one lane per voxel) and k_update_warp (first one
+//                CTA per CTA-heavy segment in shared memory, then one warp per
+//                light segment, its updates depth by depth); k_update takes
+//                the grid-heavy segments beyond the binning capacity in passes.
 //                (tsdf_handler.cu:604-665)
 //   publish      in-radius blocks counted, prefix-summed, compacted to the
 //                output arrays or a serialized Tsdf message; for pinned host
@@ -36,7 +41,8 @@
 //                whole 16-byte stores on a side stream
 //                (tsdf_handler.cu:767-825, publisher.cpp:9-31)
 //   gc           out-of-radius blocks compacted, pushed to the free list in
-//                ascending slot order, hash entries tombstoned
+//                ascending slot order, hash entries tombstoned (the passes
+//                return at once when no block left the radius)
 //                (tsdf_handler.cu:836-952); the step's stats and counters
 //                written into the host's pinned mirrors
 //
