@@ -1945,9 +1945,8 @@ __global__ void __launch_bounds__(UPD_T, 8) k_update(Ctx c) {
     int nz_delta = 0, touched = 0;
     unsigned n_upd = 0;
     {
-      // ---- a heavy segment beyond the counting sort's capacity, or a light
-      // one with more entries than the compacted arrays hold.  Pass 0:
-      // per-voxel update counts over all records
+      // ---- a grid-heavy segment beyond the counting sort's capacity.
+      // Pass 0: per-voxel update counts over all records
       for (int l = t; l < kVoxelsPerBlock; l += UPD_T) s_run[l] = 0;
       __syncthreads();
       for (long long cb = b0; cb < b1; cb += UPD_T) {
