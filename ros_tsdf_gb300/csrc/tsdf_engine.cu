@@ -488,17 +488,6 @@ bool device_accessible(const void* p, const void** dev_ptr) {
   return true;
 }
 
-// Device or managed memory, which kernels read in place.  Host memory is
-// staged into HBM first (kernels reading it over the host link would see its
-// latency on every point load): pinned memory by k_stage_points, one launch
-// for the batch; pageable memory by the DMA engine, one copy per scan.
-bool device_resident(const void* p, const void** dev_ptr) {
-  const PtrInfo r = ptr_info(p);
-  if (r.where != PTR_DEVICE) return false;
-  *dev_ptr = r.dev;
-  return true;
-}
-
 // Validate a batch and enqueue it on lane L (asynchronous).  On success the
 // lane is busy until finish_batch.
 tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans, tsdf_scan_result* res) {
