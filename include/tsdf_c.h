@@ -210,6 +210,12 @@ tsdf_status tsdf_integrate_batch(tsdf_engine* eng, int n, const tsdf_scan* scans
  * scans of one map run in submission order.  *ticket identifies it.  The
  * caller keeps scan->xyz and *result alive until the request completes. */
 tsdf_status tsdf_submit(tsdf_engine* eng, const tsdf_scan* scan, tsdf_scan_result* result, uint64_t* ticket);
+/* Queue n scans at once (all or none: nothing is queued when one of them is
+ * refused).  The scheduler sees them together, so scans that arrive in a
+ * burst (the scans of many maps at one sensor tick) share a step instead of
+ * the first one launching alone.  tickets[i] completes results[i]. */
+tsdf_status tsdf_submit_batch(tsdf_engine* eng, int n, const tsdf_scan* scans, tsdf_scan_result* results,
+                              uint64_t* tickets);
 /* TSDF_OK when done (result filled), TSDF_ERR_NOT_READY while running. */
 tsdf_status tsdf_poll(tsdf_engine* eng, uint64_t ticket);
 /* Wait up to timeout_ms (negative: no limit) for a ticket. */

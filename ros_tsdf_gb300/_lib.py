@@ -99,6 +99,7 @@ SIGNATURES = [
                                  C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(ScanStats)]),
     ("tsdf_integrate_batch", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Scan), C.POINTER(ScanResult)]),
     ("tsdf_submit", C.c_int, [C.c_void_p, C.POINTER(Scan), C.POINTER(ScanResult), C.POINTER(C.c_uint64)]),
+    ("tsdf_submit_batch", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Scan), C.POINTER(ScanResult), C.POINTER(C.c_uint64)]),
     ("tsdf_poll", C.c_int, [C.c_void_p, C.c_uint64]),
     ("tsdf_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_int64]),
     ("tsdf_ticket_times", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),

@@ -1291,6 +1291,35 @@ tsdf_status tsdf_submit(tsdf_engine* eng, const tsdf_scan* scan, tsdf_scan_resul
   return TSDF_OK;
 }
 
+tsdf_status tsdf_submit_batch(tsdf_engine* eng, int n, const tsdf_scan* scans, tsdf_scan_result* results,
+                              uint64_t* tickets) {
+  NvtxRange nvtx_range("tsdf_submit_batch");
+  if (!eng || n < 0 || (n > 0 && (!scans || !results || !tickets))) return TSDF_ERR_INVALID_ARG;
+  std::unique_lock<std::recursive_mutex> lk(eng->mu);
+  // all or none: every scan is checked before any is queued
+  for (int i = 0; i < n; ++i) {
+    const int m = scans[i].map_id;
+    if (m < 0 || m >= (int)eng->maps.size() || !eng->maps[m].live) return fail(eng, TSDF_ERR_INVALID_ARG, "unknown map id");
+    if (scans[i].n_points > eng->cfg.max_batch_points) return fail(eng, TSDF_ERR_CAPACITY, "scan larger than a step");
+  }
+  const int64_t t = now_ns();
+  for (int i = 0; i < n; ++i) {
+    auto r = std::make_shared<Request>();
+    r->ticket = eng->next_ticket++;
+    r->scan = scans[i];
+    r->result = results + i;
+    r->t_submit = t;
+    eng->queue.push_back(r);
+    eng->tickets[r->ticket] = r;
+    tickets[i] = r->ticket;
+  }
+  if (n > 0) {
+    ensure_scheduler(eng);
+    eng->cv.notify_all();
+  }
+  return TSDF_OK;
+}
+
 tsdf_status tsdf_poll(tsdf_engine* eng, uint64_t ticket) {
   if (!eng) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);

@@ -239,6 +239,39 @@ class Engine:
         self._keep[t.value] = handle
         return t.value
 
+    def submit_batch(self, items, pub_cap: int = 400000) -> list:
+        """Queue several scans at once (tsdf_submit_batch: all or none), each
+        item (map_id, xyz, origin); returns their tickets for wait().  The
+        scheduler sees them together, so they share a step."""
+        n = len(items)
+        scs = (L.Scan * n)()
+        rss = (L.ScanResult * n)()
+        tks = (C.c_uint64 * n)()
+        keep = []
+        for i, (map_id, xyz, origin) in enumerate(items):
+            a, stride = _as_points(xyz)
+            sc = scs[i]
+            sc.map_id = int(map_id)
+            sc.stride_bytes = stride
+            sc.n_points = a.shape[0]
+            sc.xyz = a.ctypes.data if a.shape[0] else None
+            sc.origin[:] = [float(v) for v in origin]
+            pos = np.empty((pub_cap, 3), np.float32)
+            data = np.empty((pub_cap, 2), np.float32)
+            rss[i].pub_pos = pos.ctypes.data
+            rss[i].pub_data = data.ctypes.data
+            rss[i].pub_cap = pub_cap
+            keep.append((a, pos, data))
+        self._check(self.lib.tsdf_submit_batch(self.h, n, scs, rss, tks), "tsdf_submit_batch")
+        out = []
+        for i in range(n):
+            a, pos, data = keep[i]
+            t = int(tks[i])
+            # the arrays hold the results struct alive with the ticket's buffers
+            self._keep[t] = (t, a, scs, rss[i], pos, data)
+            out.append(t)
+        return out
+
     def poll(self, ticket: int) -> bool:
         st = self.lib.tsdf_poll(self.h, ticket)
         if st == L.ERR_NOT_READY:

@@ -269,6 +269,36 @@ def test_served_mode_isolation(built, pinned):
                               f"map {i} scan {k}")
 
 
+def test_submit_batch_shares_steps(built):
+    """tsdf_submit_batch queues several maps' scans at once (they share a
+    step) with each map's alone-and-in-order result; a batch naming an
+    unknown map is refused whole, nothing queued."""
+    from ros_tsdf_gb300 import Engine, TsdfError, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    specs = _mixed_specs()[:5]
+    srcs = [W.ScanSource(s) for s in specs]
+    scans = [[srcs[i].scan(k) for k in range(2)] for i in range(len(specs))]
+    pool = sum(s.heap_blocks for s in specs)
+    with Engine(max_maps=8, pool_blocks=pool, max_batch_points=1 << 18, lanes=2) as eng:
+        mids = [eng.create_map(s.params, s.heap_blocks) for s in specs]
+        with pytest.raises(TsdfError) as e:
+            eng.submit_batch([(mids[0], *scans[0][0]), (99, *scans[1][0])])
+        assert e.value.status == L.ERR_INVALID_ARG
+        results = []
+        for k in range(2):
+            tickets = eng.submit_batch([(mids[i], *scans[i][k]) for i in range(len(specs))], pub_cap=1 << 20)
+            rs = [eng.wait(t, timeout_ms=60000) for t in tickets]
+            launches = {r.stats["t_launch_ns"] for r in rs}
+            assert len(launches) <= 2  # one step, or two when a lane was busy
+            results.append(rs)
+    for i, s in enumerate(specs):
+        orc = _oracle(s.params, s.heap_blocks)
+        for k in range(2):
+            assert_scan_equal(results[k][i], orc.integrate(*scans[i][k], pub_cap=1 << 20),
+                              s.params.truncation_distance, f"map {i} scan {k}")
+
+
 def test_handler_mirror(built):
     import ros_tsdf_gb300 as tsdf
     from ros_tsdf_gb300 import Engine, workloads as W
