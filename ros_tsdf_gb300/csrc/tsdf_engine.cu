@@ -464,8 +464,44 @@ tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_
 }
 
 // One pointer query: where a caller's buffer lives and the address kernels use.
+// Buffers this library allocated for callers (tsdf_host_alloc,
+// tsdf_device_alloc), by start address: their kind and device address are
+// known without asking the driver (a cudaPointerGetAttributes call costs
+// about a microsecond, and a batch asks for three buffers per scan).  An
+// entry lives from the allocation to the matching free call.
+struct KnownRange {
+  size_t size;
+  int where;
+  const char* dev;
+};
+std::mutex g_known_mu;
+std::map<uintptr_t, KnownRange> g_known;
+
+void known_add(const void* p, size_t size, int where, const void* dev) {
+  std::lock_guard<std::mutex> lk(g_known_mu);
+  g_known[reinterpret_cast<uintptr_t>(p)] = KnownRange{size, where, static_cast<const char*>(dev)};
+}
+
+void known_remove(const void* p) {
+  std::lock_guard<std::mutex> lk(g_known_mu);
+  g_known.erase(reinterpret_cast<uintptr_t>(p));
+}
+
+bool known_lookup(const void* p, PtrInfo* r) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  std::lock_guard<std::mutex> lk(g_known_mu);
+  auto it = g_known.upper_bound(a);
+  if (it == g_known.begin()) return false;
+  --it;
+  if (a >= it->first + it->second.size) return false;
+  r->where = it->second.where;
+  r->dev = it->second.dev + (a - it->first);
+  return true;
+}
+
 PtrInfo ptr_info(const void* p) {
   PtrInfo r;
+  if (p && known_lookup(p, &r)) return r;
   cudaPointerAttributes a;
   if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
@@ -1660,10 +1696,20 @@ int64_t tsdf_kernel_launches(tsdf_engine* eng) { return eng ? (int64_t)eng->laun
 
 tsdf_status tsdf_host_alloc(void** p, int64_t bytes) {
   if (!p || bytes < 0) return TSDF_ERR_INVALID_ARG;
-  return cudaMallocHost(p, (size_t)std::max<int64_t>(bytes, 1)) == cudaSuccess ? TSDF_OK : TSDF_ERR_CUDA;
+  const size_t n = (size_t)std::max<int64_t>(bytes, 1);
+  if (cudaMallocHost(p, n) != cudaSuccess) return TSDF_ERR_CUDA;
+  void* dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, *p, 0) == cudaSuccess && dev)
+    known_add(*p, n, PTR_PINNED, dev);
+  else
+    cudaGetLastError();  // left to the driver query at use
+  return TSDF_OK;
 }
 
-tsdf_status tsdf_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? TSDF_OK : TSDF_ERR_CUDA; }
+tsdf_status tsdf_host_free(void* p) {
+  known_remove(p);
+  return cudaFreeHost(p) == cudaSuccess ? TSDF_OK : TSDF_ERR_CUDA;
+}
 
 // Stamped sensor translations, kept sorted by stamp (see include/tsdf_c.h).
 struct tsdf_pose_buffer {
@@ -1754,6 +1800,7 @@ tsdf_status tsdf_device_alloc(tsdf_engine* eng, void** p, int64_t bytes) {
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   CK(cudaSetDevice(eng->device));
   CK(cudaMalloc(p, (size_t)std::max<int64_t>(bytes, 1)));
+  known_add(*p, (size_t)std::max<int64_t>(bytes, 1), PTR_DEVICE, *p);
   return TSDF_OK;
 }
 
@@ -1761,6 +1808,7 @@ tsdf_status tsdf_device_free(tsdf_engine* eng, void* p) {
   if (!eng) return TSDF_ERR_INVALID_ARG;
   std::unique_lock<std::recursive_mutex> lk(eng->mu);
   CK(cudaSetDevice(eng->device));
+  known_remove(p);
   CK(cudaFree(p));
   return TSDF_OK;
 }
