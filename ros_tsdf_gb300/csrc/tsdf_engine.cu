@@ -311,8 +311,13 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
   x.maps = eng->d_maps;
   x.mctr = eng->d_mctr;
   std::vector<void*>* tr = &L.allocs;
-  TRY(dalloc(eng, &L.d_hdr, 1, tr));
-  TRY(dalloc(eng, &L.d_items, c.max_maps, tr));
+  // the batch header and the item descriptors in one allocation, laid out
+  // as in the pinned host mirror, so that one copy carries both
+  static_assert(sizeof(BatchHdr) % alignof(ItemDev) == 0, "items follow the header");
+  char* d_desc = nullptr;
+  TRY(dalloc(eng, &d_desc, (long long)(sizeof(BatchHdr) + sizeof(ItemDev) * c.max_maps), tr));
+  L.d_hdr = reinterpret_cast<BatchHdr*>(d_desc);
+  L.d_items = reinterpret_cast<ItemDev*>(d_desc + sizeof(BatchHdr));
   x.hdr = L.d_hdr;
   x.items = L.d_items;
   TRY(dalloc(eng, &x.item_stats, (long long)c.max_maps * ST_COUNT, tr));
@@ -666,8 +671,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   const int rec_passes = std::max(1, (bits_for((unsigned long long)slot_total) + kRadixBits - 1) / kRadixBits);
   L.step_timed = eng->timing != 0;
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[0], L.stream));
-  CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr), cudaMemcpyHostToDevice, L.stream));
-  CK(cudaMemcpyAsync(L.d_items, items, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
+  CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr) + sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
   TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   // the step's stats and counters reach L.h_stats / h_ctr / h_mctr through
