@@ -159,7 +159,7 @@ struct Lane {
   long long* h_stats = nullptr; // [max_maps][ST_COUNT]
   LaneCounters* h_ctr = nullptr;
   MapCounters* h_mctr = nullptr;
-  // graphs keyed by (rank_passes, rec_passes, timing)
+  // graphs keyed by (small batch, copy-out, staged inputs, rank_passes, rec_passes, timing)
   std::map<int, cudaGraphExec_t> graphs;
   std::map<int, long long> graph_launches;
   cudaEvent_t ev_stage[STAGE_COUNT + 1] = {};
@@ -259,12 +259,17 @@ tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>*
     if (_s != TSDF_OK) return _s;       \
   } while (0)
 
+// A batch of at most this many points runs the point-bound stages on grids
+// sized for an eighth of the SMs (its own graph).
+constexpr long long kSmallBatchPoints = 4096;
+
 LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes, bool staged,
-                     bool copyout) {
+                     bool copyout, bool small) {
   LaunchCfg lc;
   lc.staged = staged ? 1 : 0;
   lc.copyout = copyout ? 1 : 0;
   lc.sm_count = eng->sm_count;
+  lc.grid_sm = small ? std::max(1, eng->sm_count / 8) : eng->sm_count;
   lc.bucket_size = eng->cfg.bucket_size;
   lc.ray_threads = eng->cfg.ray_threads;
   lc.rank_passes = rank_passes;
@@ -412,8 +417,8 @@ void lane_free(Lane& L) {
 // Enqueue the pipeline of one step on the lane's stream (used directly or
 // inside a graph capture).  Returns the number of kernel launches.
 long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
-                           bool timed, bool capturing) {
-  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout);
+                           bool small, bool timed, bool capturing) {
+  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout, small);
   lc.capturing = capturing ? 1 : 0;
   lc.cond_rank = cudaGraphConditionalHandle{};
   if (capturing) {
@@ -438,22 +443,23 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
   return n;
 }
 
-tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout) {
+tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
+                            bool small) {
   NvtxRange nvtx_range("tsdf launch_pipeline");
   const bool timed = eng->stage_timing;
   L.timed = timed;
   if (eng->cfg.no_graphs) {
-    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed, false);
+    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, small, timed, false);
     CK(cudaGetLastError());
     return TSDF_OK;
   }
-  const int key =
-      (copyout ? 2000 : 0) + (staged ? 1000 : 0) + rank_passes * 100 + rec_passes * 10 + (timed ? 1 : 0);
+  const int key = (small ? 10000 : 0) + (copyout ? 2000 : 0) + (staged ? 1000 : 0) + rank_passes * 100 +
+                  rec_passes * 10 + (timed ? 1 : 0);
   auto it = L.graphs.find(key);
   if (it == L.graphs.end()) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
-    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, timed, true);
+    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, small, timed, true);
     cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     cudaGraphExec_t ex = nullptr;
@@ -672,7 +678,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   L.step_timed = eng->timing != 0;
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[0], L.stream));
   CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr) + sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
-  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout));
+  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout, total <= kSmallBatchPoints));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   // the step's stats and counters reach L.h_stats / h_ctr / h_mctr through
   // k_step_report, the graph's last kernel

@@ -240,6 +240,11 @@ enum {
 // pipeline stage on `s`; every launch is counted in *launches.
 struct LaunchCfg {
   int sm_count;
+  // SMs the grids of the stages whose work follows the batch's points are
+  // sized for (ray passes through update): all of them, or an eighth for a
+  // small batch, whose few items would leave most CTAs of a full grid idle
+  // (publish and gc follow the maps' sizes and keep sm_count)
+  int grid_sm;
   int bucket_size;   // 1, 2, 4, 8 or 16
   int ray_threads;
   int rank_passes;

@@ -348,20 +348,38 @@ __device__ __forceinline__ int group_lookup(const HEntry* tab, unsigned mask, un
   return -1;
 }
 
+// The rest of a single-entry-bucket lookup (group_lookup<1>) whose first
+// probe, raw, was loaded earlier: the logical slot, or -1.
+__device__ __forceinline__ int probe_resolve(const HEntry* tab, unsigned mask, unsigned long long key,
+                                             ulonglong2 raw) {
+  if (raw.x == key) return (int)(unsigned)(raw.y & 0xFFFFFFFFull);
+  if (raw.x == kEmptyKey) return -1;
+  const unsigned long long h = mix64(key);
+  for (unsigned p = 1; p <= mask; ++p) {
+    raw = load_entry_ro(tab + ((unsigned)(h + p) & mask));
+    if (raw.x == key) return (int)(unsigned)(raw.y & 0xFFFFFFFFull);
+    if (raw.x == kEmptyKey) return -1;
+  }
+  return -1;
+}
+
 // Find-or-claim for the block pass.  A found pending entry gets atomicMin of
 // the rank; a claimed entry (first EMPTY or TOMB slot from the home bucket,
 // CAS on the key) becomes pending with this rank.  All inserters of one key
 // walk the same sequence and treat "entry == key" as found, so a key is never
-// claimed twice; no entry is freed during the pass.
+// claimed twice; no entry is freed during the pass.  With use_first, first
+// is the home entry loaded earlier: a key seen there is there still, and an
+// empty entry seen there is re-read by the claim loop before it is claimed.
 template <int G>
 __device__ __forceinline__ int group_insert(HEntry* tab, unsigned mask, unsigned long long key, unsigned rank, int gl,
-                                            int gbase, unsigned gmask, unsigned* entry_out, bool* from_empty) {
+                                            int gbase, unsigned gmask, unsigned* entry_out, bool* from_empty,
+                                            bool use_first = false, ulonglong2 first = ulonglong2{}) {
   const int lane = threadIdx.x & 31;
   const unsigned long long h = mix64(key);
   for (unsigned p = 0; p <= mask; ++p) {
     unsigned b = (unsigned)(h + p) & mask;
     HEntry* e = tab + (size_t)b * G + gl;
-    ulonglong2 raw = load_entry_cg(e);
+    ulonglong2 raw = (use_first && p == 0) ? first : load_entry_cg(e);
     unsigned hit = __ballot_sync(gmask, raw.x == key) & gmask;
     if (hit) {
       if (lane == __ffs(hit) - 1 && (int)(unsigned)(raw.y & 0xFFFFFFFFull) < 0) atomicMin(&e->rank, rank);
@@ -492,24 +510,43 @@ __global__ void __launch_bounds__(256) k_stage_points(Ctx c) {
   }
 }
 
+// block steps of one ray whose home hash entries k_ray_blocks loads at once
+constexpr int kProbeBatch = 4;
+
+// ----------------------------------------------------------------------------
+// Work queues (ray chunks, light segments, CTA segments): a warp or CTA whose
+// index in the grid is at least the number of items returns before it reads
+// anything else.  The ones below it are at least as many as the items and
+// each keeps taking items until the queue is empty, so every item is still
+// taken; a small step then costs neither the atomics of thousands of idle
+// warps on one address nor their set-up.
+__device__ __forceinline__ bool ray_cta_idle(long long total, long long chunk) {
+  return (long long)blockIdx.x * (blockDim.x >> 5) * chunk >= total;
+}
+// all 32 lanes call it
+__device__ __forceinline__ long long ray_next_chunk(unsigned long long* head) {
+  unsigned long long q = 0;
+  if ((threadIdx.x & 31) == 0) q = atomicAdd(head, 1ull);
+  return (long long)__shfl_sync(kFull, q, 0);
+}
+
 // ----------------------------------------------------------------------------
 // ray pass 1: block DDA + find-or-claim (getVoxelBlocksCuda + allocation lookup)
 template <int G>
 __global__ void __launch_bounds__(256) k_ray_blocks(Ctx c) {
   __shared__ long long s_pb[kMaxItems];
   const BatchHdr h = *c.hdr;
+  const long long total = h.total_points;
+  const long long chunk = c.ray_chunk;
+  if (ray_cta_idle(total, chunk)) return;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int gl = lane % G;
   const int gbase = lane - gl;
   const unsigned gmask = (G == 32) ? kFull : (((1u << G) - 1u) << gbase);
-  const long long total = h.total_points;
-  const long long chunk = c.ray_chunk;
-  while (true) {
-    unsigned long long q = 0;
-    if (lane == 0) q = atomicAdd(&c.ctr->q_blocks, 1ull);
-    long long start = (long long)__shfl_sync(kFull, q, 0) * chunk;
+  for (long long item = ray_next_chunk(&c.ctr->q_blocks);; item = ray_next_chunk(&c.ctr->q_blocks)) {
+    long long start = item * chunk;
     if (start >= total) break;
     long long end = min(start + chunk, total);
     for (long long base = start; base < end; base += 32) {
@@ -530,6 +567,47 @@ __global__ void __launch_bounds__(256) k_ray_blocks(Ctx c) {
       HEntry* tab = c.hash + m.hash_base;
       const unsigned mask = m.hash_mask;
       unsigned inc = 0;
+      if constexpr (G == 1) {
+        // single-entry buckets: the home entries of up to kProbeBatch block
+        // steps are loaded together, then the steps are inserted in order
+        for (int j0 = 0;; j0 += kProbeBatch) {
+          unsigned long long keys[kProbeBatch];
+          ulonglong2 home[kProbeBatch];
+          int nk = 0;
+#pragma unroll
+          for (int k = 0; k < kProbeBatch; ++k) {
+            float x, y, z;
+            int kx, ky, kz;
+            const bool has = valid && dda.next(&x, &y, &z, &kx, &ky, &kz);  // the steps are a prefix
+            keys[k] = has ? pack_key(kx, ky, kz) : 0ull;
+            home[k] = has ? load_entry_cg(tab + ((unsigned)mix64(keys[k]) & mask)) : make_ulonglong2(0ull, 0ull);
+            nk += has ? 1 : 0;
+          }
+          if (!__ballot_sync(kFull, nk > 0)) break;
+          inc += (unsigned)nk;
+          const unsigned own = 1u << lane;
+#pragma unroll
+          for (int k = 0; k < kProbeBatch; ++k) {
+            if (k >= nk) continue;
+            const unsigned rank = (unsigned)(g * (long long)h.rank_stride + j0 + k);
+            unsigned entry = 0;
+            bool from_empty = false;
+            const int res = group_insert<1>(tab, mask, keys[k], rank, 0, lane, own, &entry, &from_empty, true, home[k]);
+            if (res == INS_NEW) {
+              unsigned long long slot = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_new), 1ull);
+              long long gidx = (long long)(tab - c.hash) + entry;
+              if ((long long)slot < c.rank_cap)
+                c.newlist[slot] = (unsigned)gidx;
+              else
+                set_error(c.ctr, ERR_CAPACITY);
+              atomicAdd(&c.item_i[item * II_COUNT + II_NEW], 1);
+              if (from_empty) atomicAdd(&c.mctr[mi].hash_used, 1);
+            } else if (res == INS_FULL) {
+              set_error(c.ctr, ERR_HASH_FULL);
+            }
+          }
+        }
+      } else
       for (int j = 0;; ++j) {
         float x, y, z;
         int kx, ky, kz;
@@ -1016,23 +1094,22 @@ template <int G>
 __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
   __shared__ long long s_pb[kMaxItems];
   const BatchHdr h = *c.hdr;
+  const long long total = h.total_points;
+  const long long chunk = c.ray_chunk;
+  if (ray_cta_idle(total, chunk)) return;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int gl = lane % G;
   const int gbase = lane - gl;
   const unsigned gmask = (G == 32) ? kFull : (((1u << G) - 1u) << gbase);
-  const long long total = h.total_points;
-  const long long chunk = c.ray_chunk;
   const int R = h.rec_stride;
   const int VS = h.vox_stride;
   unsigned* rk = c.rec_key[0];
   unsigned* rv = c.rec_val[0];
   uint2* ent = c.entries;
-  while (true) {
-    unsigned long long q = 0;
-    if (lane == 0) q = atomicAdd(&c.ctr->q_voxels, 1ull);
-    long long start = (long long)__shfl_sync(kFull, q, 0) * chunk;
+  for (long long item = ray_next_chunk(&c.ctr->q_voxels);; item = ray_next_chunk(&c.ctr->q_voxels)) {
+    long long start = item * chunk;
     if (start >= total) break;
     long long end = min(start + chunk, total);
     for (long long base = start; base < end; base += 32) {
@@ -1066,6 +1143,27 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
       int run = -1, run_slot = -1, run_start = 0, run_cnt = 0, j = 0;
       float blx = 0.f, bly = 0.f, blz = 0.f;
       unsigned route_ovf = 0, missing = 0, bad = 0;
+      // Single-entry buckets: a run's first probe is loaded when the run
+      // starts and read when it ends, so the walk never waits on the hash
+      // table.  The run's entries are written meanwhile; when its block turns
+      // out to be missing, the run is counted as the reference counts it (its
+      // updates missing, none of them bad) and recorded with no entries.
+      ulonglong2 probe = make_ulonglong2(0ull, 0ull);
+      unsigned run_bad = 0;
+      auto close_run = [&]() {
+        if (run >= 0 && run < rmax) {
+          if constexpr (G == 1) {
+            run_slot = probe_resolve(tab, mask, cur, probe);
+            if (run_slot < 0) {
+              missing += (unsigned)(j - run_start);
+              bad -= run_bad;
+              run_cnt = 0;
+            }
+          }
+          rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
+          rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
+        }
+      };
       while (true) {
         float x, y, z;
         int kx, ky, kz;
@@ -1081,49 +1179,54 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
         }
         const bool newrun = has && bkey != cur;
         if (newrun) {
-          if (run >= 0 && run < rmax) {
-            rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
-            rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
-          }
+          close_run();
           ++run;
           cur = bkey;
           run_slot = -1;
           run_start = j;
           run_cnt = 0;
+          run_bad = 0;
           // block centre and bottom-left corner (tsdf_handler.cu:612-624)
           blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
           bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
           blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
         }
         const bool need = newrun && run < rmax;
-        const unsigned nm = __ballot_sync(kFull, need);
-        for (int i = 0; i < G && (nm & gmask) != 0u; ++i) {
-          const int src = gbase + i;
-          if (!((nm >> src) & 1u)) continue;
-          unsigned long long k2 = __shfl_sync(gmask, bkey, src);
-          const HEntry* t2 =
-              reinterpret_cast<const HEntry*>(__shfl_sync(gmask, reinterpret_cast<unsigned long long>(tab), src));
-          unsigned m2 = __shfl_sync(gmask, mask, src);
-          int res = group_lookup<G>(t2, m2, k2, gl, gbase, gmask);
-          if (lane == src) run_slot = res;
+        if constexpr (G == 1) {
+          if (need) probe = load_entry_ro(tab + ((unsigned)mix64(bkey) & mask));
+        } else {
+          const unsigned nm = __ballot_sync(kFull, need);
+          for (int i = 0; i < G && (nm & gmask) != 0u; ++i) {
+            const int src = gbase + i;
+            if (!((nm >> src) & 1u)) continue;
+            unsigned long long k2 = __shfl_sync(gmask, bkey, src);
+            const HEntry* t2 =
+                reinterpret_cast<const HEntry*>(__shfl_sync(gmask, reinterpret_cast<unsigned long long>(tab), src));
+            unsigned m2 = __shfl_sync(gmask, mask, src);
+            int res = group_lookup<G>(t2, m2, k2, gl, gbase, gmask);
+            if (lane == src) run_slot = res;
+          }
         }
         if (has) {
           if (run >= rmax) {
             ++route_ovf;
-          } else if (run_slot < 0) {
+          } else if (G != 1 && run_slot < 0) {
             ++missing;
           } else if (run_cnt >= 31) {
             ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
+            ++run_bad;
           } else {
             // getLocalVoxelIndex (tsdf_handler.cu:507-512)
             float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
             float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
             float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
             unsigned local = kBadLocal;
-            if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
+            if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f) {
               local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
-            else
+            } else {
               ++bad;
+              ++run_bad;
+            }
             const float d = distance_update(x, y, z, px, py, pz, ox, oy, oz);
             ent[ebase + j] = make_uint2(__float_as_uint(d), local);
             ++run_cnt;
@@ -1132,10 +1235,7 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
         }
       }
       if (active) {
-        if (run >= 0 && run < rmax) {
-          rk[rbase + run] = run_slot >= 0 ? (unsigned)(kbase + run_slot) : kRecSentinel;
-          rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
-        }
+        close_run();
         int first = valid ? min(run + 1, rmax) : 0;
         for (int r = first; r < R; ++r) rk[rbase + r] = kRecSentinel;
       }
@@ -2124,11 +2224,13 @@ __device__ void block_update_cta(const Ctx& c, int rec_sel, BcSmem& sm) {
   const unsigned lt = (1u << lane) - 1u;
   const unsigned* rv = c.rec_val[rec_sel];
   const long long nb = c.ctr->n_bcta;
+  if (blockIdx.x >= nb) return;  // uniform: the CTAs below take every item
+  long long q = 0;
   for (;;) {
     __syncthreads();
     if (t == 0) sm.seg = (long long)atomicAdd(&c.ctr->q_bcta, 1ull);
     __syncthreads();
-    const long long q = sm.seg;
+    q = sm.seg;
     if (q >= nb) break;
     const int sj = c.bcta[q];
     const int4 d = c.seg_desc[sj];
@@ -2304,15 +2406,22 @@ __global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
   __syncwarp();
   const long long nseg = c.ctr->n_seg;
   const unsigned* rv = c.rec_val[rec_sel];
-  long long next = 0;
-  if (lane == 0) next = (long long)atomicAdd(&c.ctr->q_update_warp, 1ull);
-  next = __shfl_sync(kFull, next, 0);
+  const long long gw = (long long)blockIdx.x * (UW_T / 32) + (threadIdx.x >> 5);
+  if (gw >= nseg) return;  // the warps below take every segment
+  // at most one segment per warp of the grid's first half (resident from the
+  // start): warp gw takes segment gw, no queue
+  const bool fixed = 2 * nseg <= (long long)gridDim.x * (UW_T / 32);
+  long long next = gw;
+  if (!fixed) {
+    if (lane == 0) next = (long long)atomicAdd(&c.ctr->q_update_warp, 1ull);
+    next = __shfl_sync(kFull, next, 0);
+  }
   while (next < nseg) {
     const long long sj = next;
     // the segment after this one: claimed now, its descriptor fetched early
-    long long q = 0;
-    if (lane == 0) q = (long long)atomicAdd(&c.ctr->q_update_warp, 1ull);
-    next = __shfl_sync(kFull, q, 0);
+    long long q = nseg;
+    if (!fixed && lane == 0) q = (long long)atomicAdd(&c.ctr->q_update_warp, 1ull);
+    next = fixed ? nseg : __shfl_sync(kFull, q, 0);
     if (next < nseg && lane == 0) prefetch_l1(c.seg_desc + next);
     const int4 d = c.seg_desc[sj];
     const int nrec = d.y - d.x;
@@ -3086,7 +3195,7 @@ cudaError_t kernels_init() {
 
 void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   if (lc.staged) {
-    k_stage_points<<<lc.sm_count * 4, 256, 0, s>>>(c);
+    k_stage_points<<<lc.grid_sm * 4, 256, 0, s>>>(c);
     *launches += 1;
   }
   k_step_init<<<8, 256, 0, s>>>(c);
@@ -3094,7 +3203,7 @@ void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* la
 }
 
 void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  const int grid = lc.sm_count * (2048 / lc.ray_threads);
+  const int grid = lc.grid_sm * (2048 / lc.ray_threads);
   switch (lc.bucket_size) {
     case 1: k_ray_blocks<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
     case 2: k_ray_blocks<2><<<grid, lc.ray_threads, 0, s>>>(c); break;
@@ -3108,11 +3217,11 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int sel = lc.rank_passes & 1;
   const int pass_launches = 3 * lc.rank_passes;
-  k_gather_ranks<<<lc.sm_count * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing, sel, pass_launches);
+  k_gather_ranks<<<lc.grid_sm * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing, sel, pass_launches);
   *launches += 1;
   auto passes = [&](cudaStream_t st) {
     radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
-               lc.rank_passes, c.max_tiles_rank, lc.sm_count, st, launches, &c.ctr->rank_small);
+               lc.rank_passes, c.max_tiles_rank, lc.grid_sm, st, launches, &c.ctr->rank_small);
   };
   // in a graph the passes are the body of a conditional node that the last
   // CTA of k_gather_ranks switches off when it sorted the keys itself;
@@ -3124,12 +3233,12 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_alloc<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_passes);
+  k_alloc<<<lc.grid_sm * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_passes);
   *launches += 1;
 }
 
 void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  const int grid = lc.sm_count * (2048 / lc.ray_threads);
+  const int grid = lc.grid_sm * (2048 / lc.ray_threads);
   switch (lc.bucket_size) {
     case 1: k_ray_voxels<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
     case 2: k_ray_voxels<2><<<grid, lc.ray_threads, 0, s>>>(c); break;
@@ -3146,7 +3255,7 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   const int P = lc.rec_passes;
   auto pass = [&](int p, cudaStream_t st, const int* skip) {
     radix_pass(c, c.rec_key, c.rec_val, &c.hdr->rec_total, kRecSentinel, &c.ctr->n_rec_live, c.rec_cap, p,
-               c.max_tiles_rec, lc.sm_count, st, launches, skip);
+               c.max_tiles_rec, lc.grid_sm, st, launches, skip);
   };
   // (the last pass's three kernels return at once when k_alloc found it
   // empty: cheaper than a conditional node around them, measured)
@@ -3154,19 +3263,19 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   pass(P - 1, s, P > 1 ? &c.ctr->rec_skip_last : nullptr);
   SegHeadIn fin{c.rec_key[0], c.rec_key[1], &c.ctr->rec_sel};
   SegHeadOut fout{c.seg_start};
-  const int grid = lc.sm_count * 2;
+  const int grid = lc.grid_sm * 2;
   k_scan_reduce<<<grid, SC_T, 0, s>>>(fin, &c.ctr->n_rec_live, c.tile_sums, &c.ctr->n_seg, &c.ctr->done_seg);
   k_scan_apply<<<grid, SC_T, 0, s>>>(fin, fout, &c.ctr->n_rec_live, c.tile_sums);
-  k_seg_classify<<<lc.sm_count * 2, 256, 0, s>>>(c);
-  k_seg_count<<<lc.sm_count * 4, 256, 0, s>>>(c);
+  k_seg_classify<<<lc.grid_sm * 2, 256, 0, s>>>(c);
+  k_seg_count<<<lc.grid_sm * 4, 256, 0, s>>>(c);
   *launches += 5;
 }
 
 void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_heavy_count<<<lc.sm_count * 12, UPD_T, 0, s>>>(c);
-  k_heavy_scan<<<lc.sm_count * 8, HS_T, 0, s>>>(c);
-  k_heavy_scan_large<<<lc.sm_count, kVoxelsPerBlock, 0, s>>>(c);
-  k_heavy_place<<<lc.sm_count * 8, UPD_T, 0, s>>>(c);
+  k_heavy_count<<<lc.grid_sm * 12, UPD_T, 0, s>>>(c);
+  k_heavy_scan<<<lc.grid_sm * 8, HS_T, 0, s>>>(c);
+  k_heavy_scan_large<<<lc.grid_sm, kVoxelsPerBlock, 0, s>>>(c);
+  k_heavy_place<<<lc.grid_sm * 8, UPD_T, 0, s>>>(c);
   *launches += 4;
 }
 
@@ -3179,13 +3288,13 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   cudaEventRecord(lc.ev_fork, s);
   cudaStreamWaitEvent(lc.side2, lc.ev_fork, 0);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
-  k_hot_chains<<<lc.sm_count, 128, kHotSmem, lc.side2>>>(c);
+  k_hot_chains<<<lc.grid_sm, 128, kHotSmem, lc.side2>>>(c);
   if (lc.ev_branch[0]) record_timing_event(lc.ev_branch[0], lc.side2, lc.capturing);
-  k_heavy_update<<<lc.sm_count * 2, HU_T, kHuSmem, lc.side>>>(c);
+  k_heavy_update<<<lc.grid_sm * 2, HU_T, kHuSmem, lc.side>>>(c);
   if (lc.ev_branch[1]) record_timing_event(lc.ev_branch[1], lc.side, lc.capturing);
-  k_update_warp<<<lc.sm_count * 8, UW_T, 0, s>>>(c);
+  k_update_warp<<<lc.grid_sm * 8, UW_T, 0, s>>>(c);
   if (lc.ev_branch[2]) record_timing_event(lc.ev_branch[2], s, lc.capturing);
-  k_update<<<lc.sm_count * 2, UPD_T, 0, s>>>(c);
+  k_update<<<lc.grid_sm * 2, UPD_T, 0, s>>>(c);
   cudaEventRecord(lc.ev_join2, lc.side2);
   cudaEventRecord(lc.ev_join, lc.side);
   cudaStreamWaitEvent(s, lc.ev_join2, 0);
