@@ -159,7 +159,7 @@ struct Lane {
   long long* h_stats = nullptr; // [max_maps][ST_COUNT]
   LaneCounters* h_ctr = nullptr;
   MapCounters* h_mctr = nullptr;
-  // graphs keyed by (small batch, copy-out, staged inputs, rank_passes, rec_passes, timing)
+  // graphs keyed by (variant, copy-out, staged inputs, rank_passes, rec_passes, timing)
   std::map<int, cudaGraphExec_t> graphs;
   std::map<int, long long> graph_launches;
   cudaEvent_t ev_stage[STAGE_COUNT + 1] = {};
@@ -260,16 +260,20 @@ tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>*
   } while (0)
 
 // A batch of at most this many points runs the point-bound stages on grids
-// sized for an eighth of the SMs (its own graph).
+// sized for an eighth of the SMs.
 constexpr long long kSmallBatchPoints = 4096;
+// Pipeline variants a batch's bounds select (bits; each has its own graph).
+enum { VAR_SMALL_GRID = 1, VAR_RANK_IN_CTA = 2, VAR_REC_IN_CTA = 4 };
 
 LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes, bool staged,
-                     bool copyout, bool small) {
+                     bool copyout, int variant) {
   LaunchCfg lc;
   lc.staged = staged ? 1 : 0;
   lc.copyout = copyout ? 1 : 0;
   lc.sm_count = eng->sm_count;
-  lc.grid_sm = small ? std::max(1, eng->sm_count / 8) : eng->sm_count;
+  lc.grid_sm = (variant & VAR_SMALL_GRID) ? std::max(1, eng->sm_count / 8) : eng->sm_count;
+  lc.rank_in_cta = (variant & VAR_RANK_IN_CTA) ? 1 : 0;
+  lc.rec_in_cta = (variant & VAR_REC_IN_CTA) ? 1 : 0;
   lc.bucket_size = eng->cfg.bucket_size;
   lc.ray_threads = eng->cfg.ray_threads;
   lc.rank_passes = rank_passes;
@@ -417,11 +421,11 @@ void lane_free(Lane& L) {
 // Enqueue the pipeline of one step on the lane's stream (used directly or
 // inside a graph capture).  Returns the number of kernel launches.
 long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
-                           bool small, bool timed, bool capturing) {
-  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout, small);
+                           int variant, bool timed, bool capturing) {
+  LaunchCfg lc = launch_cfg(eng, L, rank_passes, rec_passes, staged, copyout, variant);
   lc.capturing = capturing ? 1 : 0;
   lc.cond_rank = cudaGraphConditionalHandle{};
-  if (capturing) {
+  if (capturing && !lc.rank_in_cta) {
     // the conditional handle of the graph being captured, default 1 (run) at every launch
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
@@ -444,22 +448,22 @@ long long enqueue_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_p
 }
 
 tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_passes, bool staged, bool copyout,
-                            bool small) {
+                            int variant) {
   NvtxRange nvtx_range("tsdf launch_pipeline");
   const bool timed = eng->stage_timing;
   L.timed = timed;
   if (eng->cfg.no_graphs) {
-    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, small, timed, false);
+    eng->launches += enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, variant, timed, false);
     CK(cudaGetLastError());
     return TSDF_OK;
   }
-  const int key = (small ? 10000 : 0) + (copyout ? 2000 : 0) + (staged ? 1000 : 0) + rank_passes * 100 +
+  const int key = variant * 10000 + (copyout ? 2000 : 0) + (staged ? 1000 : 0) + rank_passes * 100 +
                   rec_passes * 10 + (timed ? 1 : 0);
   auto it = L.graphs.find(key);
   if (it == L.graphs.end()) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
-    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, small, timed, true);
+    long long n = enqueue_pipeline(eng, L, rank_passes, rec_passes, staged, copyout, variant, timed, true);
     cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     cudaGraphExec_t ex = nullptr;
@@ -678,7 +682,12 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   L.step_timed = eng->timing != 0;
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[0], L.stream));
   CK(cudaMemcpyAsync(L.d_hdr, L.h_desc, sizeof(BatchHdr) + sizeof(ItemDev) * n, cudaMemcpyHostToDevice, L.stream));
-  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout, total <= kSmallBatchPoints));
+  int variant = 0;
+  if (total <= kSmallBatchPoints) variant |= VAR_SMALL_GRID;
+  if ((unsigned long long)std::max<long long>(total, 1) * rank_stride <= (unsigned long long)kSmallRank)
+    variant |= VAR_RANK_IN_CTA;  // bounds the step's new keys
+  if (hdr->rec_total <= kSmallRecs) variant |= VAR_REC_IN_CTA;
+  TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout, variant));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   // the step's stats and counters reach L.h_stats / h_ctr / h_mctr through
   // k_step_report, the graph's last kernel

@@ -21,6 +21,11 @@ constexpr int kMaxRadixPasses = 4;
 constexpr int kUpdEntries = 24;        // voxel updates of one point inside one block (<= 3*7+1 = 22)
 constexpr int kPubTsdfMsg = 1;            // ItemDev::out_fmt of a serialized Tsdf message (TSDF_PUB_TSDF_MSG)
 constexpr unsigned kBadLocal = 0xFFFFu;  // entry whose local voxel index fell outside its block
+// Up to kSmallRank new keys are sorted by rank in k_gather_ranks' last CTA,
+// and up to kSmallRecs routing records (empty routes included) by one CTA of
+// k_route_small; a step whose bounds fit launches no radix pass for them.
+constexpr int kSmallRank = 4096;
+constexpr int kSmallRecs = 8192;
 
 // One hash entry: packed block key, logical heap slot, first-touch rank.
 // Invariants: slot >= 0 only while the key is live; rank == kRankNone except
@@ -245,6 +250,8 @@ struct LaunchCfg {
   // small batch, whose few items would leave most CTAs of a full grid idle
   // (publish and gc follow the maps' sizes and keep sm_count)
   int grid_sm;
+  int rank_in_cta;  // at most kSmallRank new keys: no rank passes, no conditional node
+  int rec_in_cta;   // at most kSmallRecs records: one CTA runs the route stage (k_route_small)
   int bucket_size;   // 1, 2, 4, 8 or 16
   int ray_threads;
   int rank_passes;

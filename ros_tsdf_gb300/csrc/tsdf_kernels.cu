@@ -939,10 +939,10 @@ void capture_if(const LaunchCfg& lc, cudaStream_t s, cudaGraphConditionalHandle 
 // The new keys' (first-touch rank, hash entry) pairs for the rank sort; the
 // CTA that finishes last also writes every item's first index among the new
 // keys (exclusive prefix of the per-item new-key counts).
-// Up to this many new keys are sorted by rank in k_gather_ranks' last CTA
+// Up to kSmallRank new keys are sorted by rank in k_gather_ranks' last CTA
 // (bitonic, in shared memory); the radix passes then do nothing, and inside a
-// graph a conditional node does not launch them.
-constexpr int kSmallRank = 2048;
+// graph a conditional node does not launch them (or, when the step's bound
+// fits, the graph has neither).
 
 __global__ void __launch_bounds__(256) k_gather_ranks(Ctx c, cudaGraphConditionalHandle cond, int use_cond,
                                                       int rank_sel, int pass_launches) {
@@ -1299,6 +1299,28 @@ __device__ __forceinline__ void push_heavy(const Ctx& c, long long j) {
 // its descriptor and, where its record count decides, its class.
 __device__ void heavy_plan_cta(const Ctx& c);
 
+__device__ __forceinline__ void classify_segment(const Ctx& c, const long long* s_pb, const BatchHdr& h, long long j,
+                                                 long long nseg, long long nrec, const unsigned* rv,
+                                                 const unsigned* rk) {
+  const long long b0 = c.seg_start[j];
+  const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
+  const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
+  c.seg_item[j] = item;
+  // what the update kernels need first, in one 16-byte load
+  // record keys number the batch's slots (each map's below its high water,
+  // after the maps before it): back to the physical slot
+  const MapDev& m = c.maps[c.items[item].map];
+  const long long phys = m.heap_base + (long long)rk[b0] - c.item_i[item * II_COUNT + II_SLOT_BASE];
+  c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)phys, __float_as_int(m.maxw));
+  const long long n = b1 - b0;
+  if (n > kBcRec) {
+    push_heavy(c, j);
+  } else if (n * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates: k_seg_count counts them
+    const unsigned long long q = atomicAdd(&c.ctr->n_cand, 1ull);
+    c.cand[q] = (int)j;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_seg_classify(Ctx c) {
   const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   __shared__ long long s_pb[kMaxItems];
@@ -1310,23 +1332,29 @@ __global__ void __launch_bounds__(256) k_seg_classify(Ctx c) {
   const unsigned* rv = c.rec_val[rec_sel];
   const unsigned* rk = c.rec_key[rec_sel];
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nseg;
-       j += (long long)gridDim.x * blockDim.x) {
-    const long long b0 = c.seg_start[j];
-    const long long b1 = (j + 1 < nseg) ? c.seg_start[j + 1] : nrec;
-    const int item = find_item(s_pb, h.n_items, (long long)((rv[b0] >> 5) / (unsigned)h.vox_stride));
-    c.seg_item[j] = item;
-    // what the update kernels need first, in one 16-byte load
-    // record keys number the batch's slots (each map's below its high water,
-    // after the maps before it): back to the physical slot
-    const MapDev& m = c.maps[c.items[item].map];
-    const long long phys = m.heap_base + (long long)rk[b0] - c.item_i[item * II_COUNT + II_SLOT_BASE];
-    c.seg_desc[j] = make_int4((int)b0, (int)b1, (int)phys, __float_as_int(m.maxw));
-    const long long n = b1 - b0;
-    if (n > kBcRec) {
-      push_heavy(c, j);
-    } else if (n * kUpdEntries > kUwCap) {  // may hold more than kUwCap updates: k_seg_count counts them
-      const unsigned long long q = atomicAdd(&c.ctr->n_cand, 1ull);
-      c.cand[q] = (int)j;
+       j += (long long)gridDim.x * blockDim.x)
+    classify_segment(c, s_pb, h, j, nseg, nrec, rv, rk);
+}
+
+// One warp: candidate segment sj's update count (eight loads per lane in
+// flight), and its class.
+__device__ __forceinline__ void count_candidate(const Ctx& c, int sj, const unsigned* rv, int lane) {
+  const int4 d = c.seg_desc[sj];
+  int e = 0;
+  for (int r = d.x + lane; r < d.y; r += 256) {
+    unsigned v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = r + 32 * u < d.y ? rv[r + 32 * u] : 0u;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) e += (int)(v[u] & 31u);
+  }
+  e = __reduce_add_sync(kFull, e);
+  if (lane == 0) {
+    if (e > kBcCap) {
+      push_heavy(c, sj);
+    } else if (d.y - d.x > UPD_T || e > kUwCap) {
+      const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
+      c.bcta[q] = sj;
     }
   }
 }
@@ -1341,28 +1369,132 @@ __global__ void __launch_bounds__(256) k_seg_count(Ctx c) {
   const unsigned* rv = c.rec_val[rec_sel];
   const int lane = threadIdx.x & 31;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; k < ncand; k += nwarps) {
-    const int sj = c.cand[k];
-    const int4 d = c.seg_desc[sj];
-    int e = 0;
-    for (int r = d.x + lane; r < d.y; r += 256) {
-      unsigned v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = r + 32 * u < d.y ? rv[r + 32 * u] : 0u;
-#pragma unroll
-      for (int u = 0; u < 8; ++u) e += (int)(v[u] & 31u);
-    }
-    e = __reduce_add_sync(kFull, e);
-    if (lane == 0) {
-      if (e > kBcCap) {
-        push_heavy(c, sj);
-      } else if (d.y - d.x > UPD_T || e > kUwCap) {
-        const unsigned long long q = atomicAdd(&c.ctr->n_bcta, 1ull);
-        c.bcta[q] = sj;
-      }
-    }
-  }
+  for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; k < ncand; k += nwarps)
+    count_candidate(c, c.cand[k], rv, lane);
   if (last_cta(&c.ctr->done_classify)) heavy_plan_cta(c);
+}
+
+// The route stage of a small step in one CTA (at most kSmallRecs records,
+// empty routes included), in place of the record sort's passes and the four
+// kernels after them:
+//  - the live records (key below the step's limit) gathered in index order;
+//  - a stable LSD sort by key, 8-bit digits, as many passes as the largest
+//    key needs: each warp ranks a contiguous run of the records (match_any
+//    per 32), the (digit, warp) counts are scanned digit-major, and every
+//    record goes to its digit's place for its warp plus its rank there;
+//  - the sorted keys and values into the second record buffer, the segment
+//    heads scanned into seg_start;
+//  - classify_segment per segment, count_candidate per candidate, and the
+//    heavy segments' plan, as k_seg_classify and k_seg_count do on the grid.
+// Equal keys keep their index order, as in the passes' stable sort.
+constexpr int kRouteT = 1024;
+constexpr int kRouteSmem = kSmallRecs * 2 * ((int)sizeof(unsigned) + (int)sizeof(unsigned short)) +
+                           256 * (kRouteT / 32) * (int)sizeof(int);
+__global__ void __launch_bounds__(kRouteT) k_route_small(Ctx c) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  unsigned* key_a = reinterpret_cast<unsigned*>(s_dyn);
+  unsigned* key_b = key_a + kSmallRecs;
+  int* hist = reinterpret_cast<int*>(key_b + kSmallRecs);  // [digit][warp]
+  unsigned short* idx_a = reinterpret_cast<unsigned short*>(hist + 256 * (kRouteT / 32));
+  unsigned short* idx_b = idx_a + kSmallRecs;
+  __shared__ long long s_pb[kMaxItems];
+  __shared__ int s_warp[32];
+  __shared__ unsigned s_maxk;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const BatchHdr h = *c.hdr;
+  for (int i = t; i < h.n_items; i += kRouteT) s_pb[i] = c.items[i].point_base;
+  if (t == 0) {
+    s_maxk = 0u;
+    if (h.rec_total > kSmallRecs) set_error(c.ctr, ERR_CAPACITY);  // the host picks this path only below the bound
+  }
+  __syncthreads();
+  // live records in index order
+  const int n = (int)min(h.rec_total, (long long)kSmallRecs);
+  const unsigned* k0 = c.rec_key[0];
+  int m = 0;
+  unsigned kmax = 0u;
+  for (int b = 0; b < n; b += kRouteT) {
+    const int i = b + t;
+    const unsigned k = i < n ? k0[i] : h.rec_key_limit;
+    const int live = k < h.rec_key_limit ? 1 : 0;
+    int tot;
+    const int ex = block_excl_scan(live, s_warp, &tot);
+    if (live) key_a[m + ex] = k, idx_a[m + ex] = (unsigned short)i, kmax = max(kmax, k);
+    m += tot;
+  }
+  kmax = __reduce_max_sync(kFull, kmax);
+  if (lane == 0) atomicMax(&s_maxk, kmax);
+  __syncthreads();
+  kmax = s_maxk;
+  // stable LSD passes
+  const int run = (((m + 31) / 32) + 31) & ~31;  // records per warp, a multiple of 32
+  const int w0 = min(m, warp * run), w1 = min(m, w0 + run);
+  for (int shift = 0; m > 0 && (shift == 0 || (shift < 32 && (kmax >> shift) != 0u)); shift += 8) {
+    for (int i = t; i < 256 * (kRouteT / 32); i += kRouteT) hist[i] = 0;
+    __syncthreads();
+    for (int g = w0; g < w1; g += 32) {  // warp-uniform bounds
+      const int i = g + lane;
+      const int d = i < w1 ? (int)((key_a[i] >> shift) & 255u) : 256;
+      const unsigned peers = __match_any_sync(kFull, d);
+      if (d < 256 && lane == __ffs(peers) - 1) hist[d * (kRouteT / 32) + warp] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    {
+      constexpr int kPer = 256 * (kRouteT / 32) / kRouteT;
+      int v[kPer], sum = 0;
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) v[k] = hist[kPer * t + k], sum += v[k];
+      int tot;
+      int ex = block_excl_scan(sum, s_warp, &tot);
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) hist[kPer * t + k] = ex, ex += v[k];
+    }
+    __syncthreads();
+    for (int g = w0; g < w1; g += 32) {
+      const int i = g + lane;
+      const bool ok = i < w1;
+      const unsigned k = ok ? key_a[i] : 0u;
+      const int d = ok ? (int)((k >> shift) & 255u) : 256;
+      const unsigned peers = __match_any_sync(kFull, d);
+      if (ok) {
+        const int pos = hist[d * (kRouteT / 32) + warp] + __popc(peers & lt);
+        key_b[pos] = k;
+        idx_b[pos] = idx_a[i];
+      }
+      __syncwarp();
+      if (ok && lane == __ffs(peers) - 1) hist[d * (kRouteT / 32) + warp] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    unsigned* tk = key_a;
+    key_a = key_b, key_b = tk;
+    unsigned short* ti = idx_a;
+    idx_a = idx_b, idx_b = ti;
+  }
+  // sorted records out; segment heads
+  const unsigned* v0 = c.rec_val[0];
+  unsigned* rk = c.rec_key[1];
+  unsigned* rv = c.rec_val[1];
+  for (int i = t; i < m; i += kRouteT) rk[i] = key_a[i], rv[i] = v0[idx_a[i]];
+  long long nseg = 0;
+  for (int b = 0; b < m; b += kRouteT) {
+    const int i = b + t;
+    const int head = (i < m && (i == 0 || key_a[i] != key_a[i - 1])) ? 1 : 0;
+    int tot;
+    const int ex = block_excl_scan(head, s_warp, &tot);
+    if (head) c.seg_start[nseg + ex] = i;
+    nseg += tot;
+  }
+  if (t == 0) c.ctr->n_rec_live = m, c.ctr->n_seg = nseg;
+  __syncthreads();
+  for (long long j = t; j < nseg; j += kRouteT) classify_segment(c, s_pb, h, j, nseg, m, rv, rk);
+  __syncthreads();
+  const long long ncand = (long long)__ldcg(&c.ctr->n_cand);
+  for (long long k = warp; k < ncand; k += kRouteT / 32) count_candidate(c, __ldcg(c.cand + k), rv, lane);
+  __syncthreads();
+  heavy_plan_cta(c);
 }
 
 
@@ -3190,6 +3322,8 @@ void launch_check_div(unsigned long long seed, long long n, unsigned long long* 
 cudaError_t kernels_init() {
   cudaError_t e = cudaFuncSetAttribute(k_heavy_update, cudaFuncAttributeMaxDynamicSharedMemorySize, kHuSmem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_route_small, cudaFuncAttributeMaxDynamicSharedMemorySize, kRouteSmem);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_hot_chains, cudaFuncAttributeMaxDynamicSharedMemorySize, kHotSmem);
 }
 
@@ -3217,8 +3351,10 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int sel = lc.rank_passes & 1;
   const int pass_launches = 3 * lc.rank_passes;
-  k_gather_ranks<<<lc.grid_sm * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing, sel, pass_launches);
+  k_gather_ranks<<<lc.grid_sm * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing && !lc.rank_in_cta, sel,
+                                                pass_launches);
   *launches += 1;
+  if (lc.rank_in_cta) return;  // at most kSmallRank new keys: k_gather_ranks' last CTA sorts them
   auto passes = [&](cudaStream_t st) {
     radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
                lc.rank_passes, c.max_tiles_rank, lc.grid_sm, st, launches, &c.ctr->rank_small);
@@ -3233,7 +3369,8 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
 }
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  k_alloc<<<lc.grid_sm * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_passes);
+  // (one record pass's parity when k_route_small writes the second buffer)
+  k_alloc<<<lc.grid_sm * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_in_cta ? 1 : lc.rec_passes);
   *launches += 1;
 }
 
@@ -3259,6 +3396,11 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
   };
   // (the last pass's three kernels return at once when k_alloc found it
   // empty: cheaper than a conditional node around them, measured)
+  if (lc.rec_in_cta) {  // at most kSmallRecs records: the whole stage in one CTA
+    k_route_small<<<1, kRouteT, kRouteSmem, s>>>(c);
+    *launches += 1;
+    return;
+  }
   for (int p = 0; p + 1 < P; ++p) pass(p, s, nullptr);
   pass(P - 1, s, P > 1 ? &c.ctr->rec_skip_last : nullptr);
   SegHeadIn fin{c.rec_key[0], c.rec_key[1], &c.ctr->rec_sel};
