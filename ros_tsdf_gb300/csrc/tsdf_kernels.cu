@@ -1384,8 +1384,10 @@ __global__ void __launch_bounds__(256) k_seg_count(Ctx c) {
 //    record goes to its digit's place for its warp plus its rank there;
 //  - the sorted keys and values into the second record buffer, the segment
 //    heads scanned into seg_start;
-//  - classify_segment per segment, count_candidate per candidate, and the
-//    heavy segments' plan, as k_seg_classify and k_seg_count do on the grid.
+//  - classify_segment per segment and count_candidate per candidate, as
+//    k_seg_classify and k_seg_count do on the grid.  No heavy segment is
+//    planned for the counting sort: a small step's grid-heavy segments all
+//    go through k_update's passes, and its pipeline has no heavy-bin stage.
 // Equal keys keep their index order, as in the passes' stable sort.
 constexpr int kRouteT = 1024;
 constexpr int kRouteSmem = kSmallRecs * 2 * ((int)sizeof(unsigned) + (int)sizeof(unsigned short)) +
@@ -1493,8 +1495,6 @@ __global__ void __launch_bounds__(kRouteT) k_route_small(Ctx c) {
   __syncthreads();
   const long long ncand = (long long)__ldcg(&c.ctr->n_cand);
   for (long long k = warp; k < ncand; k += kRouteT / 32) count_candidate(c, __ldcg(c.cand + k), rv, lane);
-  __syncthreads();
-  heavy_plan_cta(c);
 }
 
 
@@ -3414,6 +3414,7 @@ void stage_route_sort(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_heavy_bins(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  if (lc.rec_in_cta) return;  // k_route_small plans no heavy segment
   k_heavy_count<<<lc.grid_sm * 12, UPD_T, 0, s>>>(c);
   k_heavy_scan<<<lc.grid_sm * 8, HS_T, 0, s>>>(c);
   k_heavy_scan_large<<<lc.grid_sm, kVoxelsPerBlock, 0, s>>>(c);
@@ -3427,6 +3428,17 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   // sort's capacity) touch disjoint voxels: the first two are forked onto
   // the lane's side streams, launched before k_update so the chains start at
   // once, and all three join before the publish stage
+  if (lc.rec_in_cta) {
+    // a small step (k_route_small): no hot chains or binned heavy segments,
+    // its grid-heavy segments all in k_update's passes
+    for (int k = 0; k < 2; ++k)
+      if (lc.ev_branch[k]) record_timing_event(lc.ev_branch[k], s, lc.capturing);
+    k_update_warp<<<lc.grid_sm * 8, UW_T, 0, s>>>(c);
+    if (lc.ev_branch[2]) record_timing_event(lc.ev_branch[2], s, lc.capturing);
+    k_update<<<lc.grid_sm * 2, UPD_T, 0, s>>>(c);
+    *launches += 2;
+    return;
+  }
   cudaEventRecord(lc.ev_fork, s);
   cudaStreamWaitEvent(lc.side2, lc.ev_fork, 0);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);

@@ -188,6 +188,44 @@ def test_publish_overflow_truncates(built):
         assert np.array_equal(r.pos, pos) and np.array_equal(r.data, data)
 
 
+def _cluster_scan(rng, n, origin, direction, dist, spread):
+    """n points about dist along direction from origin, jittered by spread:
+    their rays share the blocks around the surface."""
+    d = np.asarray(direction, np.float64)
+    d /= np.linalg.norm(d)
+    pts = origin + d * dist + rng.uniform(-spread, spread, (n, 3))
+    return pts.astype(np.float32)
+
+
+@pytest.mark.parametrize("n_points", [480, 650, 3000])
+def test_small_steps_dense_cluster_match_oracle(built, n_points):
+    """Small steps whose rays all cross the same few blocks: segments of
+    hundreds of records and thousands of updates (grid-heavy, hot chains)
+    through the small-batch pipeline (480: new-key ranks and the route stage
+    in one CTA; 650: the route stage in one CTA; 3000: small grids, radix
+    passes), against the oracle."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+
+    spec = W.plain_small(seed=0, heap_blocks=4096)
+    T = spec.params.truncation_distance
+    orc = _oracle(spec.params, 4096)
+    rng = np.random.default_rng(n_points)
+    with Engine(max_maps=2, pool_blocks=4096, max_batch_points=1 << 14) as eng:
+        mid = eng.create_map(spec.params, 4096)
+        per_block = []
+        for k in range(4):
+            org = np.full(3, 0.3 + 0.05 * k, np.float32)
+            xyz = _cluster_scan(rng, n_points, org, (1.0, 0.9, 0.8), 12.0, 0.05)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 18)
+            assert r.status == 0
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 18), T, f"step {k}")
+            per_block.append(r.stats["voxel_updates"] / max(r.stats["blocks_touched"], 1))
+        # four or five blocks hold every update: none of them is light, and
+        # from 650 points on some hold more than a CTA's 4096
+        assert min(per_block) > 2048 and (n_points < 650 or max(per_block) > 4096)
+        assert_state_equal(eng, mid, orc, 4096)
+
+
 def test_bad_points_empty_scan_and_pcl_stride(built):
     from ros_tsdf_gb300 import Engine, workloads as W
     from ros_tsdf_gb300 import _lib as L
