@@ -1247,6 +1247,157 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels(Ctx c) {
   }
 }
 
+// The voxel pass of a small step (single-entry buckets): one warp per point.
+// Lane 0 walks the voxel DDA, 32 cells at a time into shared memory; then
+// lane i takes cell i of the window: its block key, whether it starts a run
+// (its key differs from the cell before it), the run's index and first cell
+// (ballot over the run starts), the run's slot (the run's first lane looks
+// it up; every run of the window at once) and the cell's entry.  A run's
+// record is written when the next run starts (in its window or at the next
+// window's first cell) or after the ray's last cell.  Records, entries and
+// counters are those of k_ray_voxels<1>: a cell's place in its run is its
+// distance from the run's first cell, the count of a run whose block is
+// missing is zero.  It cuts the per-point latency that bounds a step of a
+// few hundred points: the walk's cells no longer wait on their own local
+// index, distance and entry.
+constexpr int kRayWarpT = 128;
+__global__ void __launch_bounds__(kRayWarpT) k_ray_voxels_warp(Ctx c) {
+  constexpr int kW = kRayWarpT / 32;
+  __shared__ long long s_pb[kMaxItems];
+  __shared__ float s_vc[kW][3][32];
+  const BatchHdr h = *c.hdr;
+  const long long total = h.total_points;
+  if ((long long)blockIdx.x * kW >= total) return;  // uniform
+  for (int i = threadIdx.x; i < h.n_items; i += kRayWarpT) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const int R = h.rec_stride;
+  const int VS = h.vox_stride;
+  unsigned* rk = c.rec_key[0];
+  unsigned* rv = c.rec_val[0];
+  uint2* ent = c.entries;
+  const long long nwarps = (long long)gridDim.x * kW;
+  for (long long g = (long long)blockIdx.x * kW + w; g < total; g += nwarps) {
+    const int item = find_item(s_pb, h.n_items, g);
+    const ItemDev& it = c.items[item];
+    const MapDev& m = c.maps[it.map];
+    const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
+    const float px = p[0], py = p[1], pz = p[2];
+    const float ox = it.ox, oy = it.oy, oz = it.oz;
+    Seg seg;
+    const bool valid = make_segment(px, py, pz, ox, oy, oz, m, &seg);  // uniform: every lane, the same point
+    Dda dda;
+    if (valid && lane == 0) dda.init(seg, m.vs, m.scale_v, m.rs_v, m.half_vs, m.vmax);
+    const HEntry* tab = c.hash + m.hash_base;
+    const unsigned mask = m.hash_mask;
+    const long long kbase = c.item_i[item * II_COUNT + II_SLOT_BASE];
+    const float scale_b = m.scale_b, rs_b = m.rs_b, half_bs = m.half_bs, vs = m.vs, r_vs = m.r_vs;
+    const int rmax = m.rmax;
+    const long long rbase = g * (long long)R;
+    const long long ebase = g * (long long)VS;
+    // the open run (warp-uniform): its key, index, first cell and slot
+    unsigned long long cur = kEmptyKey;
+    int run = -1, run_start = 0, run_slot = -1, j0 = 0;
+    unsigned route_ovf = 0, missing = 0, bad = 0;
+    auto write_record = [&](int r, int start, int slot, int len) {
+      if (r >= 0 && r < rmax) {
+        rk[rbase + r] = slot >= 0 ? (unsigned)(kbase + slot) : kRecSentinel;
+        rv[rbase + r] = ((unsigned)(ebase + start) << 5) | (unsigned)(slot >= 0 ? min(len, 31) : 0);
+      }
+    };
+    bool more = valid;
+    while (more) {
+      int n = 0;
+      bool more0 = false;
+      if (lane == 0) {
+        float x, y, z;
+        int kx, ky, kz;
+        while (n < 32 && dda.next(&x, &y, &z, &kx, &ky, &kz)) {
+          s_vc[w][0][n] = x, s_vc[w][1][n] = y, s_vc[w][2][n] = z;
+          ++n;
+        }
+        more0 = n == 32 && !dda.done;
+      }
+      n = __shfl_sync(kFull, n, 0);
+      more = __shfl_sync(kFull, more0, 0);
+      __syncwarp();
+      const bool has = lane < n;
+      const int j = j0 + lane;
+      float x = 0.f, y = 0.f, z = 0.f, fbx = 0.f, fby = 0.f, fbz = 0.f;
+      unsigned long long bkey = 0ull;
+      if (has) {
+        x = s_vc[w][0][lane], y = s_vc[w][1][lane], z = s_vc[w][2][lane];
+        fbx = floorf(fmul(x, scale_b));
+        fby = floorf(fmul(y, scale_b));
+        fbz = floorf(fmul(z, scale_b));
+        bkey = pack_key((int)fbx, (int)fby, (int)fbz);
+      }
+      __syncwarp();  // the window is read before lane 0 writes the next one
+      unsigned long long prev = __shfl_up_sync(kFull, bkey, 1);
+      if (lane == 0) prev = cur;
+      const bool newrun = has && bkey != prev;
+      const unsigned nr = __ballot_sync(kFull, newrun);
+      const unsigned upto = nr & (lt | (1u << lane));  // run starts at or before this cell
+      const int src = upto ? 31 - __clz(upto) : -1;   // the lane of this cell's run start
+      const int my_run = run + __popc(upto);
+      const int my_start = src >= 0 ? j0 + src : run_start;
+      int slot0 = -1;
+      if (newrun && my_run < rmax) slot0 = probe_resolve(tab, mask, bkey, load_entry_ro(tab + ((unsigned)mix64(bkey) & mask)));
+      int my_slot = __shfl_sync(kFull, slot0, src >= 0 ? src : 0);
+      if (src < 0) my_slot = run_slot;
+      // the open run closes at this window's first run start
+      if (lane == 0 && newrun) write_record(run, run_start, run_slot, j0 - run_start);
+      if (has) {
+        if (my_run >= rmax) {
+          ++route_ovf;
+        } else if (my_slot < 0) {
+          ++missing;
+        } else if (j - my_start >= 31) {
+          ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
+        } else {
+          // block corner (tsdf_handler.cu:612-624); getLocalVoxelIndex (:507-512)
+          const float blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
+          const float bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
+          const float blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
+          const float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
+          const float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
+          const float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
+          unsigned local = kBadLocal;
+          if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
+            local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
+          else
+            ++bad;
+          const float d = distance_update(x, y, z, px, py, pz, ox, oy, oz);
+          ent[ebase + j] = make_uint2(__float_as_uint(d), local);
+        }
+        // a run that closes at the next cell of this window
+        if (lane + 1 < n && ((nr >> (lane + 1)) & 1u)) write_record(my_run, my_start, my_slot, j + 1 - my_start);
+      }
+      if (n > 0) {
+        cur = __shfl_sync(kFull, bkey, n - 1);
+        run = __shfl_sync(kFull, my_run, n - 1);
+        run_start = __shfl_sync(kFull, my_start, n - 1);
+        run_slot = __shfl_sync(kFull, my_slot, n - 1);
+        j0 += n;
+      }
+    }
+    if (lane == 0) write_record(run, run_start, run_slot, j0 - run_start);
+    const int first = valid ? min(run + 1, rmax) : 0;
+    for (int r = first + lane; r < R; r += 32) rk[rbase + r] = kRecSentinel;
+    route_ovf = __reduce_add_sync(kFull, route_ovf);
+    missing = __reduce_add_sync(kFull, missing);
+    bad = __reduce_add_sync(kFull, bad);
+    if (lane == 0) {
+      stat_add(c.item_stats, item, ST_VOVF, (valid && dda.ovf) ? 1 : 0);
+      stat_add(c.item_stats, item, ST_ROVF, route_ovf);
+      stat_add(c.item_stats, item, ST_MISS, missing);
+      stat_add(c.item_stats, item, ST_BADLOCAL, bad);
+    }
+    __syncwarp();
+  }
+}
+
 // segment heads of the sorted records
 struct SegHeadIn {
   const unsigned* k0;
@@ -3375,6 +3526,11 @@ void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* l
 }
 
 void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  if (lc.ray_warp) {  // a few hundred points, single-entry buckets: a warp per point
+    k_ray_voxels_warp<<<lc.grid_sm * 16, kRayWarpT, 0, s>>>(c);
+    *launches += 1;
+    return;
+  }
   const int grid = lc.grid_sm * (2048 / lc.ray_threads);
   switch (lc.bucket_size) {
     case 1: k_ray_voxels<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
