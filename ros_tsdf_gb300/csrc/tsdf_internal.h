@@ -26,7 +26,7 @@ constexpr unsigned kBadLocal = 0xFFFFu;  // entry whose local voxel index fell o
 // k_route_small; a step whose bounds fit launches no radix pass for them.
 constexpr int kSmallRank = 4096;
 constexpr int kSmallRecs = 8192;
-// Up to this many points, the voxel pass runs one warp per point.
+// Up to this many points, the block and voxel passes run one warp per point.
 constexpr int kRayWarpPoints = 1024;
 
 // One hash entry: packed block key, logical heap slot, first-touch rank.
@@ -254,7 +254,7 @@ struct LaunchCfg {
   int grid_sm;
   int rank_in_cta;  // at most kSmallRank new keys: no rank passes, no conditional node
   int rec_in_cta;   // at most kSmallRecs records: one CTA runs the route stage (k_route_small)
-  int ray_warp;     // at most kRayWarpPoints points, single-entry buckets: k_ray_voxels_warp
+  int ray_warp;     // at most kRayWarpPoints points, single-entry buckets: k_ray_blocks_warp, k_ray_voxels_warp
   int bucket_size;   // 1, 2, 4, 8 or 16
   int ray_threads;
   int rank_passes;

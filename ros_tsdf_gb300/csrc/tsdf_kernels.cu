@@ -652,6 +652,85 @@ __global__ void __launch_bounds__(256) k_ray_blocks(Ctx c) {
   }
 }
 
+// The block pass of a small step (single-entry buckets): one warp per point.
+// Lane 0 walks the block DDA, 32 cells at a time into shared memory; the
+// lanes then find-or-claim one cell each, all at once (the cells of one ray
+// are distinct blocks).  Ranks, claims, new-key list and counters are those
+// of k_ray_blocks<1>.
+constexpr int kRayWarpT_B = 128;
+__global__ void __launch_bounds__(kRayWarpT_B) k_ray_blocks_warp(Ctx c) {
+  constexpr int kW = kRayWarpT_B / 32;
+  __shared__ long long s_pb[kMaxItems];
+  __shared__ int s_bc[kW][3][32];
+  const BatchHdr h = *c.hdr;
+  const long long total = h.total_points;
+  if ((long long)blockIdx.x * kW >= total) return;  // uniform
+  for (int i = threadIdx.x; i < h.n_items; i += kRayWarpT_B) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long nwarps = (long long)gridDim.x * kW;
+  for (long long g = (long long)blockIdx.x * kW + w; g < total; g += nwarps) {
+    const int item = find_item(s_pb, h.n_items, g);
+    const ItemDev& it = c.items[item];
+    const int mi = it.map;
+    const MapDev& m = c.maps[mi];
+    const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
+    Seg seg;
+    const bool valid = make_segment(p[0], p[1], p[2], it.ox, it.oy, it.oz, m, &seg);  // uniform
+    Dda dda;
+    if (valid && lane == 0) dda.init(seg, m.bs, m.scale_b, m.rs_b, m.half_bs, m.amax);
+    HEntry* tab = c.hash + m.hash_base;
+    const unsigned mask = m.hash_mask;
+    const unsigned own = 1u << lane;
+    int j0 = 0;
+    bool more = valid;
+    while (more) {
+      int n = 0;
+      bool more0 = false;
+      if (lane == 0) {
+        float x, y, z;
+        int kx, ky, kz;
+        while (n < 32 && dda.next(&x, &y, &z, &kx, &ky, &kz)) {
+          s_bc[w][0][n] = kx, s_bc[w][1][n] = ky, s_bc[w][2][n] = kz;
+          ++n;
+        }
+        more0 = n == 32 && !dda.done;
+      }
+      n = __shfl_sync(kFull, n, 0);
+      more = __shfl_sync(kFull, more0, 0);
+      __syncwarp();
+      int kx = 0, ky = 0, kz = 0;
+      if (lane < n) kx = s_bc[w][0][lane], ky = s_bc[w][1][lane], kz = s_bc[w][2][lane];
+      __syncwarp();  // the window is read before lane 0 writes the next one
+      if (lane < n) {
+        const unsigned rank = (unsigned)(g * (long long)h.rank_stride + j0 + lane);
+        unsigned entry = 0;
+        bool from_empty = false;
+        const int res = group_insert<1>(tab, mask, pack_key(kx, ky, kz), rank, 0, lane, own, &entry, &from_empty);
+        if (res == INS_NEW) {
+          unsigned long long slot = atomicAdd(reinterpret_cast<unsigned long long*>(&c.ctr->n_new), 1ull);
+          long long gidx = (long long)(tab - c.hash) + entry;
+          if ((long long)slot < c.rank_cap)
+            c.newlist[slot] = (unsigned)gidx;
+          else
+            set_error(c.ctr, ERR_CAPACITY);
+          atomicAdd(&c.item_i[item * II_COUNT + II_NEW], 1);
+          if (from_empty) atomicAdd(&c.mctr[mi].hash_used, 1);
+        } else if (res == INS_FULL) {
+          set_error(c.ctr, ERR_HASH_FULL);
+        }
+      }
+      j0 += n;
+    }
+    if (lane == 0) {
+      stat_add(c.item_stats, item, ST_BINC, j0);
+      stat_add(c.item_stats, item, ST_BAD, valid ? 0 : 1);
+      stat_add(c.item_stats, item, ST_BOVF, (valid && dda.ovf) ? 1 : 0);
+    }
+    __syncwarp();
+  }
+}
+
 // ----------------------------------------------------------------------------
 // generic exclusive scan (3 kernels, grid-fixed, n read on the device)
 constexpr int SC_T = 256;
@@ -3488,6 +3567,11 @@ void stage_init(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* la
 }
 
 void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  if (lc.ray_warp) {  // a few hundred points, single-entry buckets: a warp per point
+    k_ray_blocks_warp<<<lc.grid_sm * 16, kRayWarpT_B, 0, s>>>(c);
+    *launches += 1;
+    return;
+  }
   const int grid = lc.grid_sm * (2048 / lc.ray_threads);
   switch (lc.bucket_size) {
     case 1: k_ray_blocks<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
