@@ -2838,18 +2838,21 @@ __global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
         if (lane >= o) wb += y;
       }
       wb -= __popc(my_mask);  // records starting before window `lane`
+      // (the window loops leave at the segment's last window: a skipped
+      // window's code is then not even fetched, which matters to a warp that
+      // runs this code cold)
       uint2 xs[kUwCap / 32];
 #pragma unroll
+      for (int i = 0; i < kUwCap / 32; ++i) xs[i] = make_uint2(0u, kBadLocal);
+#pragma unroll
       for (int i = 0; i < kUwCap / 32; ++i) {
+        if (32 * i >= n_ent) break;  // uniform
         const int f = 32 * i + lane;
-        xs[i] = make_uint2(0u, kBadLocal);
-        if (32 * i < n_ent) {  // uniform: the windows past the segment's updates cost nothing
-          const unsigned wm = __shfl_sync(kFull, my_mask, i);
-          const int wbi = __shfl_sync(kFull, wb, i);
-          if (f < n_ent) {
-            const int j = wbi + __popc(wm << (31 - lane)) - 1;
-            xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
-          }
+        const unsigned wm = __shfl_sync(kFull, my_mask, i);
+        const int wbi = __shfl_sync(kFull, wb, i);
+        if (f < n_ent) {
+          const int j = wbi + __popc(wm << (31 - lane)) - 1;
+          xs[i] = c.entries[ebase[j] + (unsigned)(f - rpos[j])];
         }
       }
       // the next segment's record values into L1 while these loads are in flight
@@ -2860,24 +2863,23 @@ __global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
       int maxdep = 0;
 #pragma unroll
       for (int i = 0; i < kUwCap / 32; ++i) {
-        if (32 * i < n_ent) {  // uniform
-          const unsigned l = xs[i].y;
-          const bool ok = l != kBadLocal;
-          const unsigned pv = __match_any_sync(kFull, ok ? l : (0x10000u | lane));
-          int dep = 0;
-          if (ok) dep = (int)sm.cnt[l] + __popc(pv & lt);
-          const unsigned pd = __match_any_sync(kFull, ok ? (unsigned)dep : (0x10000u | lane));
-          int pil = 0;
-          // dep < nrec <= 128: a record updates a voxel at most once (the
-          // mask only keeps the index inside the array)
-          if (ok) pil = sm.lvl[dep & 127] + __popc(pd & lt);
-          __syncwarp();
-          if (ok && (pv >> lane) == 1u) sm.cnt[l] = (unsigned char)(dep + 1);
-          if (ok && (pd >> lane) == 1u) sm.lvl[dep & 127] = pil + 1;
-          __syncwarp();
-          if (ok) ++n_upd, maxdep = max(maxdep, dep);
-          xs[i].y = ok ? (l | ((unsigned)dep << 9) | ((unsigned)pil << 16)) : kUwNone;
-        }
+        if (32 * i >= n_ent) break;  // uniform
+        const unsigned l = xs[i].y;
+        const bool ok = l != kBadLocal;
+        const unsigned pv = __match_any_sync(kFull, ok ? l : (0x10000u | lane));
+        int dep = 0;
+        if (ok) dep = (int)sm.cnt[l] + __popc(pv & lt);
+        const unsigned pd = __match_any_sync(kFull, ok ? (unsigned)dep : (0x10000u | lane));
+        int pil = 0;
+        // dep < nrec <= 128: a record updates a voxel at most once (the
+        // mask only keeps the index inside the array)
+        if (ok) pil = sm.lvl[dep & 127] + __popc(pd & lt);
+        __syncwarp();
+        if (ok && (pv >> lane) == 1u) sm.cnt[l] = (unsigned char)(dep + 1);
+        if (ok && (pd >> lane) == 1u) sm.lvl[dep & 127] = pil + 1;
+        __syncwarp();
+        if (ok) ++n_upd, maxdep = max(maxdep, dep);
+        xs[i].y = ok ? (l | ((unsigned)dep << 9) | ((unsigned)pil << 16)) : kUwNone;
       }
       const int n_dep = __reduce_max_sync(kFull, (unsigned)maxdep) + 1;
       // ---- (B) depth bases, entries depth-major, touched voxels loaded
@@ -2900,8 +2902,9 @@ __global__ void __launch_bounds__(UW_T, 6) k_update_warp(Ctx c) {
       __syncwarp();
 #pragma unroll
       for (int i = 0; i < kUwCap / 32; ++i) {
+        if (32 * i >= n_ent) break;  // uniform
         const uint2 x = xs[i];
-        if (32 * i < n_ent && x.y != kUwNone)  // packed by the depth pass
+        if (x.y != kUwNone)  // packed by the depth pass
           sm.sorted[sm.lvl[(x.y >> 9) & 127u] + (int)(x.y >> 16)] = make_uint2(x.x, x.y & 511u);
       }
       __syncwarp();
@@ -3669,13 +3672,18 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
   // the lane's side streams, launched before k_update so the chains start at
   // once, and all three join before the publish stage
   if (lc.rec_in_cta) {
-    // a small step (k_route_small): no hot chains or binned heavy segments,
-    // its grid-heavy segments all in k_update's passes
-    for (int k = 0; k < 2; ++k)
-      if (lc.ev_branch[k]) record_timing_event(lc.ev_branch[k], s, lc.capturing);
+    // a small step (k_route_small): no hot chains or binned heavy segments;
+    // its grid-heavy segments all go through k_update's passes, on the side
+    // stream beside k_update_warp (disjoint segments)
+    if (lc.ev_branch[0]) record_timing_event(lc.ev_branch[0], s, lc.capturing);
+    cudaEventRecord(lc.ev_fork, s);
+    cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
+    k_update<<<lc.grid_sm * 2, UPD_T, 0, lc.side>>>(c);
+    if (lc.ev_branch[1]) record_timing_event(lc.ev_branch[1], lc.side, lc.capturing);
     k_update_warp<<<lc.grid_sm * 8, UW_T, 0, s>>>(c);
     if (lc.ev_branch[2]) record_timing_event(lc.ev_branch[2], s, lc.capturing);
-    k_update<<<lc.grid_sm * 2, UPD_T, 0, s>>>(c);
+    cudaEventRecord(lc.ev_join, lc.side);
+    cudaStreamWaitEvent(s, lc.ev_join, 0);
     *launches += 2;
     return;
   }
