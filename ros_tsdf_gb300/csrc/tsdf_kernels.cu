@@ -1085,53 +1085,45 @@ __global__ void __launch_bounds__(256) k_gather_ranks(Ctx c, cudaGraphConditiona
 
 // One warp per new block, in first-touch order: pop the free list, resolve
 // the pending entry, zero the 4 KiB block (the reference's new VoxelBlock()).
-__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, int rec_passes) {
-  __shared__ long long s_pb[kMaxItems];
-  __shared__ int s_warp[32];
-  const BatchHdr h = *c.hdr;
-  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
-  __syncthreads();
-  const long long n = min(c.ctr->n_new, c.rank_cap);
-  const int lane = threadIdx.x & 31;
-  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  const unsigned* rk = c.rank_key[rank_sel];
-  const unsigned* rv = c.rank_val[rank_sel];
-  for (long long i = wid; i < n; i += nw) {
-    unsigned rank = rk[i];
-    unsigned e = rv[i];
-    long long g = (long long)(rank / (unsigned)h.rank_stride);
-    int item = find_item(s_pb, h.n_items, g);
-    int mi = c.items[item].map;
-    const MapDev& m = c.maps[mi];
-    long long rb = i - c.item_i[item * II_COUNT + II_NEW_BASE];
-    long long bc = c.mctr[mi].block_count;
-    HEntry* en = c.hash + e;
-    if (bc + rb < m.heap_cap) {
-      int slot = c.free_list[m.heap_base + bc + rb];
-      long long phys = m.heap_base + slot;
-      if (lane == 0) {
-        en->slot = slot;
-        en->rank = kRankNone;
-        c.slot_key[phys] = en->key;
-        c.nnz[phys] = 0;
-        atomicMax(&c.mctr[mi].hw, slot + 1);
-        stat_add(c.item_stats, item, ST_NEW, 1);
-      }
-      float4* dst = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
-      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int k = 0; k < kVoxelsPerBlock / 2 / 32; ++k) dst[k * 32 + lane] = z;
-    } else if (lane == 0) {
-      en->key = kTombKey;
-      en->slot = -1;
+// One new block, in rank order (one warp): slot = free_list[block_count +
+// its rank within its item], entry resolved, slot key and count set, 4 KiB
+// zeroed; a full heap tombstones the entry instead.
+__device__ __forceinline__ void alloc_block(const Ctx& c, const long long* s_pb, const BatchHdr& h, long long i,
+                                            unsigned rank, unsigned e, int lane) {
+  long long g = (long long)(rank / (unsigned)h.rank_stride);
+  int item = find_item(s_pb, h.n_items, g);
+  int mi = c.items[item].map;
+  const MapDev& m = c.maps[mi];
+  long long rb = i - c.item_i[item * II_COUNT + II_NEW_BASE];
+  long long bc = c.mctr[mi].block_count;
+  HEntry* en = c.hash + e;
+  if (bc + rb < m.heap_cap) {
+    int slot = c.free_list[m.heap_base + bc + rb];
+    long long phys = m.heap_base + slot;
+    if (lane == 0) {
+      en->slot = slot;
       en->rank = kRankNone;
-      stat_add(c.item_stats, item, ST_HEAPFULL, 1);
+      c.slot_key[phys] = en->key;
+      c.nnz[phys] = 0;
+      atomicMax(&c.mctr[mi].hw, slot + 1);
+      stat_add(c.item_stats, item, ST_NEW, 1);
     }
+    float4* dst = reinterpret_cast<float4*>(c.voxels + phys * kVoxelsPerBlock);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kVoxelsPerBlock / 2 / 32; ++k) dst[k * 32 + lane] = z;
+  } else if (lane == 0) {
+    en->key = kTombKey;
+    en->slot = -1;
+    en->rank = kRankNone;
+    stat_add(c.item_stats, item, ST_HEAPFULL, 1);
   }
-  // the CTA that finishes last: block_count += allocated, and the slot
-  // enumeration bases for publish / gc (items' high waters, prefix-summed)
-  if (!last_cta(&c.ctr->done_alloc)) return;
+}
+
+// After every new block is placed (one CTA): block_count += allocated, and
+// the slot enumeration bases for publish / gc (items' high waters,
+// prefix-summed); which record buffer the sort leaves its output in.
+__device__ __forceinline__ void alloc_finish(const Ctx& c, const BatchHdr& h, int rec_passes, int* s_warp) {
   const int ni = h.n_items;
   long long carry = 0;
   for (int b = 0; b < ni; b += blockDim.x) {
@@ -1161,6 +1153,86 @@ __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, int rec_pass
     c.ctr->rec_skip_last = rec_passes > 1 && !last ? 1 : 0;
     c.ctr->rec_sel = (rec_passes - (c.ctr->rec_skip_last ? 1 : 0)) & 1;
   }
+}
+
+__global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, int rec_passes) {
+  __shared__ long long s_pb[kMaxItems];
+  __shared__ int s_warp[32];
+  const BatchHdr h = *c.hdr;
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const long long n = min(c.ctr->n_new, c.rank_cap);
+  const int lane = threadIdx.x & 31;
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const unsigned* rk = c.rank_key[rank_sel];
+  const unsigned* rv = c.rank_val[rank_sel];
+  for (long long i = wid; i < n; i += nw) alloc_block(c, s_pb, h, i, rk[i], rv[i], lane);
+  if (!last_cta(&c.ctr->done_alloc)) return;
+  alloc_finish(c, h, rec_passes, s_warp);
+}
+
+// The allocation order and the allocation of a small step in one CTA (at
+// most kSmallRank new keys): the new keys' first-touch ranks gathered into
+// shared memory, each item's first new-key index, a bitonic sort by rank
+// (ranks are distinct), then alloc_block per key in rank order and
+// alloc_finish: k_gather_ranks, its sort and k_alloc in one launch.
+constexpr int kAllocT = 1024;
+__global__ void __launch_bounds__(kAllocT) k_alloc_small(Ctx c, int rec_passes) {
+  __shared__ long long s_pb[kMaxItems];
+  __shared__ int s_warp[32];
+  __shared__ unsigned s_k[kSmallRank];
+  __shared__ unsigned s_v[kSmallRank];
+  const BatchHdr h = *c.hdr;
+  const int t = threadIdx.x;
+  for (int i = t; i < h.n_items; i += kAllocT) s_pb[i] = c.items[i].point_base;
+  const long long n_all = c.ctr->n_new;
+  const int n = (int)min(n_all, (long long)kSmallRank);
+  if (t == 0 && n_all > kSmallRank) set_error(c.ctr, ERR_CAPACITY);  // the host picks this path only below the bound
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int i = t; i < P; i += kAllocT) {
+    unsigned k = 0xFFFFFFFFu, v = 0u;  // ranks are below 0xFFFFFFFF, which pads
+    if (i < n) {
+      v = c.newlist[i];
+      k = c.hash[v].rank;
+    }
+    s_k[i] = k, s_v[i] = v;
+  }
+  {
+    const int ni = h.n_items;
+    long long carry = 0;
+    for (int b = 0; b < ni; b += kAllocT) {
+      const int i = b + t;
+      const int v = i < ni ? c.item_i[i * II_COUNT + II_NEW] : 0;
+      int tot;
+      const int ex = block_excl_scan(v, s_warp, &tot);
+      if (i < ni) c.item_i[i * II_COUNT + II_NEW_BASE] = (int)(carry + ex);
+      carry += tot;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = t; i < P; i += kAllocT) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const unsigned a = s_k[i], b2 = s_k[ixj];
+          if ((a > b2) == ((i & k) == 0)) {
+            s_k[i] = b2, s_k[ixj] = a;
+            const unsigned tv = s_v[i];
+            s_v[i] = s_v[ixj], s_v[ixj] = tv;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (t == 0) c.ctr->n_rank_live = n;
+  const int lane = t & 31;
+  for (int i = t >> 5; i < n; i += kAllocT / 32) alloc_block(c, s_pb, h, i, s_k[i], s_v[i], lane);
+  __syncthreads();
+  alloc_finish(c, h, rec_passes, s_warp);
 }
 
 // ----------------------------------------------------------------------------
@@ -3587,6 +3659,7 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
+  if (lc.rank_in_cta && lc.rec_in_cta) return;  // k_alloc_small (the alloc stage) does it all
   const int sel = lc.rank_passes & 1;
   const int pass_launches = 3 * lc.rank_passes;
   k_gather_ranks<<<lc.grid_sm * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing && !lc.rank_in_cta, sel,
@@ -3608,6 +3681,11 @@ void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long l
 
 void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   // (one record pass's parity when k_route_small writes the second buffer)
+  if (lc.rank_in_cta && lc.rec_in_cta) {
+    k_alloc_small<<<1, kAllocT, 0, s>>>(c, 1);
+    *launches += 1;
+    return;
+  }
   k_alloc<<<lc.grid_sm * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_in_cta ? 1 : lc.rec_passes);
   *launches += 1;
 }
