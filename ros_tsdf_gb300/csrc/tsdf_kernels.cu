@@ -1713,20 +1713,26 @@ __global__ void __launch_bounds__(kRouteT) k_route_small(Ctx c) {
     if (h.rec_total > kSmallRecs) set_error(c.ctr, ERR_CAPACITY);  // the host picks this path only below the bound
   }
   __syncthreads();
-  // live records in index order
+  // live records in index order: each thread a contiguous run of at most
+  // kSmallRecs / kRouteT records, one scan of the runs' live counts
   const int n = (int)min(h.rec_total, (long long)kSmallRecs);
   const unsigned* k0 = c.rec_key[0];
-  int m = 0;
+  constexpr int kRun = kSmallRecs / kRouteT;
+  const int per = (n + kRouteT - 1) / kRouteT;  // <= kRun
+  unsigned kr[kRun];
+  int nl = 0;
   unsigned kmax = 0u;
-  for (int b = 0; b < n; b += kRouteT) {
-    const int i = b + t;
-    const unsigned k = i < n ? k0[i] : h.rec_key_limit;
-    const int live = k < h.rec_key_limit ? 1 : 0;
-    int tot;
-    const int ex = block_excl_scan(live, s_warp, &tot);
-    if (live) key_a[m + ex] = k, idx_a[m + ex] = (unsigned short)i, kmax = max(kmax, k);
-    m += tot;
+#pragma unroll
+  for (int u = 0; u < kRun; ++u) {
+    const int i = t * per + u;
+    kr[u] = (u < per && i < n) ? k0[i] : h.rec_key_limit;
+    if (kr[u] < h.rec_key_limit) ++nl, kmax = max(kmax, kr[u]);
   }
+  int m;
+  int pos = block_excl_scan(nl, s_warp, &m);
+#pragma unroll
+  for (int u = 0; u < kRun; ++u)
+    if (kr[u] < h.rec_key_limit) key_a[pos] = kr[u], idx_a[pos] = (unsigned short)(t * per + u), ++pos;
   kmax = __reduce_max_sync(kFull, kmax);
   if (lane == 0) atomicMax(&s_maxk, kmax);
   __syncthreads();
@@ -1782,14 +1788,17 @@ __global__ void __launch_bounds__(kRouteT) k_route_small(Ctx c) {
   unsigned* rk = c.rec_key[1];
   unsigned* rv = c.rec_val[1];
   for (int i = t; i < m; i += kRouteT) rk[i] = key_a[i], rv[i] = v0[idx_a[i]];
+  // segment heads: each thread a contiguous run of the sorted records
   long long nseg = 0;
-  for (int b = 0; b < m; b += kRouteT) {
-    const int i = b + t;
-    const int head = (i < m && (i == 0 || key_a[i] != key_a[i - 1])) ? 1 : 0;
+  {
+    const int pm = (m + kRouteT - 1) / kRouteT;  // <= kRun
+    int nh = 0;
+    for (int i = t * pm; i < min(m, t * pm + pm); ++i) nh += (i == 0 || key_a[i] != key_a[i - 1]) ? 1 : 0;
     int tot;
-    const int ex = block_excl_scan(head, s_warp, &tot);
-    if (head) c.seg_start[nseg + ex] = i;
-    nseg += tot;
+    int at = block_excl_scan(nh, s_warp, &tot);
+    for (int i = t * pm; i < min(m, t * pm + pm); ++i)
+      if (i == 0 || key_a[i] != key_a[i - 1]) c.seg_start[at++] = i;
+    nseg = tot;
   }
   if (t == 0) c.ctr->n_rec_live = m, c.ctr->n_seg = nseg;
   __syncthreads();
