@@ -226,6 +226,33 @@ def test_small_steps_dense_cluster_match_oracle(built, n_points):
         assert_state_equal(eng, mid, orc, 4096)
 
 
+@pytest.mark.parametrize("vs,T,n_points", [(0.05, 1.0, 160), (0.05, 2.4, 80)])
+def test_small_steps_fine_voxels_match_oracle(built, vs, T, n_points):
+    """Small steps of fine voxels: rays of 60 to 150 cells and up to 36 block
+    cells, so the warp-per-point passes walk their DDAs over several 32-cell
+    windows and runs cross the windows' edges (all small-step variants:
+    ranks, allocation and the route stage in one CTA each)."""
+    from ros_tsdf_gb300 import Engine
+    from ros_tsdf_gb300.engine import TsdfParams
+
+    params = TsdfParams(vs, T, 1000.0, 2500.0, 250000.0)
+    heap = 1 << 15
+    orc = _oracle(params, heap)
+    rng = np.random.default_rng(n_points)
+    with Engine(max_maps=2, pool_blocks=heap, max_batch_points=1 << 12, max_routes=params.routes()) as eng:
+        mid = eng.create_map(params, heap)
+        for k in range(4):
+            org = np.array([0.3 + 0.1 * k, -0.2, 0.1], np.float32)
+            # near-diagonal rays (random octant): the most cells per length
+            d = rng.choice([-1.0, 1.0], size=(n_points, 3)) + rng.normal(0.0, 0.05, (n_points, 3))
+            d /= np.linalg.norm(d, axis=1, keepdims=True)
+            xyz = (org + d * rng.uniform(2.0, 6.0, (n_points, 1))).astype(np.float32)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 20)
+            assert r.status == 0
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 20), T, f"step {k}")
+        assert_state_equal(eng, mid, orc, heap)
+
+
 def test_bad_points_empty_scan_and_pcl_stride(built):
     from ros_tsdf_gb300 import Engine, workloads as W
     from ros_tsdf_gb300 import _lib as L
