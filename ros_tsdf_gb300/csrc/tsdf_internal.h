@@ -144,7 +144,6 @@ struct LaneCounters {
   unsigned done_seg;      // CTA tickets of the scans whose last CTA finishes the scan
   unsigned done_enum;
   unsigned done_pub;
-  unsigned done_gc;
   unsigned done_gather;   // k_gather_ranks, k_alloc, k_seg_classify, k_gc_apply: their last CTA
   unsigned done_alloc;    // runs the step's bookkeeping that follows them
   unsigned done_classify;

@@ -3254,32 +3254,28 @@ __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
   }
 }
 
-// The apply level of a scan of an enumeration array (flags -> prefix), then,
-// in the CTA that finishes last, every item's base and count in that prefix
-// (its slots are the enumeration range [SLOT_BASE, SLOT_BASE + SLOT_N)).
+// The apply level of the scans of the enumeration arrays (flags -> prefix):
+// the publish counts always, the collect flags unless k_enum_flags found
+// nothing to collect; then, in the CTA that finishes last, every item's base
+// and count in each prefix (its slots are the enumeration range
+// [SLOT_BASE, SLOT_BASE + SLOT_N)) and, for pinned host outputs, the copy-out
+// plan.  One launch for both scans.
 __device__ void copyout_plan_cta(const Ctx& c, int* s_warp);
 
-__global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, const int* flags, int* prefix, const int* tile_offs,
-                                                     const long long* total, int base_field, int count_field,
-                                                     int stat_field, unsigned* done, int plan_copyout,
-                                                     const int* skip) {
-  __shared__ int s_warp[32];
-  if (skip && *skip) return;
-  const long long n = c.ctr->n_enum;
-  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    int carry = tile_offs[tile];
-    for (int r = 0; r < SC_IPT; ++r) {
-      const long long i = tile * SC_TILE + r * SC_T + threadIdx.x;
-      const int v = i < n ? flags[i] : 0;
-      int tot;
-      const int ex = block_excl_scan(v, s_warp, &tot);
-      if (i < n) prefix[i] = carry + ex;
-      carry += tot;
-    }
+__device__ __forceinline__ void enum_scan_tile(const int* flags, int* prefix, int carry, long long tile, long long n,
+                                               int* s_warp) {
+  for (int r = 0; r < SC_IPT; ++r) {
+    const long long i = tile * SC_TILE + r * SC_T + threadIdx.x;
+    const int v = i < n ? flags[i] : 0;
+    int tot;
+    const int ex = block_excl_scan(v, s_warp, &tot);
+    if (i < n) prefix[i] = carry + ex;
+    carry += tot;
   }
-  if (!last_cta(done)) return;
-  const long long tot = *total;
+}
+
+__device__ __forceinline__ void enum_item_bases(const Ctx& c, const int* prefix, long long tot, long long n,
+                                                int base_field, int count_field, int stat_field) {
   for (int i = threadIdx.x; i < c.hdr->n_items; i += blockDim.x) {
     const long long sb = c.item_i[i * II_COUNT + II_SLOT_BASE];
     const long long se = sb + c.item_i[i * II_COUNT + II_SLOT_N];
@@ -3289,6 +3285,20 @@ __global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, const int* flags, in
     if (count_field >= 0) c.item_i[i * II_COUNT + count_field] = (int)(e - b);
     if (stat_field >= 0) c.item_stats[i * ST_COUNT + stat_field] = e - b;
   }
+}
+
+__global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, int plan_copyout) {
+  __shared__ int s_warp[32];
+  const long long n = c.ctr->n_enum;
+  const bool collect = !c.ctr->gc_skip;
+  const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    enum_scan_tile(c.enum_cnt, c.pub_prefix, c.tile_sums2[tile], tile, n, s_warp);
+    if (collect) enum_scan_tile(c.enum_gc, c.gc_prefix, c.tile_sums3[tile], tile, n, s_warp);
+  }
+  if (!last_cta(&c.ctr->done_pub)) return;
+  enum_item_bases(c, c.pub_prefix, c.ctr->scan_total, n, II_PUB_BASE, -1, ST_PUB);
+  if (collect) enum_item_bases(c, c.gc_prefix, c.ctr->scan_total2, n, II_GC_BASE, II_GC_N, -1);
   if (plan_copyout) {
     __syncthreads();
     copyout_plan_cta(c, s_warp);
@@ -3794,8 +3804,7 @@ void stage_update(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* 
 void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   const int grid = lc.sm_count * 2;
   k_enum_flags<<<lc.sm_count * 4, 256, 0, s>>>(c);
-  k_enum_apply<<<grid, SC_T, 0, s>>>(c, c.enum_cnt, c.pub_prefix, c.tile_sums2, &c.ctr->scan_total, II_PUB_BASE, -1,
-                                     ST_PUB, &c.ctr->done_pub, lc.copyout, nullptr);
+  k_enum_apply<<<grid, SC_T, 0, s>>>(c, lc.copyout);  // the publish prefix and the collect prefix
   *launches += 2;
   if (!lc.copyout) {
     k_pub_write<<<lc.sm_count * 4, 256, 0, s>>>(c, -1);
@@ -3820,16 +3829,11 @@ void stage_publish(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long*
 }
 
 void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  const int grid = lc.sm_count * 2;
-  auto collect = [&](cudaStream_t st) {
-    k_enum_apply<<<grid, SC_T, 0, st>>>(c, c.enum_gc, c.gc_prefix, c.tile_sums3, &c.ctr->scan_total2, II_GC_BASE,
-                                        II_GC_N, -1, &c.ctr->done_gc, 0, &c.ctr->gc_skip);
-    k_gc_apply<<<lc.sm_count * 4, 256, 0, st>>>(c, lc.bucket_size);
-    *launches += 2;
-  };
-  // (they return at once when k_enum_flags found nothing to collect:
-  // cheaper than a conditional node around them, measured)
-  collect(s);
+  // (the collect prefix comes from the publish stage's k_enum_apply;
+  // k_gc_apply returns at once when k_enum_flags found nothing to collect:
+  // cheaper than a conditional node around it, measured)
+  k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
+  *launches += 1;
   if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
   k_step_report<<<1, 256, 0, s>>>(c);
   *launches += 1;
