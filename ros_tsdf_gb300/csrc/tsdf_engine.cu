@@ -692,7 +692,7 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout, variant));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   // the step's stats and counters reach L.h_stats / h_ctr / h_mctr through
-  // k_step_report, the graph's last kernel
+  // the graph's last kernel (k_gc_apply, or k_step_report after a copy-out)
   CK(cudaEventRecord(L.ev_done, L.stream));
   for (int i = 0; i < n; ++i) {
     eng->maps[scans[i].map_id].in_flight = true;

@@ -3499,9 +3499,29 @@ __global__ void __launch_bounds__(256) k_pub_copyout(Ctx c, int part) {
 }
 
 // gc apply: free_list push in ascending slot order, entry tombstoned
-__global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
+// The step's stats and counters into the host's pinned mirrors (one CTA;
+// everything else of the step done).
+__device__ void step_report(const Ctx& c) {
+  const int t = threadIdx.x;
+  const long long ns = (long long)c.hdr->n_items * ST_COUNT;
+  for (long long i = t; i < ns; i += blockDim.x) c.out_stats[i] = __ldcg(c.item_stats + i);
+  const unsigned* src = reinterpret_cast<const unsigned*>(c.ctr);
+  unsigned* dst = reinterpret_cast<unsigned*>(c.out_ctr);
+  for (int i = t; i < (int)(sizeof(LaneCounters) / 4); i += blockDim.x) dst[i] = __ldcg(src + i);
+  const int4* msrc = reinterpret_cast<const int4*>(c.mctr);
+  int4* mdst = reinterpret_cast<int4*>(c.out_mctr);
+  static_assert(sizeof(MapCounters) == sizeof(int4), "map counters copied as one int4");
+  for (int i = t; i < c.n_mctr; i += blockDim.x) mdst[i] = __ldcg(msrc + i);
+}
+
+// report: the step's last kernel also writes the report (device outputs; with
+// pinned host outputs k_step_report follows the copy-out instead).
+__global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size, int report) {
   __shared__ int s_sb[kMaxItems];
-  if (c.ctr->gc_skip) return;  // k_enum_flags found nothing to collect
+  if (c.ctr->gc_skip) {  // k_enum_flags found nothing to collect
+    if (report && blockIdx.x == 0) step_report(c);
+    return;
+  }
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
@@ -3539,20 +3559,16 @@ __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size) {
     c.item_stats[i * ST_COUNT + ST_GC] = g;
     c.item_stats[i * ST_COUNT + ST_BC] = bc;
   }
+  if (report) {
+    __syncthreads();
+    step_report(c);
+  }
 }
 
 // The step's results for the host, written into its pinned mirrors by the
 // graph's last kernel (instead of three copies after the graph): the items'
 // stats, the lane's counters (error flags) and every map's counters.
-__global__ void __launch_bounds__(256) k_step_report(Ctx c) {
-  const int t = threadIdx.x;
-  const long long ns = (long long)c.hdr->n_items * ST_COUNT;
-  for (long long i = t; i < ns; i += blockDim.x) c.out_stats[i] = c.item_stats[i];
-  const unsigned* src = reinterpret_cast<const unsigned*>(c.ctr);
-  unsigned* dst = reinterpret_cast<unsigned*>(c.out_ctr);
-  for (int i = t; i < (int)(sizeof(LaneCounters) / 4); i += blockDim.x) dst[i] = src[i];
-  for (int i = t; i < c.n_mctr; i += blockDim.x) c.out_mctr[i] = c.mctr[i];
-}
+__global__ void __launch_bounds__(256) k_step_report(Ctx c) { step_report(c); }
 
 // ----------------------------------------------------------------------------
 // map maintenance
@@ -3832,11 +3848,15 @@ void stage_gc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* laun
   // (the collect prefix comes from the publish stage's k_enum_apply;
   // k_gc_apply returns at once when k_enum_flags found nothing to collect:
   // cheaper than a conditional node around it, measured)
-  k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size);
+  // (device outputs: k_gc_apply writes the report; pinned host outputs:
+  // k_step_report after the copy-out)
+  k_gc_apply<<<lc.sm_count * 4, 256, 0, s>>>(c, lc.bucket_size, lc.copyout ? 0 : 1);
   *launches += 1;
-  if (lc.copyout) cudaStreamWaitEvent(s, lc.ev_join, 0);
-  k_step_report<<<1, 256, 0, s>>>(c);
-  *launches += 1;
+  if (lc.copyout) {
+    cudaStreamWaitEvent(s, lc.ev_join, 0);
+    k_step_report<<<1, 256, 0, s>>>(c);
+    *launches += 1;
+  }
 }
 
 void launch_map_init(float2* voxels, unsigned long long* slot_key, int* nnz, int* free_list, HEntry* hash,
