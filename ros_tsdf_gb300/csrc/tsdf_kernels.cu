@@ -777,6 +777,23 @@ __device__ __forceinline__ bool last_cta(unsigned* done) {
   return s_last;
 }
 
+// CTAs of a grid-strided loop over n items of `per` each that get any:
+// the others return before they read anything, and last_cta_of counts the
+// tickets of these alone (at least one CTA finishes, even for no items).
+__device__ __forceinline__ unsigned busy_ctas(long long n, long long per) {
+  const long long k = (n + per - 1) / per;
+  return (unsigned)max(1ll, min((long long)gridDim.x, k));
+}
+__device__ __forceinline__ bool last_cta_of(unsigned* done, unsigned ncta) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == ncta - 1;
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
 // Exclusive scan of the tile sums in place by one CTA; returns the total.
 __device__ __forceinline__ long long scan_tile_sums(int* tile_sums, long long ntiles, int* s_warp) {
   long long carry = 0;
@@ -3199,11 +3216,13 @@ __device__ __forceinline__ int find_item_i(const int* base, int n, long long e) 
 __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
   __shared__ int s_sb[kMaxItems];
   __shared__ int s_warp[32];
+  const long long n = c.ctr->n_enum;
+  const unsigned busy = busy_ctas(n, blockDim.x);
+  if (blockIdx.x >= busy) return;  // uniform
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const long long n = c.ctr->n_enum;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long w0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += stride) {
     const long long e = w0 + lane;
@@ -3237,7 +3256,7 @@ __global__ void __launch_bounds__(256) k_enum_flags(Ctx c) {
       if (sg) atomicAdd(&c.tile_sums3[w0 / SC_TILE], sg);
     }
   }
-  if (last_cta(&c.ctr->done_enum)) {
+  if (last_cta_of(&c.ctr->done_enum, busy)) {
     const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
     const long long tp = scan_tile_sums(c.tile_sums2, ntiles, s_warp);
     const long long tg = scan_tile_sums(c.tile_sums3, ntiles, s_warp);
@@ -3290,13 +3309,15 @@ __device__ __forceinline__ void enum_item_bases(const Ctx& c, const int* prefix,
 __global__ void __launch_bounds__(SC_T) k_enum_apply(Ctx c, int plan_copyout) {
   __shared__ int s_warp[32];
   const long long n = c.ctr->n_enum;
+  const unsigned busy = busy_ctas(n, SC_TILE);
+  if (blockIdx.x >= busy) return;  // uniform
   const bool collect = !c.ctr->gc_skip;
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     enum_scan_tile(c.enum_cnt, c.pub_prefix, c.tile_sums2[tile], tile, n, s_warp);
     if (collect) enum_scan_tile(c.enum_gc, c.gc_prefix, c.tile_sums3[tile], tile, n, s_warp);
   }
-  if (!last_cta(&c.ctr->done_pub)) return;
+  if (!last_cta_of(&c.ctr->done_pub, busy)) return;
   enum_item_bases(c, c.pub_prefix, c.ctr->scan_total, n, II_PUB_BASE, -1, ST_PUB);
   if (collect) enum_item_bases(c, c.gc_prefix, c.ctr->scan_total2, n, II_GC_BASE, II_GC_N, -1);
   if (plan_copyout) {
@@ -3522,10 +3543,12 @@ __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size, int re
     if (report && blockIdx.x == 0) step_report(c);
     return;
   }
+  const long long n = c.ctr->n_enum;
+  const unsigned busy = busy_ctas(n, blockDim.x);
+  if (blockIdx.x >= busy) return;  // uniform
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_sb[i] = c.item_i[i * II_COUNT + II_SLOT_BASE];
   __syncthreads();
-  const long long n = c.ctr->n_enum;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
     if (!c.enum_gc[e]) continue;
     int item = find_item_i(s_sb, h.n_items, e);
@@ -3550,7 +3573,7 @@ __global__ void __launch_bounds__(256) k_gc_apply(Ctx c, int bucket_size, int re
     }
   }
   // the CTA that finishes last: block_count -= collected
-  if (!last_cta(&c.ctr->done_gcapply)) return;
+  if (!last_cta_of(&c.ctr->done_gcapply, busy)) return;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) {
     const int mi = c.items[i].map;
     const int g = c.item_i[i * II_COUNT + II_GC_N];
