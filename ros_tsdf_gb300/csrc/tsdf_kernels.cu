@@ -763,27 +763,18 @@ __device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total) {
   return warp_off + x - v;
 }
 
-// True in the CTA that finishes last.  Every thread fences its own writes
-// before its CTA takes a ticket, and the last CTA fences again after taking
-// the last one, so it sees all of them through L2 (it reads them with
-// __ldcg).  All threads of every CTA must call it.
-__device__ __forceinline__ bool last_cta(unsigned* done) {
-  __shared__ bool s_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (s_last) __threadfence();
-  return s_last;
-}
-
-// CTAs of a grid-strided loop over n items of `per` each that get any:
-// the others return before they read anything, and last_cta_of counts the
-// tickets of these alone (at least one CTA finishes, even for no items).
+// CTAs of a grid-strided loop over n items of `per` each that get any: the
+// others return before they read anything (at least one CTA stays, even for
+// no items), and last_cta_of counts the tickets of the busy ones alone.
 __device__ __forceinline__ unsigned busy_ctas(long long n, long long per) {
   const long long k = (n + per - 1) / per;
   return (unsigned)max(1ll, min((long long)gridDim.x, k));
 }
+
+// True in the CTA that finishes last of ncta.  Every thread fences its own
+// writes before its CTA takes a ticket, and the last CTA fences again after
+// taking the last one, so it sees all of them through L2 (it reads them with
+// __ldcg).  All threads of each of the ncta CTAs must call it.
 __device__ __forceinline__ bool last_cta_of(unsigned* done, unsigned ncta) {
   __shared__ bool s_last;
   __threadfence();
@@ -814,8 +805,10 @@ template <class F>
 __global__ void __launch_bounds__(SC_T) k_scan_reduce(F f_in, const long long* n_ptr, int* tile_sums,
                                                       long long* total_out, unsigned* done) {
   __shared__ int s_warp[32];
-  const F f = f_in.bind();
   const long long n = *n_ptr;
+  const unsigned busy = busy_ctas(n, SC_TILE);
+  if (blockIdx.x >= busy) return;  // uniform
+  const F f = f_in.bind();
   const long long ntiles = (n + SC_TILE - 1) / SC_TILE;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int sum = 0;
@@ -827,7 +820,7 @@ __global__ void __launch_bounds__(SC_T) k_scan_reduce(F f_in, const long long* n
     block_excl_scan(sum, s_warp, &tot);
     if (threadIdx.x == 0) tile_sums[tile] = tot;
   }
-  if (last_cta(done)) {
+  if (last_cta_of(done, busy)) {
     const long long tot = scan_tile_sums(tile_sums, ntiles, s_warp);
     if (threadIdx.x == 0) *total_out = tot;
   }
@@ -1046,12 +1039,14 @@ __global__ void __launch_bounds__(256) k_gather_ranks(Ctx c, cudaGraphConditiona
   __shared__ unsigned s_k[kSmallRank];
   __shared__ unsigned s_v[kSmallRank];
   const long long n = min(c.ctr->n_new, c.rank_cap);
+  const unsigned busy = busy_ctas(n, blockDim.x);
+  if (blockIdx.x >= busy) return;  // uniform
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     unsigned e = c.newlist[i];
     c.rank_key[0][i] = c.hash[e].rank;
     c.rank_val[0][i] = e;
   }
-  if (!last_cta(&c.ctr->done_gather)) return;
+  if (!last_cta_of(&c.ctr->done_gather, busy)) return;
   const int ni = c.hdr->n_items;
   long long carry = 0;
   for (int b = 0; b < ni; b += blockDim.x) {
@@ -1175,17 +1170,19 @@ __device__ __forceinline__ void alloc_finish(const Ctx& c, const BatchHdr& h, in
 __global__ void __launch_bounds__(256) k_alloc(Ctx c, int rank_sel, int rec_passes) {
   __shared__ long long s_pb[kMaxItems];
   __shared__ int s_warp[32];
+  const long long n = min(c.ctr->n_new, c.rank_cap);
+  const unsigned busy = busy_ctas(n, blockDim.x >> 5);  // a warp per new block
+  if (blockIdx.x >= busy) return;  // uniform
   const BatchHdr h = *c.hdr;
   for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
   __syncthreads();
-  const long long n = min(c.ctr->n_new, c.rank_cap);
   const int lane = threadIdx.x & 31;
   const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
   const unsigned* rk = c.rank_key[rank_sel];
   const unsigned* rv = c.rank_val[rank_sel];
   for (long long i = wid; i < n; i += nw) alloc_block(c, s_pb, h, i, rk[i], rv[i], lane);
-  if (!last_cta(&c.ctr->done_alloc)) return;
+  if (!last_cta_of(&c.ctr->done_alloc, busy)) return;
   alloc_finish(c, h, rec_passes, s_warp);
 }
 
@@ -1685,12 +1682,14 @@ __device__ __forceinline__ void count_candidate(const Ctx& c, int sj, const unsi
 __global__ void __launch_bounds__(256) k_seg_count(Ctx c) {
   const int rec_sel = c.ctr->rec_sel;  // the sorted records' buffer (set by k_alloc)
   const long long ncand = c.ctr->n_cand;
+  const unsigned busy = busy_ctas(ncand, blockDim.x >> 5);  // a warp per candidate
+  if (blockIdx.x >= busy) return;  // uniform
   const unsigned* rv = c.rec_val[rec_sel];
   const int lane = threadIdx.x & 31;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; k < ncand; k += nwarps)
     count_candidate(c, c.cand[k], rv, lane);
-  if (last_cta(&c.ctr->done_classify)) heavy_plan_cta(c);
+  if (last_cta_of(&c.ctr->done_classify, busy)) heavy_plan_cta(c);
 }
 
 // The route stage of a small step in one CTA (at most kSmallRecs records,
