@@ -186,6 +186,7 @@ struct tsdf_engine {
   tsdf_engine_cfg cfg{};
   int device = 0;
   int sm_count = 0;
+  int prio_high = 0;  // the device's greatest stream priority (the allocation chain's launches)
   std::recursive_mutex mu;
   std::string err;
   // global device state
@@ -271,6 +272,8 @@ LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_p
   lc.staged = staged ? 1 : 0;
   lc.copyout = copyout ? 1 : 0;
   lc.sm_count = eng->sm_count;
+  lc.prio_high = eng->prio_high;
+  lc.walk_ctas = (int)((eng->cfg.max_batch_points + 255) / 256);
   lc.grid_sm = (variant & VAR_SMALL_GRID) ? std::max(1, eng->sm_count / 8) : eng->sm_count;
   lc.rank_in_cta = (variant & VAR_RANK_IN_CTA) ? 1 : 0;
   lc.rec_in_cta = (variant & VAR_REC_IN_CTA) ? 1 : 0;
@@ -341,6 +344,8 @@ tsdf_status lane_init(tsdf_engine* eng, Lane& L) {
     TRY(dalloc(eng, &x.rec_val[i], rec_cap, tr));
   }
   TRY(dalloc(eng, &x.entries, entry_cap, tr));
+  TRY(dalloc(eng, &x.rec_bkey, rec_cap, tr));
+  TRY(dalloc(eng, &x.rec_nruns, npts, tr));
   TRY(dalloc(eng, &x.bin_d, entry_cap, tr));
   TRY(dalloc(eng, &x.heavy, rec_cap, tr));
   TRY(dalloc(eng, &x.bcta, rec_cap, tr));
@@ -468,7 +473,8 @@ tsdf_status launch_pipeline(tsdf_engine* eng, Lane& L, int rank_passes, int rec_
     cudaError_t ce = cudaStreamEndCapture(L.stream, &g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     cudaGraphExec_t ex = nullptr;
-    ce = cudaGraphInstantiate(&ex, g, 0);
+    // per-node priorities: the allocation chain beside the voxel walks
+    ce = cudaGraphInstantiate(&ex, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return fail(eng, TSDF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
     it = L.graphs.emplace(key, ex).first;
@@ -977,6 +983,9 @@ tsdf_status tsdf_engine_create(const tsdf_engine_cfg* cfg_in, tsdf_engine** out)
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess) return TSDF_ERR_CUDA;
   eng->sm_count = sms;
+  int prio_least = 0, prio_greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest) != cudaSuccess) return TSDF_ERR_CUDA;
+  eng->prio_high = prio_greatest;
   if (kernels_init() != cudaSuccess) return TSDF_ERR_CUDA;
   // global state
   eng->hash_pool = c.pool_blocks * 4 + 4096;

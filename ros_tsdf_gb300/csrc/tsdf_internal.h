@@ -197,6 +197,8 @@ struct Ctx {
   unsigned* rank_val[2];
   unsigned* rec_key[2];
   unsigned* rec_val[2];
+  unsigned long long* rec_bkey;  // per route: its block key (k_ray_voxels_keys), made a slot number by k_resolve_records
+  unsigned char* rec_nruns;      // per point: its routes (at most max_routes <= 64)
   uint2* entries;                // per voxel update: (float bits of d, local index)
   int* hist;                     // [256][max_tiles]
   int* digit_tot;                // [256]
@@ -253,6 +255,8 @@ struct LaunchCfg {
   int grid_sm;
   int rank_in_cta;  // at most kSmallRank new keys: no rank passes, no conditional node
   int rec_in_cta;   // at most kSmallRecs records: one CTA runs the route stage (k_route_small)
+  int prio_high;    // launch priority of the allocation chain (beside the voxel walks)
+  int walk_ctas;    // k_ray_voxels_keys' grid: one 256-point CTA per 256 points of the largest batch
   int ray_warp;     // at most kRayWarpPoints points, single-entry buckets: k_ray_blocks_warp, k_ray_voxels_warp
   int bucket_size;   // 1, 2, 4, 8 or 16
   int ray_threads;

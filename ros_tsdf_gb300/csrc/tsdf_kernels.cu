@@ -1563,6 +1563,164 @@ __global__ void __launch_bounds__(kRayWarpT) k_ray_voxels_warp(Ctx c) {
   }
 }
 
+// The voxel pass without the hash table, beside the allocation (the block
+// keys it needs are fixed once the block pass is done): per point the voxel
+// DDA, per voxel an entry {d, local index}, per run of one block a record
+// {block key, entry range} and the point's run count.  k_resolve_records
+// turns the block keys into slot numbers after the allocation.  Entries
+// are written for every run; a run whose block turns out to be missing is
+// corrected there (its updates counted missing, none of them bad, no entries
+// recorded), which gives the counters and records of a pass that looked the
+// blocks up as it went.
+// One CTA per blockDim.x points, a point per thread (no work queue): CTAs
+// retire as their rays end, so the allocation chain's launches, at a higher
+// priority, take SMs as they free up.
+__global__ void __launch_bounds__(256, 3) k_ray_voxels_keys(Ctx c) {
+  __shared__ long long s_pb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  const long long total = h.total_points;
+  if ((long long)blockIdx.x * blockDim.x >= total) return;  // uniform
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const int R = h.rec_stride;
+  const int VS = h.vox_stride;
+  unsigned* rk = c.rec_key[0];
+  unsigned* rv = c.rec_val[0];
+  unsigned long long* rb = c.rec_bkey;
+  uint2* ent = c.entries;
+  {
+    {
+      const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+      const bool active = g < total;
+      int item = active ? find_item(s_pb, h.n_items, g) : 0;
+      const ItemDev& it = c.items[item];
+      const MapDev& m = c.maps[it.map];
+      Seg seg;
+      bool valid = false;
+      float px = 0.f, py = 0.f, pz = 0.f;
+      if (active) {
+        const float* p = reinterpret_cast<const float*>(it.pts + (g - it.point_base) * (long long)it.stride);
+        px = p[0], py = p[1], pz = p[2];
+        valid = make_segment(px, py, pz, it.ox, it.oy, it.oz, m, &seg);
+      }
+      Dda dda;
+      if (valid) dda.init(seg, m.vs, m.scale_v, m.rs_v, m.half_vs, m.vmax);
+      // per-map constants and the origin in registers: the loop's stores
+      // could alias the map and item records as far as the compiler knows
+      const float scale_b = m.scale_b, rs_b = m.rs_b, half_bs = m.half_bs, vs = m.vs, r_vs = m.r_vs;
+      const int rmax = m.rmax;
+      const float ox = it.ox, oy = it.oy, oz = it.oz;
+      const long long rbase = g * (long long)R;
+      const long long ebase = g * (long long)VS;
+      unsigned long long cur = kEmptyKey;
+      int run = -1, run_start = 0, run_cnt = 0, j = 0;
+      float blx = 0.f, bly = 0.f, blz = 0.f;
+      unsigned route_ovf = 0, bad = 0;
+      // (no hash lookups: the lanes walk their rays independently)
+      while (valid) {
+        float x, y, z;
+        int kx, ky, kz;
+        if (!dda.next(&x, &y, &z, &kx, &ky, &kz)) break;
+        const float fbx = floorf(fmul(x, scale_b));
+        const float fby = floorf(fmul(y, scale_b));
+        const float fbz = floorf(fmul(z, scale_b));
+        const unsigned long long bkey = pack_key((int)fbx, (int)fby, (int)fbz);
+        if (bkey != cur) {
+          if (run >= 0 && run < rmax) {
+            rb[rbase + run] = cur;
+            rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
+          }
+          ++run;
+          cur = bkey;
+          run_start = j;
+          run_cnt = 0;
+          // block centre and bottom-left corner (tsdf_handler.cu:612-624)
+          blx = fsub(fadd(div_const(fbx, scale_b, rs_b), half_bs), half_bs);
+          bly = fsub(fadd(div_const(fby, scale_b, rs_b), half_bs), half_bs);
+          blz = fsub(fadd(div_const(fbz, scale_b, rs_b), half_bs), half_bs);
+        }
+        if (run >= rmax) {
+          ++route_ovf;
+        } else if (run_cnt >= 31) {
+          ++bad;  // unreachable: a DDA crosses at most 3*7+1 voxels of one block
+        } else {
+          // getLocalVoxelIndex (tsdf_handler.cu:507-512)
+          const float ix = floorf(div_const(fsub(x, blx), vs, r_vs));
+          const float iy = floorf(div_const(fsub(y, bly), vs, r_vs));
+          const float iz = floorf(div_const(fsub(z, blz), vs, r_vs));
+          unsigned local = kBadLocal;
+          if (ix >= 0.f && ix < 8.f && iy >= 0.f && iy < 8.f && iz >= 0.f && iz < 8.f)
+            local = (unsigned)((int)ix + (int)iy * 8 + (int)iz * 64);
+          else
+            ++bad;
+          const float d = distance_update(x, y, z, px, py, pz, ox, oy, oz);
+          ent[ebase + j] = make_uint2(__float_as_uint(d), local);
+          ++run_cnt;
+        }
+        ++j;
+      }
+      if (active) {
+        if (run >= 0 && run < rmax) {
+          rb[rbase + run] = cur;
+          rv[rbase + run] = ((unsigned)(ebase + run_start) << 5) | (unsigned)run_cnt;
+        }
+        const int first = valid ? min(run + 1, rmax) : 0;
+        c.rec_nruns[g] = (unsigned char)first;
+        for (int r = first; r < R; ++r) rk[rbase + r] = kRecSentinel;
+      }
+      stat_add_warp(c.item_stats, item, ST_VOVF, (valid && dda.ovf) ? 1u : 0u);
+      stat_add_warp(c.item_stats, item, ST_ROVF, route_ovf);
+      stat_add_warp(c.item_stats, item, ST_BADLOCAL, bad);
+    }
+  }
+}
+
+// After the allocation: each point's route block keys (k_ray_voxels_keys)
+// become slot numbers (the item's first slot number plus the block's slot).
+// A block the table does not hold (a block the block DDA did not visit, or
+// one a full heap could not take) gets the empty route: its updates are
+// counted missing, its entries with a bad local index no longer bad, and its
+// record keeps no entries.
+__global__ void __launch_bounds__(256) k_resolve_records(Ctx c, int bucket_size) {
+  __shared__ long long s_pb[kMaxItems];
+  const BatchHdr h = *c.hdr;
+  const long long total = h.total_points;
+  if ((long long)blockIdx.x * blockDim.x >= total) return;  // uniform
+  for (int i = threadIdx.x; i < h.n_items; i += blockDim.x) s_pb[i] = c.items[i].point_base;
+  __syncthreads();
+  const int R = h.rec_stride;
+  unsigned* rk = c.rec_key[0];
+  unsigned* rv = c.rec_val[0];
+  const unsigned long long* rb = c.rec_bkey;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int n = c.rec_nruns[g];
+    if (n == 0) continue;
+    const int item = find_item(s_pb, h.n_items, g);
+    const MapDev& m = c.maps[c.items[item].map];
+    const HEntry* tab = c.hash + m.hash_base;
+    const unsigned mask = m.hash_mask;
+    const long long kbase = c.item_i[item * II_COUNT + II_SLOT_BASE];
+    const long long rbase = g * (long long)R;
+    for (int r = 0; r < n; ++r) {
+      const long long ei = thread_find_entry(tab, mask, bucket_size, rb[rbase + r]);
+      const int slot = ei >= 0 ? tab[ei].slot : -1;
+      if (slot >= 0) {
+        rk[rbase + r] = (unsigned)(kbase + slot);
+      } else {
+        rk[rbase + r] = kRecSentinel;
+        const unsigned v = rv[rbase + r];
+        const unsigned cnt = v & 31u;
+        long long nbad = 0;
+        for (unsigned k = 0; k < cnt; ++k) nbad += c.entries[(v >> 5) + k].y == kBadLocal ? 1 : 0;
+        rv[rbase + r] = v & ~31u;
+        stat_add(c.item_stats, item, ST_MISS, cnt);
+        stat_add(c.item_stats, item, ST_BADLOCAL, -nbad);
+      }
+    }
+  }
+}
+
 // segment heads of the sorted records
 struct SegHeadIn {
   const unsigned* k0;
@@ -3681,6 +3839,24 @@ void launch_check_div(unsigned long long seed, long long n, unsigned long long* 
 
 // ----------------------------------------------------------------------------
 // stage launchers
+
+// A launch at the device's greatest priority: the allocation chain, which
+// runs beside the voxel walks, takes SMs as the walks' CTAs retire.
+template <class... P, class... A>
+void launch_high(const LaunchCfg& lc, cudaStream_t s, dim3 grid, dim3 block, void (*k)(P...), A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = lc.prio_high;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, static_cast<P>(args)...);
+}
+
 cudaError_t kernels_init() {
   cudaError_t e = cudaFuncSetAttribute(k_heavy_update, cudaFuncAttributeMaxDynamicSharedMemorySize, kHuSmem);
   if (e != cudaSuccess) return e;
@@ -3712,15 +3888,21 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
     case 16: k_ray_blocks<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
     default: k_ray_blocks<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
   }
-  *launches += 1;
+  // the voxel walks need no slot numbers: they run on the side stream beside
+  // the allocation order and the allocation; the voxel stage joins them
+  cudaEventRecord(lc.ev_fork, s);
+  cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
+  k_ray_voxels_keys<<<lc.walk_ctas, 256, 0, lc.side>>>(c);
+  cudaEventRecord(lc.ev_join, lc.side);
+  *launches += 2;
 }
 
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
   if (lc.rank_in_cta && lc.rec_in_cta) return;  // k_alloc_small (the alloc stage) does it all
   const int sel = lc.rank_passes & 1;
   const int pass_launches = 3 * lc.rank_passes;
-  k_gather_ranks<<<lc.grid_sm * 2, 256, 0, s>>>(c, lc.cond_rank, lc.capturing && !lc.rank_in_cta, sel,
-                                                pass_launches);
+  launch_high(lc, s, dim3(lc.grid_sm * 2), dim3(256), k_gather_ranks, c, lc.cond_rank,
+              (int)(lc.capturing && !lc.rank_in_cta), sel, pass_launches);
   *launches += 1;
   if (lc.rank_in_cta) return;  // at most kSmallRank new keys: k_gather_ranks' last CTA sorts them
   auto passes = [&](cudaStream_t st) {
@@ -3743,7 +3925,8 @@ void stage_alloc(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* l
     *launches += 1;
     return;
   }
-  k_alloc<<<lc.grid_sm * 4, 256, 0, s>>>(c, lc.rank_passes & 1, lc.rec_in_cta ? 1 : lc.rec_passes);
+  launch_high(lc, s, dim3(lc.grid_sm * 4), dim3(256), k_alloc, c, lc.rank_passes & 1,
+              lc.rec_in_cta ? 1 : lc.rec_passes);
   *launches += 1;
 }
 
@@ -3753,14 +3936,10 @@ void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
     *launches += 1;
     return;
   }
-  const int grid = lc.grid_sm * (2048 / lc.ray_threads);
-  switch (lc.bucket_size) {
-    case 1: k_ray_voxels<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
-    case 2: k_ray_voxels<2><<<grid, lc.ray_threads, 0, s>>>(c); break;
-    case 4: k_ray_voxels<4><<<grid, lc.ray_threads, 0, s>>>(c); break;
-    case 16: k_ray_voxels<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
-    default: k_ray_voxels<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
-  }
+  // the walks (k_ray_voxels_keys, forked after the block pass) joined; their
+  // routes' block keys become slot numbers
+  cudaStreamWaitEvent(s, lc.ev_join, 0);
+  k_resolve_records<<<lc.grid_sm * 8, 256, 0, s>>>(c, lc.bucket_size);
   *launches += 1;
 }
 
