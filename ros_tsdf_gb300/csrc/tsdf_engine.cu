@@ -264,7 +264,7 @@ tsdf_status dalloc(tsdf_engine* eng, T** p, long long count, std::vector<void*>*
 // sized for an eighth of the SMs.
 constexpr long long kSmallBatchPoints = 4096;
 // Pipeline variants a batch's bounds select (bits; each has its own graph).
-enum { VAR_SMALL_GRID = 1, VAR_RANK_IN_CTA = 2, VAR_REC_IN_CTA = 4, VAR_RAY_WARP = 8 };
+enum { VAR_SMALL_GRID = 1, VAR_RANK_IN_CTA = 2, VAR_REC_IN_CTA = 4, VAR_RAY_WARP = 8, VAR_SPLIT_WALK = 16 };
 
 LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_passes, bool staged,
                      bool copyout, int variant) {
@@ -278,6 +278,7 @@ LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_p
   lc.rank_in_cta = (variant & VAR_RANK_IN_CTA) ? 1 : 0;
   lc.rec_in_cta = (variant & VAR_REC_IN_CTA) ? 1 : 0;
   lc.ray_warp = (variant & VAR_RAY_WARP) ? 1 : 0;
+  lc.split_walk = (variant & VAR_SPLIT_WALK) ? 1 : 0;
   lc.bucket_size = eng->cfg.bucket_size;
   lc.ray_threads = eng->cfg.ray_threads;
   lc.rank_passes = rank_passes;
@@ -694,7 +695,10 @@ tsdf_status start_batch(tsdf_engine* eng, Lane& L, int n, const tsdf_scan* scans
   if ((unsigned long long)std::max<long long>(total, 1) * rank_stride <= (unsigned long long)kSmallRank)
     variant |= VAR_RANK_IN_CTA;  // bounds the step's new keys
   if (hdr->rec_total <= kSmallRecs) variant |= VAR_REC_IN_CTA;
-  if (total <= kRayWarpPoints && eng->cfg.bucket_size == 1) variant |= VAR_RAY_WARP;
+  if (total <= kRayWarpPoints && eng->cfg.bucket_size == 1)
+    variant |= VAR_RAY_WARP;
+  else if (total <= kSplitWalkPoints)
+    variant |= VAR_SPLIT_WALK;
   TRY(launch_pipeline(eng, L, rank_passes, rec_passes, chunks > 0, copyout, variant));
   if (L.step_timed) CK(cudaEventRecord(L.ev_step[1], L.stream));
   // the step's stats and counters reach L.h_stats / h_ctr / h_mctr through

@@ -28,6 +28,10 @@ constexpr int kSmallRank = 4096;
 constexpr int kSmallRecs = 8192;
 // Up to this many points, the block and voxel passes run one warp per point.
 constexpr int kRayWarpPoints = 1024;
+// Up to this many points (and above kRayWarpPoints), the voxel walks run
+// beside the allocation; a larger batch's walks outlast the allocation chain
+// by far and its separate slot lookups cost more than the overlap saves.
+constexpr long long kSplitWalkPoints = 1ll << 20;
 
 // One hash entry: packed block key, logical heap slot, first-touch rank.
 // Invariants: slot >= 0 only while the key is live; rank == kRankNone except
@@ -257,6 +261,7 @@ struct LaunchCfg {
   int rec_in_cta;   // at most kSmallRecs records: one CTA runs the route stage (k_route_small)
   int prio_high;    // launch priority of the allocation chain (beside the voxel walks)
   int walk_ctas;    // k_ray_voxels_keys' grid: one 256-point CTA per 256 points of the largest batch
+  int split_walk;   // voxel walks beside the allocation (k_ray_voxels_keys + k_resolve_records)
   int ray_warp;     // at most kRayWarpPoints points, single-entry buckets: k_ray_blocks_warp, k_ray_voxels_warp
   int bucket_size;   // 1, 2, 4, 8 or 16
   int ray_threads;

@@ -3888,13 +3888,15 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
     case 16: k_ray_blocks<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
     default: k_ray_blocks<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
   }
+  *launches += 1;
+  if (!lc.split_walk) return;
   // the voxel walks need no slot numbers: they run on the side stream beside
   // the allocation order and the allocation; the voxel stage joins them
   cudaEventRecord(lc.ev_fork, s);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_ray_voxels_keys<<<lc.walk_ctas, 256, 0, lc.side>>>(c);
   cudaEventRecord(lc.ev_join, lc.side);
-  *launches += 2;
+  *launches += 1;
 }
 
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
@@ -3936,10 +3938,22 @@ void stage_ray_voxels(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
     *launches += 1;
     return;
   }
-  // the walks (k_ray_voxels_keys, forked after the block pass) joined; their
-  // routes' block keys become slot numbers
-  cudaStreamWaitEvent(s, lc.ev_join, 0);
-  k_resolve_records<<<lc.grid_sm * 8, 256, 0, s>>>(c, lc.bucket_size);
+  if (lc.split_walk) {
+    // the walks (k_ray_voxels_keys, forked after the block pass) joined;
+    // their routes' block keys become slot numbers
+    cudaStreamWaitEvent(s, lc.ev_join, 0);
+    k_resolve_records<<<lc.grid_sm * 8, 256, 0, s>>>(c, lc.bucket_size);
+    *launches += 1;
+    return;
+  }
+  const int grid = lc.grid_sm * (2048 / lc.ray_threads);
+  switch (lc.bucket_size) {
+    case 1: k_ray_voxels<1><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 2: k_ray_voxels<2><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 4: k_ray_voxels<4><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    case 16: k_ray_voxels<16><<<grid, lc.ray_threads, 0, s>>>(c); break;
+    default: k_ray_voxels<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
+  }
   *launches += 1;
 }
 
