@@ -605,7 +605,7 @@ def traffic_from_profiles(kernel: str, workload: str):
 STAGE_KERNELS = {
     "update": (["k_hot_chains", "k_heavy_update", "k_update_warp"], "blocks_touched"),
     "publish": (["k_pub_write"], "published_blocks"),
-    "ray_voxels": (["k_ray_voxels"], "n_points"),
+    "ray_voxels": (["k_ray_voxels_keys", "k_resolve_records"], "n_points"),
     "ray_blocks": (["k_ray_blocks"], "n_points"),
 }
 
