@@ -1702,9 +1702,7 @@ __global__ void __launch_bounds__(256) k_resolve_records(Ctx c, int bucket_size)
     const unsigned mask = m.hash_mask;
     const long long kbase = c.item_i[item * II_COUNT + II_SLOT_BASE];
     const long long rbase = g * (long long)R;
-    for (int r = 0; r < n; ++r) {
-      const long long ei = thread_find_entry(tab, mask, bucket_size, rb[rbase + r]);
-      const int slot = ei >= 0 ? tab[ei].slot : -1;
+    auto put = [&](int r, int slot) {
       if (slot >= 0) {
         rk[rbase + r] = (unsigned)(kbase + slot);
       } else {
@@ -1716,6 +1714,28 @@ __global__ void __launch_bounds__(256) k_resolve_records(Ctx c, int bucket_size)
         rv[rbase + r] = v & ~31u;
         stat_add(c.item_stats, item, ST_MISS, cnt);
         stat_add(c.item_stats, item, ST_BADLOCAL, -nbad);
+      }
+    };
+    if (bucket_size == 1) {
+      // single-entry buckets: the keys and then the home entries (key and
+      // slot in one 16-byte load) of up to kResolveBatch routes at once
+      constexpr int kResolveBatch = 8;
+      for (int r0 = 0; r0 < n; r0 += kResolveBatch) {
+        unsigned long long key[kResolveBatch];
+        ulonglong2 home[kResolveBatch];
+#pragma unroll
+        for (int u = 0; u < kResolveBatch; ++u) key[u] = r0 + u < n ? rb[rbase + r0 + u] : 0ull;
+#pragma unroll
+        for (int u = 0; u < kResolveBatch; ++u)
+          home[u] = r0 + u < n ? load_entry_ro(tab + ((unsigned)mix64(key[u]) & mask)) : make_ulonglong2(0ull, 0ull);
+#pragma unroll
+        for (int u = 0; u < kResolveBatch; ++u)
+          if (r0 + u < n) put(r0 + u, probe_resolve(tab, mask, key[u], home[u]));
+      }
+    } else {
+      for (int r = 0; r < n; ++r) {
+        const long long ei = thread_find_entry(tab, mask, bucket_size, rb[rbase + r]);
+        put(r, ei >= 0 ? tab[ei].slot : -1);
       }
     }
   }
