@@ -3909,10 +3909,15 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
     default: k_ray_blocks<8><<<grid, lc.ray_threads, 0, s>>>(c); break;
   }
   *launches += 1;
+  // the voxel walks need no slot numbers: they fork from here onto the side
+  // stream (launched by stage_alloc_order, after the rank gather, whose CTAs
+  // then reach the SMs first) and run beside the allocation order and the
+  // allocation; the voxel stage joins them
+  if (lc.split_walk) cudaEventRecord(lc.ev_fork, s);
+}
+
+void fork_walks(const Ctx& c, const LaunchCfg& lc, long long* launches) {
   if (!lc.split_walk) return;
-  // the voxel walks need no slot numbers: they run on the side stream beside
-  // the allocation order and the allocation; the voxel stage joins them
-  cudaEventRecord(lc.ev_fork, s);
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
   k_ray_voxels_keys<<<lc.walk_ctas, 256, 0, lc.side>>>(c);
   cudaEventRecord(lc.ev_join, lc.side);
@@ -3920,12 +3925,16 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 }
 
 void stage_alloc_order(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long long* launches) {
-  if (lc.rank_in_cta && lc.rec_in_cta) return;  // k_alloc_small (the alloc stage) does it all
+  if (lc.rank_in_cta && lc.rec_in_cta) {  // k_alloc_small (the alloc stage) does it all
+    fork_walks(c, lc, launches);
+    return;
+  }
   const int sel = lc.rank_passes & 1;
   const int pass_launches = 3 * lc.rank_passes;
   launch_high(lc, s, dim3(lc.grid_sm * 2), dim3(256), k_gather_ranks, c, lc.cond_rank,
               (int)(lc.capturing && !lc.rank_in_cta), sel, pass_launches);
   *launches += 1;
+  fork_walks(c, lc, launches);
   if (lc.rank_in_cta) return;  // at most kSmallRank new keys: k_gather_ranks' last CTA sorts them
   auto passes = [&](cudaStream_t st) {
     radix_sort(c, c.rank_key, c.rank_val, &c.ctr->n_new, 0xFFFFFFFFu, &c.ctr->n_rank_live, c.rank_cap,
