@@ -171,6 +171,35 @@ def test_heap_full_matches_oracle(built):
         assert_state_equal(eng, mid, orc, 300)
 
 
+@pytest.mark.parametrize("which,bucket", [("multimap32", 1), ("plain_small", 2)])
+def test_heap_full_on_the_walk_beside_the_allocation(built, which, bucket):
+    """A full heap on the pipeline whose voxel walks run beside the
+    allocation (a 24k-point scan; a small scan with two-entry buckets): the
+    routes of the blocks that found no slot become empty routes after the
+    allocation, their updates counted missing, as the oracle counts them."""
+    from ros_tsdf_gb300 import Engine, workloads as W
+    from ros_tsdf_gb300 import _lib as L
+
+    spec = W.multimap32()[10] if which == "multimap32" else W.plain_small(seed=1)
+    heap = 600 if which == "multimap32" else 300
+    spec = replace(spec, heap_blocks=heap)
+    src = W.ScanSource(spec)
+    orc = _oracle(spec.params, heap)
+    with Engine(max_maps=2, pool_blocks=heap, max_batch_points=1 << 17, bucket_size=bucket) as eng:
+        mid = eng.create_map(spec.params, heap)
+        drops = missing = 0
+        for k in range(3):
+            xyz, org = src.scan(k)
+            r = eng.integrate(mid, xyz, org, pub_cap=1 << 20)
+            assert_scan_equal(r, orc.integrate(xyz, org, pub_cap=1 << 20), spec.params.truncation_distance, f"scan {k}")
+            drops += r.stats["heap_full_drops"]
+            missing += r.stats["missing_updates"]
+            if r.stats["heap_full_drops"]:
+                assert r.status == L.ERR_HEAP_FULL
+        assert drops > 0 and missing > 0
+        assert_state_equal(eng, mid, orc, heap, voxels=False)
+
+
 def test_publish_overflow_truncates(built):
     from ros_tsdf_gb300 import Engine, workloads as W
     from ros_tsdf_gb300 import _lib as L
