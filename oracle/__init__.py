@@ -2,7 +2,7 @@
 
 A sequential restatement of ros_tsdf's algorithm in C++ (tsdf_oracle.cpp),
 used by tests/, __graft_entry__.smoke() and the CPU-baseline legs of
-bench.py as the checker.  The engine never imports it.
+bench.py, to compare results with.  The engine never imports it.
 
 Parity status: pinned to the reference's own code.  ros_tsdf ships no tests
 or golden vectors, so oracle/ref.py compiles its tsdf_handler.cu and

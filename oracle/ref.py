@@ -15,7 +15,7 @@ Recipe and driver for the reference-side parity harness:
   double: its semantics as host code).  Flags: ``-ffp-contract=off`` (no FMA,
   like the oracle and the engine; nvcc would contract the reference's device
   code by default) and ``-fwrapv`` (the hash's int multiply wraps as it does on
-  the GPU).  A machine without the reference sources (the GPU machine) rebuilds the
+  the GPU).  A machine without the reference sources rebuilds the
   programs from the generated copy when it travelled with the repository.
 * ``run()`` feeds scans to a program in a subprocess (a crash in reference code
   cannot take the caller down) and parses what it wrote.

@@ -1,7 +1,7 @@
 // TSDF oracle: a sequential CPU restatement of the ros_tsdf integration call.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the GB300
-// engine in ros_tsdf_gb300/: only tests/, __graft_entry__.smoke() and the
+// TEST INFRASTRUCTURE ONLY.  The GB300 engine in ros_tsdf_gb300/ is compared
+// with this file's results for parity: only tests/, __graft_entry__.smoke() and the
 // CPU-baseline legs of bench.py may load it.  The product never links it.
 //
 // Parity status: PINNED to the reference's own code.  ros_tsdf ships no tests,

@@ -1,7 +1,7 @@
 """The C++ drop-in (include/tsdf_handler.hpp) run on the GPU: a C++ program,
 compiled and linked against libtsdf_gb300.so as a ros_tsdf user would build
 theirs, calls initGlobalVars -> TSDFHandler -> processPointCloudAndUpdateVoxels
-on configs[0] scans given as a PCL-style cloud pointer (16-byte records,
+on plain_small scans (16x64 lidar, 0.5 m voxels) given as a PCL-style cloud pointer (16-byte records,
 tsdf_handler.cuh:50-51) with the in/out publish count zeroed per call, then the
 sub-stage getVoxelBlocks and the container views.  Everything it writes is
 compared with the oracle."""

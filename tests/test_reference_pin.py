@@ -308,7 +308,7 @@ def test_pow_as_host_double(ref_built):
     (promoted to double; its functions compiled as host code) instead of the
     float square.  The allocated block sets and the publish counts stay the
     same; the magnitude and the DDA's first cell move for some rays, so some
-    voxels get different updates.  Measured on configs[0]'s first 8 scans:
+    voxels get different updates.  Measured on the first 8 plain_small scans:
     4957 of 25698 voxels differ, max |dsdf| 2.1e-3 m (5.2e-4 T), max |dW|
     0.49."""
     from oracle import OracleMap
