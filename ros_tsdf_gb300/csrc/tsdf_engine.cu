@@ -273,7 +273,6 @@ LaunchCfg launch_cfg(tsdf_engine* eng, const Lane& L, int rank_passes, int rec_p
   lc.copyout = copyout ? 1 : 0;
   lc.sm_count = eng->sm_count;
   lc.prio_high = eng->prio_high;
-  lc.walk_ctas = (int)((eng->cfg.max_batch_points + 255) / 256);
   lc.grid_sm = (variant & VAR_SMALL_GRID) ? std::max(1, eng->sm_count / 8) : eng->sm_count;
   lc.rank_in_cta = (variant & VAR_RANK_IN_CTA) ? 1 : 0;
   lc.rec_in_cta = (variant & VAR_REC_IN_CTA) ? 1 : 0;

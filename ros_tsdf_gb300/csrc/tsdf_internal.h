@@ -260,7 +260,6 @@ struct LaunchCfg {
   int rank_in_cta;  // at most kSmallRank new keys: no rank passes, no conditional node
   int rec_in_cta;   // at most kSmallRecs records: one CTA runs the route stage (k_route_small)
   int prio_high;    // launch priority of the allocation chain (beside the voxel walks)
-  int walk_ctas;    // k_ray_voxels_keys' grid: one 256-point CTA per 256 points of the largest batch
   int split_walk;   // voxel walks beside the allocation (k_ray_voxels_keys + k_resolve_records)
   int ray_warp;     // at most kRayWarpPoints points, single-entry buckets: k_ray_blocks_warp, k_ray_voxels_warp
   int bucket_size;   // 1, 2, 4, 8 or 16

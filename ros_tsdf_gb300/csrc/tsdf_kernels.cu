@@ -1572,9 +1572,9 @@ __global__ void __launch_bounds__(kRayWarpT) k_ray_voxels_warp(Ctx c) {
 // corrected there (its updates counted missing, none of them bad, no entries
 // recorded), which gives the counters and records of a pass that looked the
 // blocks up as it went.
-// One CTA per blockDim.x points, a point per thread (no work queue): CTAs
-// retire as their rays end, so the allocation chain's launches, at a higher
-// priority, take SMs as they free up.
+// A point per thread, blockDim.x points per chunk, chunks taken in turn by
+// a grid of three CTAs per SM on all but a few SMs (no work queue): slots
+// stay free for the allocation chain's launches beside the walks.
 __global__ void __launch_bounds__(256, 3) k_ray_voxels_keys(Ctx c) {
   __shared__ long long s_pb[kMaxItems];
   const BatchHdr h = *c.hdr;
@@ -1588,9 +1588,9 @@ __global__ void __launch_bounds__(256, 3) k_ray_voxels_keys(Ctx c) {
   unsigned* rv = c.rec_val[0];
   unsigned long long* rb = c.rec_bkey;
   uint2* ent = c.entries;
-  {
+  for (long long cb = blockIdx.x; cb * blockDim.x < total; cb += gridDim.x) {  // uniform
     {
-      const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+      const long long g = cb * blockDim.x + threadIdx.x;
       const bool active = g < total;
       int item = active ? find_item(s_pb, h.n_items, g) : 0;
       const ItemDev& it = c.items[item];
@@ -3919,7 +3919,9 @@ void stage_ray_blocks(const Ctx& c, const LaunchCfg& lc, cudaStream_t s, long lo
 void fork_walks(const Ctx& c, const LaunchCfg& lc, long long* launches) {
   if (!lc.split_walk) return;
   cudaStreamWaitEvent(lc.side, lc.ev_fork, 0);
-  k_ray_voxels_keys<<<lc.walk_ctas, 256, 0, lc.side>>>(c);
+  // three CTAs per SM (their registers) on all but eight SMs: slots stay
+  // free for the allocation chain beside the walks
+  k_ray_voxels_keys<<<std::max(1, 3 * (lc.sm_count - 8)), 256, 0, lc.side>>>(c);
   cudaEventRecord(lc.ev_join, lc.side);
   *launches += 1;
 }
